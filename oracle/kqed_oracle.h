@@ -1,0 +1,51 @@
+/*
+ * ORACLE -- test infrastructure only.
+ *
+ * A CPU restatement, in plain C, of the reference KQED library's kernel path
+ * (QED_kernel_L0..L3 and everything beneath them), following the reference's
+ * portable (non-AVX) code path step for step.  It is the checker for the CUDA
+ * implementation: only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may load it.  The product never calls it.
+ *
+ * Parity is pinned three ways: against the reference library compiled from its
+ * own sources (oracle/Makefile), against the reference's golden regression
+ * files for the table-independent branches (PRECOMP/REGexample2.txt,
+ * REGexample10.txt), and through the reference's identity tests.
+ */
+#ifndef KQED_ORACLE_H
+#define KQED_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Loads LIB_PATH/PRECOMP/{FFxy_single_cksum,taylorx_cksum,taylory_cksum}.bin
+   with checksum validation.  Returns 0 on success. */
+int oracle_load(const char *lib_path);
+void oracle_free(void);
+int oracle_grid(int *nstpx, int *nstpy, double *xlo, double *xhi, double *ylo, double *yhi);
+
+/* out[n][384] = QED_kernel_L<variant>(x[i], y[i]); variant 0..3. */
+int oracle_kernel(int variant, long n, const double *x, const double *y, double *out,
+                  int nthreads);
+
+/* dots[i] = sum_c L<variant>_c(x[i],y[i]) * pi[i][c] */
+int oracle_contract(int variant, long n, const double *x, const double *y, const double *pi,
+                    double *dots, int nthreads);
+
+/* Branch taken by L0(x,y): 0 zero (x=y=0), 1 x=0, 2 y=0, 3 x=y, 4 generic,
+   5 generic with |x| below the grid (Taylor in x); +8 if the x<->(x-y) swap is
+   active; 16 if the kernel is zero because an argument is outside the grid. */
+int oracle_branch(long n, const double *x, const double *y, int *code);
+
+/* The 37 interpolated weight-function values of a generic pair, evaluated at
+   the post-swap invariants (|x|, |y|, cb) inside the grid: the inputs of the
+   learned surrogate.  out[n][37]; returns 0. */
+int oracle_weights(long n, const double *X, const double *Y, const double *CB, double *out,
+                   int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

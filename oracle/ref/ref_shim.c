@@ -1,0 +1,103 @@
+/*
+ * Thin wrapper compiled together with the reference KQED library sources
+ * (test infrastructure only; see oracle/Makefile).  It gives ctypes a flat
+ * interface to the reference's own QED_kernel_L0..L3
+ * (src/LIBFILES/kernels.c:82-177) and initialise/free_QED_temps
+ * (src/LIBFILES/init.c:38,142), without re-declaring struct QED_kernel_temps
+ * on the Python side.
+ */
+#include "KQED.h"
+
+#include <omp.h>
+
+const char *kqedref_lib_path(void)
+{
+  const char *p = getenv("KQEDREF_PATH");
+  return p ? p : ".";
+}
+
+static struct QED_kernel_temps T;
+static int T_ready = 0;
+
+int ref_init(void)
+{
+  if (T_ready) return 0;
+  memset(&T, 0, sizeof(T));
+  if (initialise(&T)) return 1;
+  T_ready = 1;
+  return 0;
+}
+
+void ref_free(void)
+{
+  if (!T_ready) return;
+  free_QED_temps(&T);
+  memset(&T, 0, sizeof(T));
+  T_ready = 0;
+}
+
+int ref_grid_info(int *nstpx, int *nstpy, int *nffa, double *xlo, double *xhi,
+                  double *ylo, double *yhi)
+{
+  if (!T_ready) return 1;
+  *nstpx = T.Grid.nstpx; *nstpy = T.Grid.nstpy; *nffa = T.Grid.Nffa;
+  *xlo = T.Grid.XX[0]; *xhi = T.Grid.XX[T.Grid.nstpx - 1];
+  *ylo = T.Grid.YY[0]; *yhi = T.Grid.YY[T.Grid.nstpy - 1];
+  return 0;
+}
+
+typedef void (*kfun)(const double *, const double *, const struct QED_kernel_temps,
+                     double[6][4][4][4]);
+
+static kfun pick(int variant)
+{
+  switch (variant) {
+  case 0: return (kfun)QED_kernel_L0;
+  case 1: return (kfun)QED_kernel_L1;
+  case 2: return (kfun)QED_kernel_L2;
+  case 3: return (kfun)QED_kernel_L3;
+  default: return NULL;
+  }
+}
+
+/* out[n][384]; pairs spread over OpenMP threads like the reference's own
+   stress test (src/amu_forlattice.c:1419-1429). */
+int ref_kernel(int variant, long n, const double *x, const double *y, double *out,
+               int nthreads)
+{
+  kfun f = pick(variant);
+  if (!T_ready || !f) return 1;
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  long i;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+  for (i = 0; i < n; i++) {
+    double kerv[6][4][4][4] KQED_ALIGN;
+    f(x + 4 * i, y + 4 * i, T, kerv);
+    memcpy(out + 384 * i, kerv, 384 * sizeof(double));
+  }
+  return 0;
+}
+
+/* Fused lattice contraction sum_i L_i(x,y) Pi_i(x,y) over n pairs, the way
+   the reference's example driver contracts a kernel with pihat
+   (src/amu_forlattice.c:100-108).  Returns the per-pair dot products. */
+int ref_contract(int variant, long n, const double *x, const double *y,
+                 const double *pi, double *dots, int nthreads)
+{
+  kfun f = pick(variant);
+  if (!T_ready || !f) return 1;
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  long i;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+  for (i = 0; i < n; i++) {
+    double kerv[6][4][4][4] KQED_ALIGN;
+    f(x + 4 * i, y + 4 * i, T, kerv);
+    const double *k = (const double *)kerv;
+    const double *p = pi + 384 * i;
+    double s = 0.0;
+    int c;
+    for (c = 0; c < 384; c++) s += k[c] * p[c];
+    dots[i] = s;
+  }
+  return 0;
+}

@@ -1,0 +1,109 @@
+"""Generates the golden fixtures under tests/golden/ (run here, where the
+reference sources exist; the fixtures travel, the reference does not).
+
+1. reg_axis.npz -- the table-independent columns of the reference's own
+   regression files (PRECOMP/REGexample2.txt, REGexample10.txt, printed with
+   %lg): kernels with one argument zero, which use only the Taylor tables and
+   the x grid.  Inputs follow src/amu_forlattice.c:119-156 (example2) and
+   :358-379 (example10).
+2. ref_synth.npz -- outputs of the reference library itself (compiled from its
+   own sources by oracle/Makefile, scalar flavour) on the synthetic
+   form-factor table, for seeded pairs covering every branch, plus the table's
+   checksums so a test can confirm the same table is in use.
+
+Usage: python tests/golden/make_golden.py   (needs `make -C oracle ref`)
+"""
+import ctypes
+import os
+import struct
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("KQED_REFERENCE", "/root/reference")
+
+
+def parse_reg(path):
+    """Rows 'rhosig= r mu= m nu= n lda= l v1 v2' -> array [nblocks, 384, 2]."""
+    vals = []
+    for ln in open(path):
+        if ln.startswith("rhosig"):
+            p = ln.split()
+            vals.append((float(p[8]), float(p[9])))
+    v = np.array(vals)
+    return v.reshape(-1, 384, 2)
+
+
+def reg_axis():
+    ex2 = parse_reg(os.path.join(REF, "PRECOMP", "REGexample2.txt"))
+    ex10 = parse_reg(os.path.join(REF, "PRECOMP", "REGexample10.txt"))
+    vi = (1.228, 0.209243, 0.0484223)
+    co, si = np.cos(vi[1]), np.sin(vi[1])
+    yv = np.array([0, 0, 0, vi[2]])
+    xv = np.array([0, 0, vi[0] * si, vi[0] * co])
+    x10 = np.array([0.1, 0.1, 0.1, 0.1])
+    z = np.zeros(4)
+    # (x, y, golden L0(x,y)) for the four table-independent columns
+    cases_x = np.array([z, z, x10, xv])
+    cases_y = np.array([yv, x10, z, z])
+    golden = np.array([ex2[0, :, 1], ex10[0, :, 0], ex10[0, :, 1], ex2[1, :, 1]])
+    np.savez(os.path.join(HERE, "reg_axis.npz"), x=cases_x, y=cases_y, L0=golden)
+
+
+def seeded_pairs():
+    """Seeded pairs that cover every branch of L0."""
+    rng = np.random.default_rng(20240601)
+    gen_x = rng.uniform(-2, 2, (96, 4))
+    gen_y = rng.uniform(-2, 2, (96, 4))
+    d = rng.uniform(-1, 1, (32, 4))
+    s = 10 ** rng.uniform(-6, -3, 32)
+    small = d * s[:, None]
+    other = rng.uniform(-2, 2, (32, 4))
+    xs = [gen_x, small[:16], other[16:]]
+    ys = [gen_y, other[:16], small[16:]]
+    # exact special cases: x=0, y=0, x=y, both zero, far outside the grid
+    big = np.array([[4.0, 4.0, 4.0, 4.0]])
+    sp_x = np.vstack([np.zeros((1, 4)), gen_x[:2], gen_x[2:4], np.zeros((1, 4)), big, gen_x[4:5]])
+    sp_y = np.vstack([gen_y[:1], np.zeros((2, 4)), gen_x[2:4], np.zeros((1, 4)), gen_y[5:6], big])
+    xs.append(sp_x)
+    ys.append(sp_y)
+    # the reference's own example inputs (src/amu_forlattice.c:209-314)
+    fac = 0.046241301098278
+    ex_x = np.array([[1, 1, 1, 1.1], [0.001] * 4, [1 * fac, 3 * fac, 3 * fac, 52 * fac],
+                     [0.001] * 4])
+    ex_y = np.array([[1, 1, 1, 1], [1, 1, 1, 1], [fac] * 4, [0.001, 0.001, 0.001, -0.001]])
+    xs += [ex_x, ex_y]
+    ys += [ex_y, ex_x]
+    return np.vstack(xs), np.vstack(ys)
+
+
+def table_checksums(path):
+    with open(path, "rb") as f:
+        f.seek(-16, os.SEEK_END)
+        return np.array(struct.unpack("<4I", f.read(16)), dtype=np.uint32)
+
+
+def ref_synth():
+    os.environ["KQEDREF_PATH"] = os.path.join(ROOT, "kqed_gb300")
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libkqedref_scalar.so"))
+    assert lib.ref_init() == 0, "reference initialise() failed"
+    dp = ctypes.POINTER(ctypes.c_double)
+    x, y = seeded_pairs()
+    out = {}
+    for v in range(4):
+        o = np.zeros((len(x), 384))
+        lib.ref_kernel(v, len(x), x.ctypes.data_as(dp), y.ctypes.data_as(dp),
+                       o.ctypes.data_as(dp), 1)
+        out["L%d" % v] = o
+    ck = table_checksums(os.path.join(ROOT, "kqed_gb300", "PRECOMP", "FFxy_single_cksum.bin"))
+    np.savez_compressed(os.path.join(HERE, "ref_synth.npz"), x=x, y=y, table_cksum=ck, **out)
+
+
+if __name__ == "__main__":
+    if not os.path.isdir(REF):
+        sys.exit("reference sources not found at %s" % REF)
+    reg_axis()
+    ref_synth()
+    print("wrote", os.listdir(HERE))
