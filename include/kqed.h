@@ -1,0 +1,149 @@
+/*
+ * kqed.h -- C ABI of libkqed_gb300.so, a GB300 (sm_103a) evaluator of KQED's
+ * position-space QED kernel L^{(0..3)}_{[rho sigma]; mu nu lambda}(x, y).
+ *
+ * Part 1 is a drop-in for the reference library's kernel API: the same
+ * structs (field order and sizes unchanged), the same function names,
+ * argument meaning, table files and error behaviour.  A lattice code that
+ * includes the reference's KQED.h and links this library instead gets the
+ * kernel evaluated on the GPU.
+ *
+ * Part 2 adds batched and fused entry points that carry the throughput.
+ * All pointers are plain host or device pointers; no library types appear in
+ * the signatures.  Return value 0 means success; a positive value is an error
+ * code and kqed_last_error() gives the message for the calling thread.
+ */
+#ifndef KQED_GB300_H
+#define KQED_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------
+ * Part 1: reference-compatible API
+ * ---------------------------------------------------------------------- */
+
+/* src/HEADERS/KQED.h:63-67 of the reference.  In this library `Fm` holds the
+   opaque device context and `Fp`, `nmax` are unused. */
+struct AVX_precomps {
+  void *Fm, *Fp;
+  int nmax;
+};
+
+/* src/HEADERS/KQED.h:69-87.  initialise() fills every field exactly as the
+   reference does (grids, ragged Ffm/Ffp coefficient arrays, Taylor tables);
+   PC points at the library's device context. */
+struct Grid_coeffs {
+  int Nffa;
+  float ****Ffp;
+  float ****Ffm;
+  double *XX;
+  double *YY;
+  double xstp;
+  double ystp;
+  int nstpx;
+  int nstpy;
+  double **TX; /* [23][NY_tay] */
+  int NtayX;
+  int NY_tay;
+  double **TY; /* [14][NX_tay] */
+  int NtayY;
+  int NX_tay;
+  struct AVX_precomps *PC;
+  int *nfx;
+};
+
+/* src/HEADERS/KQED.h:90-93.  G8 (the Dirac-trace table used only by the
+   reference's perturbative pion-loop code, not by the kernel) is left NULL. */
+struct QED_kernel_temps {
+  struct Grid_coeffs Grid;
+  int *G8;
+};
+
+/* Replaces initialise(), src/LIBFILES/init.c:142 (declared src/HEADERS/init.h:7).
+   Reads LIB_PATH/PRECOMP/{FFxy_single_cksum,taylorx_cksum,taylory_cksum}.bin,
+   validates their CRC32C checksums, and uploads the tables to the GPU.
+   LIB_PATH is the environment variable KQED_LIB_PATH if set, else the
+   directory the library was built in.  Returns 1 on failure with a message
+   on stderr, 0 on success. */
+int initialise(struct QED_kernel_temps *t);
+
+/* Alias with the name used in the project description. */
+int initialize_QED_kernel_temps(struct QED_kernel_temps *t);
+
+/* Replaces free_QED_temps(), src/LIBFILES/init.c:38 (src/HEADERS/init.h:4). */
+void free_QED_temps(struct QED_kernel_temps *t);
+
+/* Replace QED_kernel_L0..L3, src/LIBFILES/kernels.c:81-177
+   (src/HEADERS/kernels.h:4-33).  kerv is fully overwritten; a pair outside
+   the tabulated grid gives an all-zero kernel, as in the reference.
+   Thread-safe: concurrent callers each get their own stream and staging. */
+void QED_kernel_L0(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                   double kerv[6][4][4][4]);
+void QED_kernel_L1(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                   double kerv[6][4][4][4]);
+void QED_kernel_L2(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                   double kerv[6][4][4][4]);
+void QED_kernel_L3(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                   double kerv[6][4][4][4]);
+
+/* ------------------------------------------------------------------------
+ * Part 2: batched and fused entry points (no counterpart in the reference's
+ * library; they replace the caller-side loop of src/amu_forlattice.c:1419-1429
+ * and the contraction of src/amu_forlattice.c:100-108)
+ * ---------------------------------------------------------------------- */
+
+enum kqed_precision {
+  KQED_FP64 = 0,        /* plain FP64 throughout */
+  KQED_FP32_MIXED = 1,  /* FP32 interpolation/assembly, FP64 where stability needs it */
+  KQED_SURROGATE = 2    /* learned weight functions with interpolation fallback */
+};
+
+/* Per-pair status bits written by the batched calls when status != NULL. */
+enum kqed_status_bits {
+  KQED_ST_OK = 0,
+  KQED_ST_OUT_OF_GRID = 1, /* kernel set to zero, as the reference does */
+  KQED_ST_TAYLOR_X = 2,    /* |x| below the first grid node: Taylor branch */
+  KQED_ST_SWAP = 4,        /* x <-> (x - y) swap branch */
+  KQED_ST_AXIS = 8         /* x = 0, y = 0 or x = y special form */
+};
+
+/* kerv[i][384] = QED_kernel_L<variant>(x[i], y[i]) for i < n, host buffers
+   (x, y: n*4 doubles; kerv: n*384 doubles; status: n bytes or NULL). */
+int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, size_t n, const double *x,
+                      const double *y, double *kerv, uint8_t *status, int precision);
+
+/* Same with device pointers, enqueued on `stream` (a cudaStream_t, NULL for
+   the legacy default stream); returns after enqueueing. */
+int kqed_kernel_batch_dev(const struct QED_kernel_temps *t, int variant, size_t n,
+                          const double *d_x, const double *d_y, double *d_kerv,
+                          uint8_t *d_status, int precision, void *stream);
+
+/* Fused lattice integrand.  For each of nx points x_k and all ny sites y_n:
+     sums[k] = sum_n sum_c L<variant>_c(x_k, y_n) * pi[k][n][c]
+   with pi laid out [nx][ny][384].  Accumulation is FP64 with compensated
+   (Neumaier) summation and a fixed reduction order, so results are
+   reproducible.  Host buffers. */
+int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, size_t nx, const double *x,
+                     size_t ny, const double *y, const double *pi, double *sums, int precision);
+
+/* Same with device pointers on `stream`; d_sums must hold nx doubles. */
+int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t nx,
+                         const double *d_x, size_t ny, const double *d_y, const double *d_pi,
+                         double *d_sums, int precision, void *stream);
+
+/* Message of the last error on the calling thread ("" if none). */
+const char *kqed_last_error(void);
+
+/* Number of this library's GPU kernels launched so far by this process. */
+uint64_t kqed_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

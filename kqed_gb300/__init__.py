@@ -1,0 +1,223 @@
+"""kqed_gb300 -- GB300-native evaluator of KQED's position-space QED kernel.
+
+Python mirror of the reference C API over libkqed_gb300.so (include/kqed.h):
+
+    t = KernelTemps()                  # initialise(&t): load + checksum + upload tables
+    k = QED_kernel_L0(x, y, t)         # one pair, 384 doubles as [6][4][4][4]
+    K = kernel_batch(t, 2, X, Y)       # many pairs, [n][384]
+    s = lattice_sum(t, 2, X, Ysites, Pi)   # fused sum_y L(x,y).Pi(x,y) per x
+    t.free()                           # free_QED_temps(&t)
+
+All arithmetic runs in the CUDA library; there is no CPU fallback.  If the
+library is missing the import of the binding raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libkqed_gb300.so")
+
+KQED_FP64, KQED_FP32_MIXED, KQED_SURROGATE = 0, 1, 2
+ST_OUT_OF_GRID, ST_TAYLOR_X, ST_SWAP, ST_AXIS = 1, 2, 4, 8
+
+
+class AVX_precomps(ctypes.Structure):
+    _fields_ = [("Fm", ctypes.c_void_p), ("Fp", ctypes.c_void_p), ("nmax", ctypes.c_int)]
+
+
+class Grid_coeffs(ctypes.Structure):
+    """struct Grid_coeffs, src/HEADERS/KQED.h:69-87 (layout unchanged)."""
+    _fields_ = [
+        ("Nffa", ctypes.c_int),
+        ("Ffp", ctypes.c_void_p),
+        ("Ffm", ctypes.c_void_p),
+        ("XX", ctypes.POINTER(ctypes.c_double)),
+        ("YY", ctypes.POINTER(ctypes.c_double)),
+        ("xstp", ctypes.c_double),
+        ("ystp", ctypes.c_double),
+        ("nstpx", ctypes.c_int),
+        ("nstpy", ctypes.c_int),
+        ("TX", ctypes.POINTER(ctypes.POINTER(ctypes.c_double))),
+        ("NtayX", ctypes.c_int),
+        ("NY_tay", ctypes.c_int),
+        ("TY", ctypes.POINTER(ctypes.POINTER(ctypes.c_double))),
+        ("NtayY", ctypes.c_int),
+        ("NX_tay", ctypes.c_int),
+        ("PC", ctypes.POINTER(AVX_precomps)),
+        ("nfx", ctypes.POINTER(ctypes.c_int)),
+    ]
+
+
+class QED_kernel_temps(ctypes.Structure):
+    """struct QED_kernel_temps, src/HEADERS/KQED.h:90-93."""
+    _fields_ = [("Grid", Grid_coeffs), ("G8", ctypes.POINTER(ctypes.c_int))]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libkqed_gb300.so not built: run `python -m kqed_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        T = ctypes.POINTER(QED_kernel_temps)
+        L.initialise.argtypes = [T]
+        L.initialise.restype = ctypes.c_int
+        L.free_QED_temps.argtypes = [T]
+        L.free_QED_temps.restype = None
+        for v in range(4):
+            f = getattr(L, "QED_kernel_L%d" % v)
+            f.argtypes = [dp, dp, QED_kernel_temps, dp]
+            f.restype = None
+        L.kqed_kernel_batch.argtypes = [T, ctypes.c_int, ctypes.c_size_t, dp, dp, dp,
+                                        ctypes.POINTER(ctypes.c_uint8), ctypes.c_int]
+        L.kqed_kernel_batch.restype = ctypes.c_int
+        L.kqed_kernel_batch_dev.argtypes = [T, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int, ctypes.c_void_p]
+        L.kqed_kernel_batch_dev.restype = ctypes.c_int
+        L.kqed_lattice_sum.argtypes = [T, ctypes.c_int, ctypes.c_size_t, dp, ctypes.c_size_t, dp,
+                                       dp, dp, ctypes.c_int]
+        L.kqed_lattice_sum.restype = ctypes.c_int
+        L.kqed_lattice_sum_dev.argtypes = [T, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
+                                           ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.kqed_lattice_sum_dev.restype = ctypes.c_int
+        L.kqed_last_error.restype = ctypes.c_char_p
+        L.kqed_launch_count.restype = ctypes.c_uint64
+        _lib = L
+    return _lib
+
+
+class KQEDError(RuntimeError):
+    pass
+
+
+def _check(rc):
+    if rc != 0:
+        raise KQEDError(lib().kqed_last_error().decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _pairs(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.ndim == 1:
+        a = a.reshape(1, 4)
+    if a.ndim != 2 or a.shape[1] != 4:
+        raise ValueError("expected 4-vectors, got shape %s" % (a.shape,))
+    return a
+
+
+class KernelTemps:
+    """Owns a struct QED_kernel_temps; initialise() on construction
+    (src/LIBFILES/init.c:142), free_QED_temps() on free()."""
+
+    def __init__(self, lib_path=None):
+        if lib_path is not None:
+            os.environ["KQED_LIB_PATH"] = lib_path
+        self.t = QED_kernel_temps()
+        if lib().initialise(ctypes.byref(self.t)) != 0:
+            raise KQEDError("initialise failed: " + lib().kqed_last_error().decode())
+
+    @property
+    def ptr(self):
+        return ctypes.byref(self.t)
+
+    def grid(self):
+        g = self.t.Grid
+        return {
+            "nstpx": g.nstpx, "nstpy": g.nstpy,
+            "XX": np.ctypeslib.as_array(g.XX, (g.nstpx,)).copy(),
+            "YY": np.ctypeslib.as_array(g.YY, (g.nstpy,)).copy(),
+            "nfx": np.ctypeslib.as_array(g.nfx, (g.nstpx,)).copy(),
+        }
+
+    def free(self):
+        if self.t.Grid.PC:
+            lib().free_QED_temps(ctypes.byref(self.t))
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _legacy(v, x, y, t):
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(4)
+    y = np.ascontiguousarray(y, dtype=np.float64).reshape(4)
+    out = np.zeros((6, 4, 4, 4))
+    getattr(lib(), "QED_kernel_L%d" % v)(_dptr(x), _dptr(y), t.t, _dptr(out))
+    return out
+
+
+def QED_kernel_L0(x, y, t):
+    """QED_kernel_L0, src/LIBFILES/kernels.c:81-115."""
+    return _legacy(0, x, y, t)
+
+
+def QED_kernel_L1(x, y, t):
+    """QED_kernel_L1, src/LIBFILES/kernels.c:117-134."""
+    return _legacy(1, x, y, t)
+
+
+def QED_kernel_L2(x, y, t):
+    """QED_kernel_L2, src/LIBFILES/kernels.c:136-154."""
+    return _legacy(2, x, y, t)
+
+
+def QED_kernel_L3(x, y, t):
+    """QED_kernel_L3, src/LIBFILES/kernels.c:156-177."""
+    return _legacy(3, x, y, t)
+
+
+def kernel_batch(t, variant, x, y, precision=KQED_FP64, with_status=False):
+    """L<variant>(x[i], y[i]) for all i: returns [n][384] (and [n] status bytes)."""
+    x, y = _pairs(x), _pairs(y)
+    if x.shape != y.shape:
+        raise ValueError("x and y must have the same number of pairs")
+    n = x.shape[0]
+    out = np.empty((n, 384))
+    st = np.zeros(n, dtype=np.uint8) if with_status else None
+    stp = st.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)) if with_status else None
+    _check(lib().kqed_kernel_batch(t.ptr, variant, n, _dptr(x), _dptr(y), _dptr(out), stp,
+                                   precision))
+    return (out, st) if with_status else out
+
+
+def kernel_batch_dev(t, variant, x_ptr, y_ptr, out_ptr, n, precision=KQED_FP64, status_ptr=None,
+                     stream=None):
+    """Device-pointer form (e.g. torch tensor .data_ptr()); enqueued on stream."""
+    _check(lib().kqed_kernel_batch_dev(t.ptr, variant, n, x_ptr, y_ptr, out_ptr, status_ptr,
+                                       precision, stream))
+
+
+def lattice_sum(t, variant, x, ysites, pi, precision=KQED_FP64):
+    """sums[k] = sum_n sum_c L<variant>_c(x_k, y_n) pi[k][n][c]."""
+    x, ysites = _pairs(x), _pairs(ysites)
+    pi = np.ascontiguousarray(pi, dtype=np.float64)
+    if pi.shape != (x.shape[0], ysites.shape[0], 384):
+        raise ValueError("pi must be [nx][ny][384]")
+    sums = np.empty(x.shape[0])
+    _check(lib().kqed_lattice_sum(t.ptr, variant, x.shape[0], _dptr(x), ysites.shape[0],
+                                  _dptr(ysites), _dptr(pi), _dptr(sums), precision))
+    return sums
+
+
+def lattice_sum_dev(t, variant, x_ptr, nx, y_ptr, ny, pi_ptr, sums_ptr, precision=KQED_FP64,
+                    stream=None):
+    _check(lib().kqed_lattice_sum_dev(t.ptr, variant, nx, x_ptr, ny, y_ptr, pi_ptr, sums_ptr,
+                                      precision, stream))
+
+
+def launch_count():
+    return int(lib().kqed_launch_count())

@@ -1,0 +1,1375 @@
+/*
+ * Plain-FP64 evaluation of KQED's kernel L0(x,y) on sm_103a.
+ *
+ * One kernel, three phases, one pair per thread in phase A and one pair per
+ * warp in phases B/C:
+ *
+ *  A (per thread)  invariants, grid position and Hermite weights
+ *                  (set_invariants, src/LIBFILES/getff-new.c:315-370); the 37
+ *                  interpolated weight functions of a generic pair
+ *                  (extractff2/extractff, getff-new.c:213-312) evaluated as
+ *                  33 Clenshaw recurrences run in lockstep over the Chebyshev
+ *                  index on interpolation-weighted combinations of the
+ *                  precomputed node coefficients -- interpolation in x and y is
+ *                  linear, so it is applied to the coefficients before the
+ *                  (linear) Clenshaw sums instead of to 8-16 separate sums;
+ *                  then the scalar parts of chnr_dS/dT/dV
+ *                  (src/LIBFILES/chnr_dS.c, chnr_dT.c, chnr_dV.c) including the
+ *                  x <-> (x-y) chain rule.  Special branches (x=0, y=0, x=y:
+ *                  src/LIBFILES/Tabd.c; |x| below the grid: the TAYLORX
+ *                  branches) follow the reference call by call.  The result is
+ *                  a per-pair record in shared memory.
+ *  B (per warp)    the 200 STV components (Sx, Sy, Tx, Ty, V) of one pair,
+ *                  32 lanes in parallel, from the record.
+ *  C (per warp)    the fixed STV -> 384 linear map (CONSTRUCT_FULL_KERNEL,
+ *                  src/LIBFILES/QED_kernel.c:16-423, or its x=0/y=0 form,
+ *                  QED_kernel_xy0.c:8-399), rows dealt to lanes by length;
+ *                  then either the 384 components are written or they are
+ *                  contracted with Pi(x,y) and reduced (fused lattice sum).
+ *
+ * Everything is FP64.  The kernel is bound by GB300's FP64 pipe.
+ */
+#include "kqed_internal.h"
+
+#include <stdio.h>
+
+namespace kqed {
+
+std::atomic<uint64_t> g_launches{0};
+
+/* Clenshaw ratio constants for derivative orders 1..3 (cheby.c:403-460):
+   order d step j: yb = 2x*Ra[d][j]*yb - Rb[d][j]*ya + c_j */
+__constant__ double cRa[4][kNKMax];
+__constant__ double cRb[4][kNKMax];
+
+int upload_map_constants()
+{
+  double ra[4][kNKMax] = {}, rb[4][kNKMax] = {};
+  for (int j = 0; j < kNKMax; j++) {
+    if (j >= 1) { ra[1][j] = (j + 1) / (double)j; rb[1][j] = (j + 3) / (double)(j + 1); }
+    if (j >= 2) { ra[2][j] = (j + 1) / (double)(j - 1); rb[2][j] = (j + 4) / (double)j; }
+    if (j >= 3) { ra[3][j] = (j + 1) / (double)(j - 2); rb[3][j] = (j + 5) / (double)(j - 1); }
+  }
+  if (cudaMemcpyToSymbol(cRa, ra, sizeof(ra)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(cRb, rb, sizeof(rb)) != cudaSuccess) return 1;
+  return 0;
+}
+
+/* device copies of the table slot / shift maps of kqed_internal.h */
+__constant__ int cSlot[NFFA] = {0, 6, 8, 11, 4, 2, 1, 7, 9, 12, 5, 3, 10, 13};
+__constant__ int cShift[NFFA] = {0, 0, 1, 0, 1, 2, 0, 0, 1, 0, 1, 2, 1, 0};
+
+/* TAYLORX / TAYLORY row names (src/HEADERS/KQED.h:57-60) */
+enum { TYY = 0, G0dy, G0dx, Gl2, Gl2dy, Gl21, Gl21dy, Gl3, Gl3dy, G21, G21dy, G22A, G22B,
+       G22Ady, G22Bdy, G3A, G3B, G3Ady, G3Bdy, G31A, G31B, G31Ady, G31Bdy };
+enum { alpha0dx_0p = 0, alpha0_1p, alpha3_0p, beta2_1p, alpha3_1p, alpha1_0p, beta4_1p,
+       alpha1_1p, alpha1dx_1p, alpha3dx_0p, alpha3dxdx_0p, beta2dx_1p, alpha3dx_1p,
+       alpha1dx_0p };
+
+/* ------------------------------------------------------------ records */
+
+enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4 };
+
+/* generic record (doubles) */
+enum {
+  R_XV = 0, R_YV = 4, R_XH = 8, R_YH = 12, R_C2 = 16, R_C4 = 20,
+  R_X = 24, R_YO = 25, R_CB = 26, R_XSQ = 27, R_YSQ = 28, R_XDY = 29, R_RX = 30, R_RY = 31,
+  R_S = 32,                 /* dg0dx, dg0dy, dg0dcb */
+  R_T = 35,                 /* ell1 ell2 ell3 d1x d1y d1cb d2x d2y d2cb d3x d3y d3cb */
+  R_VD = 47,                /* D1..D8 [4] each */
+  R_VA = 79, R_VB = 83,     /* astuff[4], bstuff[4] */
+  REC = 88
+};
+/* x = 0 record (Tabd_xeq0) */
+enum {
+  X0_Q = 0, X0_QH = 4, X0_YVE = 8, X0_YVL3 = 12, X0_YHD1 = 16, X0_YHD2 = 20, X0_YHD3 = 24,
+  X0_YHG2 = 28, X0_TII = 32, X0_TIII = 36, X0_YA2 = 40, X0_YD12 = 44, X0_PHI1 = 48, X0_PHI2 = 49
+};
+/* y = 0 record (Tabd_yeq0) */
+enum {
+  Y0_X = 0, Y0_XH = 4, Y0_XVE = 8, Y0_XVL1 = 12, Y0_XHD = 16, Y0_TII = 20, Y0_DG0 = 24,
+  Y0_XSQ4 = 28, Y0_D1 = 29, Y0_D2 = 30, Y0_D3 = 31, Y0_D4 = 32
+};
+
+/* ------------------------------------------------------------ helpers */
+
+__device__ __forceinline__ double lerp(double a, double t1, double t2) { return a * t1 + (1.0 - a) * t2; }
+
+/* bsrch, src/LIBFILES/getff-new.c:199-210 */
+__device__ __forceinline__ int bsrch(const double *__restrict__ arr, double t, int lo, int hi)
+{
+  while (hi - lo >= 2) {
+    const int mid = (hi + lo) >> 1;
+    if (__ldg(arr + mid) > t) hi = mid;
+    else lo = mid;
+  }
+  return lo;
+}
+
+struct Herm { double A, B, C1, C2, D, lA; };
+
+/* precompute_INV(x), getff-new.c:30-47 */
+__device__ __forceinline__ Herm herm(double y, double y1, double y2)
+{
+  Herm h;
+  const double dy = y1 - y2, ymy1 = y - y1, ymy2 = y - y2;
+  const double ym2sq = ymy2 * ymy2, ym1sq = ymy1 * ymy1;
+  h.A = -(ym2sq) * (2 * y - 3 * y1 + y2);
+  h.B = (ym1sq) * (2 * y + y1 - 3 * y2);
+  h.C1 = (ymy1) * (ym2sq)*dy;
+  h.C2 = (ym1sq) * (ymy2)*dy;
+  h.D = 1. / (dy * dy * dy);
+  h.lA = (y2 - y) / (y2 - y1);
+  return h;
+}
+
+struct Rc { double a, b; };
+__device__ __forceinline__ void st0(Rc &r, double twox, double c)
+{
+  const double t = fma(twox, r.b, c - r.a);
+  r.a = r.b; r.b = t;
+}
+__device__ __forceinline__ void stn(Rc &r, double A, double mB, double c)
+{
+  const double t = fma(A, r.b, fma(mB, r.a, c));
+  r.a = r.b; r.b = t;
+}
+__device__ __forceinline__ double fin0(const Rc &r, double twox, double c0) { return c0 + fma(twox, r.b, -r.a); }
+
+__device__ __forceinline__ double2 ld2(const double *p) { return __ldg(reinterpret_cast<const double2 *>(p)); }
+
+/* interpolation weights of one generic pair */
+struct Wts {
+  double xA, xB, xC1, xC2, lAx;   /* Hermite in x (D folded in), lerp in x */
+  double yA, yB, yC1, yC2, lAy;   /* Hermite in y, lerp in y */
+  double dd;                      /* 1 when the flag2 y-difference is live, else 0 */
+};
+
+/* Hermite-y of a (value, y-derivative) node pair at iy0/iy1; lerp-y of the
+   y-derivatives; difference of y-derivatives */
+#define HY(a, b) fma(w.yA, (a).x, fma(w.yB, (b).x, fma(w.yC1, (a).y, w.yC2 * (b).y)))
+#define LY(a, b) fma(w.lAy, (a).y - (b).y, (b).y)
+#define HX(f0, f1, g0, g1) fma(w.xA, f0, fma(w.xB, f1, fma(w.xC1, g0, w.xC2 * g1)))
+#define LX(f0, f1) fma(w.lAx, (f0) - (f1), f1)
+
+/* The 37 (+2) weight-function values of a generic pair, W layout:
+   [0..3]   QG0 d0     (d/dcb, d/dx, d/dy, value)   chnr_dS.c:68
+   [4..7]   QL2 d0     [8..11] QL4 d0   [12..15] QG1 d0      chnr_dT.c:299-315
+   [16..19] QG2 d0     [20..23] dxQG2 d0  [24..27] dxQG3 d0
+   [28..31] QG2 d1     [32..35] QG3 d1    [36] QG3 d/dy      chnr_dV.c:383-411
+   [37],[38] y-derivative differences of QG2, QG3 between the two y nodes
+             (the flag2 second y-derivative, chnr_dV.c:444-466) */
+__device__ __noinline__ void interp_generic(const DevTables &T, const double *__restrict__ b00,
+                                            const double *__restrict__ b01,
+                                            const double *__restrict__ b10,
+                                            const double *__restrict__ b11, int Ktop,
+                                            const Wts &w, double twox, double *W)
+{
+  /* ---- pass 1: (QG0,dxQG0) (QL2,dxQL2) (QL4,dxQL4) (QG1,dxQG1) ---- */
+  {
+    Rc A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
+    Rc B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
+    Rc C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
+    Rc D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
+    double fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
+#pragma unroll 1
+    for (int K = Ktop - 1; K >= 0; --K) {
+      const int o = K * kRow;
+      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
+      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
+      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
+#pragma unroll
+      for (int f = 0; f < 4; f++) {
+        const int sn = 2 * (2 * f), sp = 2 * (2 * f + 1);
+        const double2 n00 = ld2(b00 + o + sn), n01 = ld2(b01 + o + sn);
+        const double2 n10 = ld2(b10 + o + sn), n11 = ld2(b11 + o + sn);
+        const double2 p00 = ld2(b00 + o + sp), p01 = ld2(b01 + o + sp);
+        const double2 p10 = ld2(b10 + o + sp), p11 = ld2(b11 + o + sp);
+        const double hN0 = HY(n00, n01), hN1 = HY(n10, n11);
+        const double hP0 = HY(p00, p01), hP1 = HY(p10, p11);
+        const double lN0 = LY(n00, n01), lN1 = LY(n10, n11);
+        const double lP0 = LY(p00, p01), lP1 = LY(p10, p11);
+        const double c3 = HX(hN0, hN1, hP0, hP1);
+        const double c2 = HX(lN0, lN1, lP0, lP1);
+        const double c1 = LX(hP0, hP1);
+        if (f == 0) { /* QG0, shift 0: c3 {0,1}, c2 0, c1 0 */
+          if (K >= 1) { st0(A3o0, twox, c3); st0(A2o0, twox, c2); st0(A1o0, twox, c1); stn(A3o1, A1, mB1, c3); }
+          else { fA3 = fin0(A3o0, twox, c3); fA2 = fin0(A2o0, twox, c2); fA1 = fin0(A1o0, twox, c1); }
+        } else if (f == 1) { /* QL2, shift 2: c3 {2,3}, c2 2, c1 2 */
+          if (K >= 2) { stn(B3o2, A2, mB2, c3); stn(B2o2, A2, mB2, c2); stn(B1o2, A2, mB2, c1); }
+          if (K >= 3) stn(B3o3, A3, mB3, c3);
+        } else if (f == 2) { /* QL4, shift 1: c3 {1,2}, c2 1, c1 1 */
+          if (K >= 1) { stn(C3o1, A1, mB1, c3); stn(C2o1, A1, mB1, c2); stn(C1o1, A1, mB1, c1); }
+          if (K >= 2) stn(C3o2, A2, mB2, c3);
+        } else { /* QG1, shift 0: c3 {0,1}, c2 0, c1 0 */
+          if (K >= 1) { st0(D3o0, twox, c3); st0(D2o0, twox, c2); st0(D1o0, twox, c1); stn(D3o1, A1, mB1, c3); }
+          else { fD3 = fin0(D3o0, twox, c3); fD2 = fin0(D2o0, twox, c2); fD1 = fin0(D1o0, twox, c1); }
+        }
+      }
+    }
+    W[0] = 2.0 * A3o1.b; W[1] = fA1; W[2] = fA2; W[3] = fA3;
+    W[4] = 48.0 * B3o3.b; W[5] = 8.0 * B1o2.b; W[6] = 8.0 * B2o2.b; W[7] = 8.0 * B3o2.b;
+    W[8] = 8.0 * C3o2.b; W[9] = 2.0 * C1o1.b; W[10] = 2.0 * C2o1.b; W[11] = 2.0 * C3o1.b;
+    W[12] = 2.0 * D3o1.b; W[13] = fD1; W[14] = fD2; W[15] = fD3;
+  }
+  /* ---- pass 2: QG2 (8), dxQG2 (9), d2xQG2 (10), QG3 (11), dxQG3 (12), d2xQG3 (13) ---- */
+  {
+    Rc E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
+    Rc F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
+    Rc G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
+    Rc H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
+    double fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
+#pragma unroll 1
+    for (int K = Ktop - 1; K >= 0; --K) {
+      const int o = K * kRow;
+      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
+      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
+      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
+      double hy0[6], hy1[6], ly0[6], ly1[6], dl0[6], dl1[6];
+#pragma unroll
+      for (int s = 0; s < 6; s++) {
+        const int so = 2 * (8 + s);
+        const double2 q00 = ld2(b00 + o + so), q01 = ld2(b01 + o + so);
+        const double2 q10 = ld2(b10 + o + so), q11 = ld2(b11 + o + so);
+        hy0[s] = HY(q00, q01); hy1[s] = HY(q10, q11);
+        ly0[s] = LY(q00, q01); ly1[s] = LY(q10, q11);
+        dl0[s] = q01.y - q00.y; dl1[s] = q11.y - q10.y;
+      }
+      /* s: 0 QG2, 1 dxQG2, 2 d2xQG2, 3 QG3, 4 dxQG3, 5 d2xQG3 */
+      const double e3 = HX(hy0[0], hy1[0], hy0[1], hy1[1]);
+      const double e2 = HX(ly0[0], ly1[0], ly0[1], ly1[1]);
+      const double ed = w.dd * HX(dl0[0], dl1[0], dl0[1], dl1[1]);
+      const double f3 = HX(hy0[1], hy1[1], hy0[2], hy1[2]);
+      const double f2 = HX(ly0[1], ly1[1], ly0[2], ly1[2]);
+      const double f1 = LX(hy0[2], hy1[2]);
+      const double g3 = HX(hy0[4], hy1[4], hy0[5], hy1[5]);
+      const double g2 = HX(ly0[4], ly1[4], ly0[5], ly1[5]);
+      const double g1 = LX(hy0[5], hy1[5]);
+      const double h3 = HX(hy0[3], hy1[3], hy0[4], hy1[4]);
+      const double h2 = HX(ly0[3], ly1[3], ly0[4], ly1[4]);
+      const double hd = w.dd * HX(dl0[3], dl1[3], dl0[4], dl1[4]);
+      if (K >= 1) {
+        stn(E3o1, A1, mB1, e3); stn(E2o1, A1, mB1, e2); stn(Edo1, A1, mB1, ed);
+        stn(F3o1, A1, mB1, f3); stn(F2o1, A1, mB1, f2); stn(F1o1, A1, mB1, f1);
+        st0(G3o0, twox, g3); st0(G2o0, twox, g2); st0(G1o0, twox, g1); stn(G3o1, A1, mB1, g3);
+        stn(H3o1, A1, mB1, h3); st0(H2o0, twox, h2); stn(H2o1, A1, mB1, h2); st0(Hdo0, twox, hd);
+      } else {
+        fG3 = fin0(G3o0, twox, g3); fG2 = fin0(G2o0, twox, g2); fG1 = fin0(G1o0, twox, g1);
+        fH2 = fin0(H2o0, twox, h2); fHd = fin0(Hdo0, twox, hd);
+      }
+      if (K >= 2) {
+        stn(E3o2, A2, mB2, e3); stn(E2o2, A2, mB2, e2); stn(F3o2, A2, mB2, f3); stn(H3o2, A2, mB2, h3);
+      }
+      if (K >= 3) stn(E3o3, A3, mB3, e3);
+    }
+    /* QG2 d0 */ W[16] = 8.0 * E3o2.b; W[17] = 2.0 * F3o1.b; W[18] = 2.0 * E2o1.b; W[19] = 2.0 * E3o1.b;
+    /* dxQG2 d0 */ W[20] = 8.0 * F3o2.b; W[21] = 2.0 * F1o1.b; W[22] = 2.0 * F2o1.b; W[23] = 2.0 * F3o1.b;
+    /* dxQG3 d0 */ W[24] = 2.0 * G3o1.b; W[25] = fG1; W[26] = fG2; W[27] = fG3;
+    /* QG2 d1 */ W[28] = 48.0 * E3o3.b; W[29] = 8.0 * F3o2.b; W[30] = 8.0 * E2o2.b; W[31] = 8.0 * E3o2.b;
+    /* QG3 d1 */ W[32] = 8.0 * H3o2.b; W[33] = 2.0 * G3o1.b; W[34] = 2.0 * H2o1.b; W[35] = 2.0 * H3o1.b;
+    W[36] = fH2;
+    W[37] = 2.0 * Edo1.b; W[38] = fHd;
+  }
+}
+#undef HY
+#undef LY
+#undef HX
+#undef LX
+
+/* --------------------------------------------- single-node access (Taylor) */
+
+/* Clenshaw sum of order d over one node's stored coefficients (cheby.c) */
+__device__ double node_cheb(const double *__restrict__ base, int comp, int NK, int order, double x)
+{
+  const double twox = 2.0 * x;
+  Rc r = {0, 0};
+  if (order == 0) {
+    for (int K = NK - 1; K >= 1; --K) st0(r, twox, __ldg(base + K * kRow + comp));
+    return fin0(r, twox, __ldg(base + comp));
+  }
+  for (int K = NK - 1; K >= order; --K)
+    stn(r, twox * cRa[order][K], -cRb[order][K], __ldg(base + K * kRow + comp));
+  return (order == 1 ? 2.0 : order == 2 ? 8.0 : 48.0) * r.b;
+}
+
+/* accessv, src/LIBFILES/getff-new.c:160-194 */
+__device__ double accessv_d(const DevTables &T, int flag_hy, int use_y_derivs, int ix, int iy,
+                            int nm, int ndy, int ndcb, double cb, double y)
+{
+  const int slot = cSlot[nm];
+  const int order = cShift[nm] + ndcb;
+  const int NK = T.NK;
+  const double *b1 = T.node + ((size_t)ix * T.nstpy + iy) * NK * kRow + 2 * slot;
+  const double y1 = __ldg(T.YY + iy);
+  const double r1d = node_cheb(b1, 1, NK, order, cb);
+  const double r1v = ndy ? r1d : node_cheb(b1, 0, NK, order, cb);
+  if (!flag_hy) {
+    const double *b2 = b1 + (size_t)NK * kRow;
+    const double y2 = __ldg(T.YY + iy + 1);
+    const double r2d = node_cheb(b2, 1, NK, order, cb);
+    const double r2v = ndy ? r2d : node_cheb(b2, 0, NK, order, cb);
+    if (use_y_derivs) {
+      const double dy = y1 - y2;
+      return ((-r1v * (y - y2) * (y - y2) * (2 * y - 3 * y1 + y2) +
+               (y - y1) * (r2v * (y - y1) * (2 * y + y1 - 3 * y2) +
+                           (y - y2) * dy * (r1d * y + r2d * y - r2d * y1 - r1d * y2))) /
+              (dy * dy * dy));
+    }
+    return lerp((y2 - y) / (y2 - y1), r1v, r2v);
+  }
+  return r1v;
+}
+
+/* ------------------------------------------------------------ invariants */
+
+struct Inv {
+  double x, cb, y, xsq, ysq, xdoty, cborig, yorig, xmysq, xmy;
+  int flag2, ix, iy;
+};
+
+/* set_invariants, src/LIBFILES/getff-new.c:315-370 (grid search included) */
+__device__ __forceinline__ void invariants(const DevTables &T, const double *xv, const double *yv,
+                                           Inv &I)
+{
+  const double EPSIN = 1E-7;
+  I.xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
+  I.xsq = I.xsq < EPSIN ? EPSIN : I.xsq;
+  I.x = sqrt(fabs(I.xsq));
+  I.ysq = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
+  I.ysq = I.ysq < EPSIN ? EPSIN : I.ysq;
+  I.y = sqrt(fabs(I.ysq));
+  I.xdoty = xv[0] * yv[0] + xv[1] * yv[1] + xv[2] * yv[2] + xv[3] * yv[3];
+  I.cb = I.xdoty / (I.x * I.y);
+  I.cborig = I.cb;
+  I.yorig = I.y;
+  I.xmysq = (I.xsq + I.ysq) * (1.00000000000001) - 2.0 * I.xdoty;
+  I.xmy = sqrt(fabs(I.xmysq));
+  I.flag2 = 0;
+  const double rx = (I.x > I.xmy ? I.xmy / I.x : I.x / I.xmy);
+  const double rxy = (I.x > I.y ? I.y / I.x : I.x / I.y);
+  if (rx < rxy && I.xmy < __ldg(T.YY + T.nstpy - 1) && fabs(I.xmysq) > 1E-28) {
+    I.cb = (I.x - I.y * I.cb) / I.xmy;
+    I.y = I.xmy;
+    I.flag2 = 1;
+  }
+  I.ix = bsrch(T.XX, I.x, 0, T.nstpx);
+  I.iy = bsrch(T.YY, I.y, 0, T.nstpy);
+}
+
+/* ------------------------------------------- chnr scalar parts (generic) */
+
+struct TS {
+  double ell1, ell2, ell3, d1x, d1y, d1cb, d2x, d2y, d2cb, d3x, d3y, d3cb;
+};
+
+struct VS {
+  double g2, dg1dx, dg1dy, dg1dcb, dg2dx, dg2dy, dg2dcb, dg3dx, dg3dy, dg3dcb;
+  double ddg2dxdx, ddg2dxdy, ddg2dxdcb, ddg2dydcb, ddg2dcbdcb;
+  double ddg3dxdx, ddg3dxdy, ddg3dxdcb, ddg3dydcb, ddg3dcbdcb;
+  double ddg1dxdx, ddg1dxdy, ddg1dxdcb, ddg1dydcb, ddg1dcbdcb;
+  double ddg1dydy, ddg2dydy;
+};
+
+/* chain rule x <-> (x-y), chnr_dS.c:74-83 / chnr_dT.c:240-275 */
+__device__ __forceinline__ void swap3(const Inv &I, double &dx, double &dcb, double &dy)
+{
+  const double ca = I.cb;
+  const double cd = (I.yorig - I.x * I.cborig) / I.xmy;
+  const double ox = dx, ocb = dcb, oy = dy;
+  dx = ox + (1.0 - ca * ca) / I.xmy * ocb + ca * oy;
+  dcb = -(I.ysq * cd * ocb + I.x * I.yorig * I.xmy * oy) / I.xmysq;
+  dy = -(I.cborig + ca * cd) / I.xmy * ocb + cd * oy;
+}
+
+/* generic T scalars from the weights, chnr_dT.c:297-347 */
+__device__ void T_generic(const Inv &I, const double *W, TS &T)
+{
+  const double X = I.x, Y = I.y, cb = I.cb, xsq = I.xsq;
+  const double ysq = I.flag2 ? I.xmysq : I.ysq;
+  T.d2x = W[5]; T.d2y = W[6]; T.ell2 = W[7]; T.d2cb = W[4];
+  const double ell4 = W[11], d4x = W[9], d4y = W[10], d4cb = W[8];
+  const double v1 = W[15], dv1dx = W[13], dv1dy = W[14], dv1dcb = W[12];
+  const double ccq = cb * cb - 0.25;
+  T.ell3 = ell4 / (2.0 * xsq * ysq) - Y * cb * T.ell2 / X;
+  T.ell1 = 4.0 / (3.0 * xsq * xsq) * (v1 - xsq * ysq * ccq * T.ell2 - 1.5 * xsq * X * Y * cb * T.ell3);
+  T.d3y = (-ell4 / (ysq * Y) + d4y / (2.0 * ysq) - cb * X * T.ell2 - Y * X * cb * T.d2y) / (xsq);
+  T.d3cb = (d4cb / (2.0 * X * ysq) - Y * T.ell2 - Y * cb * T.d2cb) / X;
+  T.d3x = (-ell4 / (X * ysq) + d4x / (2.0 * ysq) + Y * cb * T.ell2 - Y * X * cb * T.d2x) / xsq;
+  T.d1y = 4.0 / (3.0 * xsq * xsq) *
+          (dv1dy - 2.0 * xsq * Y * ccq * T.ell2 - xsq * ysq * ccq * T.d2y -
+           1.5 * xsq * X * cb * T.ell3 - 1.5 * xsq * X * Y * cb * T.d3y);
+  T.d1cb = 4.0 / (3.0 * xsq * xsq) *
+           (dv1dcb - 2.0 * xsq * ysq * cb * T.ell2 - xsq * ysq * ccq * T.d2cb -
+            1.5 * xsq * X * Y * T.ell3 - 1.5 * xsq * X * Y * cb * T.d3cb);
+  T.d1x = -4.0 * T.ell1 / X +
+          4.0 / (3.0 * xsq * xsq) *
+              (dv1dx - 2.0 * X * ysq * ccq * T.ell2 - xsq * ysq * ccq * T.d2x -
+               4.5 * xsq * Y * cb * T.ell3 - 1.5 * xsq * X * Y * cb * T.d3x);
+}
+
+/* XMYSWAP_T_contrib, chnr_dT.c:240-275 */
+__device__ void T_swap(const Inv &I, TS &T)
+{
+  swap3(I, T.d2x, T.d2cb, T.d2y);
+  double e3x = -T.d3x, e3cb = -T.d3cb, e3y = -T.d3y;
+  T.ell3 = -T.ell3 - T.ell2;
+  swap3(I, e3x, e3cb, e3y);
+  T.d3x = e3x - T.d2x; T.d3cb = e3cb - T.d2cb; T.d3y = e3y - T.d2y;
+  double e1x = T.d1x, e1cb = T.d1cb, e1y = T.d1y;
+  T.ell1 = T.ell1 - T.ell2 - 2.0 * T.ell3;
+  swap3(I, e1x, e1cb, e1y);
+  T.d1x = e1x - T.d2x - 2.0 * T.d3x;
+  T.d1cb = e1cb - T.d2cb - 2.0 * T.d3cb;
+  T.d1y = e1y - T.d2y - 2.0 * T.d3y;
+}
+
+/* generic V scalars from the weights, chnr_dV.c:380-466 */
+__device__ void V_generic(const Inv &I, const double *W, double ystp, VS &D)
+{
+  const double X = I.x, Y = I.y, cb = I.cb, xsq = I.xsq;
+  D.dg3dy = W[36];
+  D.g2 = W[19]; D.dg2dy = W[18];
+  D.ddg2dxdx = W[21]; D.dg2dx = W[23]; D.ddg2dxdy = W[22]; D.ddg2dxdcb = W[20];
+  D.ddg3dxdx = W[25]; D.dg3dx = W[27]; D.ddg3dxdy = W[26]; D.ddg3dxdcb = W[24];
+  D.dg2dcb = W[31]; D.ddg2dydcb = W[30]; D.ddg2dcbdcb = W[28];
+  D.dg3dcb = W[35]; D.ddg3dydcb = W[34]; D.ddg3dcbdcb = W[32];
+  D.dg1dx = D.dg3dx + Y / xsq * cb * D.g2 - Y / X * cb * D.dg2dx;
+  D.dg1dy = D.dg3dy - cb / X * D.g2 - (Y / X) * cb * D.dg2dy;
+  D.dg1dcb = D.dg3dcb - Y / X * D.g2 - Y / X * cb * D.dg2dcb;
+  D.ddg1dxdx = D.ddg3dxdx - 2.0 * Y / (xsq * X) * cb * D.g2 + Y / xsq * cb * D.dg2dx +
+               Y / xsq * cb * D.dg2dx - Y / X * cb * D.ddg2dxdx;
+  D.ddg1dxdy = D.ddg3dxdy + cb / xsq * D.g2 + Y * cb / xsq * D.dg2dy - cb / X * D.dg2dx -
+               Y / X * cb * D.ddg2dxdy;
+  D.ddg1dxdcb = D.ddg3dxdcb + Y / xsq * D.g2 + Y / xsq * cb * D.dg2dcb - Y / X * D.dg2dx -
+                Y / X * cb * D.ddg2dxdcb;
+  D.ddg1dydcb = D.ddg3dydcb - D.g2 / X - cb / X * D.dg2dcb - Y / X * D.dg2dy -
+                Y / X * cb * D.ddg2dydcb;
+  D.ddg1dcbdcb = D.ddg3dcbdcb - 2.0 * Y / X * D.dg2dcb - Y / X * cb * D.ddg2dcbdcb;
+  D.ddg2dydy = 0.0; D.ddg1dydy = 0.0;
+  if (I.flag2) {
+    D.ddg2dydy = W[37] / ystp;
+    const double ddg3dydy = W[38] / ystp;
+    D.ddg1dydy = ddg3dydy - (Y * D.ddg2dydy + 2.0 * D.dg2dy) * cb / X;
+  }
+}
+
+/* XMYSWAP_V_contrib with v_flip2, chnr_dV.c:176-274 */
+__device__ void V_swap(VS *Dp, double x, double xmy, double y, double xsq, double xmysq,
+                       double ysq, double ca, double cborig)
+{
+  VS &D = *Dp;
+  VS F = D;
+  F.g2 = -D.g2; F.dg2dx = -D.dg2dx; F.dg2dy = -D.dg2dy; F.dg2dcb = -D.dg2dcb;
+  F.ddg2dxdx = -D.ddg2dxdx; F.ddg2dxdy = -D.ddg2dxdy; F.ddg2dydy = -D.ddg2dydy;
+  F.ddg2dxdcb = -D.ddg2dxdcb; F.ddg2dydcb = -D.ddg2dydcb; F.ddg2dcbdcb = -D.ddg2dcbdcb;
+  const double cd = (y - x * cborig) / xmy;
+  const double omc = 1.0 - ca * ca;
+  D.g2 = F.g2;
+  D.dg2dx = F.dg2dx + omc / xmy * F.dg2dcb + ca * F.dg2dy;
+  D.dg2dcb = -(ysq * cd * F.dg2dcb + x * y * xmy * F.dg2dy) / xmysq;
+  D.dg2dy = -(cborig + ca * cd) / xmy * F.dg2dcb + cd * F.dg2dy;
+  D.dg1dx = F.dg1dx + omc / xmy * F.dg1dcb + ca * F.dg1dy - D.dg2dx;
+  D.dg1dcb = -(ysq * cd * F.dg1dcb + x * y * xmy * F.dg1dy) / xmysq - D.dg2dcb;
+  D.dg1dy = -(cborig + ca * cd) / xmy * F.dg1dcb + cd * F.dg1dy - D.dg2dy;
+#define DXDX(g)                                                                                  \
+  ((F.ddg##g##dxdx + omc / xmy * F.ddg##g##dxdcb + ca * F.ddg##g##dxdy) -                        \
+   3.0 * ca * omc / xmysq * F.dg##g##dcb +                                                       \
+   omc / xmy * (F.ddg##g##dxdcb + omc / xmy * F.ddg##g##dcbdcb + ca * F.ddg##g##dydcb) +         \
+   omc / xmy * F.dg##g##dy + ca * (F.ddg##g##dxdy + omc / xmy * F.ddg##g##dydcb + ca * F.ddg##g##dydy))
+#define DXDCB(g)                                                                                 \
+  (ysq / (xmysq * xmy) * (cborig + 3.0 * ca * cd) * F.dg##g##dcb -                                \
+   ysq / xmysq * cd * (F.ddg##g##dxdcb + omc / xmy * F.ddg##g##dcbdcb + ca * F.ddg##g##dydcb) +   \
+   y / xmysq * (x * ca - xmy) * F.dg##g##dy -                                                    \
+   x * y / xmy * (F.ddg##g##dxdy + omc / xmy * F.ddg##g##dydcb + ca * F.ddg##g##dydy))
+#define DXDY(g)                                                                                  \
+  ((-(cborig + ca * cd) / xmy * F.ddg##g##dxdcb + cd * F.ddg##g##dxdy) +                          \
+   (2.0 * ca * cborig + cd * (3.0 * ca * ca - 1.0)) / xmysq * F.dg##g##dcb +                      \
+   omc / xmy * (-(cborig + ca * cd) / xmy * F.ddg##g##dcbdcb + cd * F.ddg##g##dydcb) -            \
+   (cborig + ca * cd) / xmy * F.dg##g##dy +                                                      \
+   ca * (-(cborig + ca * cd) / xmy * F.ddg##g##dydcb + cd * F.ddg##g##dydy))
+#define DYDCB(g)                                                                                 \
+  (y / (xmysq * xmy) * ((3.0 * cd * cd - 1.0) * y - 2 * xmy * cd) * F.dg##g##dcb -                \
+   ysq / (xmysq)*cd * (-(cborig + ca * cd) / xmy * F.ddg##g##dcbdcb + cd * F.ddg##g##dydcb) +     \
+   x / xmysq * (y * cd - xmy) * F.dg##g##dy -                                                    \
+   x * y / xmy * (-(cborig + ca * cd) / xmy * F.ddg##g##dydcb + cd * F.ddg##g##dydy))
+#define DCBDCB(g)                                                                                \
+  (x * ysq / (xmysq * xmysq) * (xmy - 3.0 * y * cd) * F.dg##g##dcb -                              \
+   ysq / (xmysq)*cd * (-(ysq * cd * F.ddg##g##dcbdcb + x * y * xmy * F.ddg##g##dydcb) / xmysq) -  \
+   xsq * ysq / (xmysq * xmy) * F.dg##g##dy -                                                     \
+   x * y / xmy * (-(ysq * cd * F.ddg##g##dydcb + x * y * xmy * F.ddg##g##dydy) / xmysq))
+  D.ddg2dxdx = DXDX(2);
+  D.ddg2dxdcb = DXDCB(2);
+  D.ddg2dxdy = DXDY(2);
+  D.ddg2dydcb = DYDCB(2);
+  D.ddg2dcbdcb = DCBDCB(2);
+  D.ddg1dxdx = DXDX(1) - D.ddg2dxdx;
+  D.ddg1dxdcb = DXDCB(1) - D.ddg2dxdcb;
+  D.ddg1dxdy = DXDY(1) - D.ddg2dxdy;
+  D.ddg1dydcb = DYDCB(1) - D.ddg2dydcb;
+  D.ddg1dcbdcb = DCBDCB(1) - D.ddg2dcbdcb;
+#undef DXDX
+#undef DXDCB
+#undef DXDY
+#undef DYDCB
+#undef DCBDCB
+}
+
+/* ---------------------------------------------------- Taylor-x branches */
+
+/* compute_dg_TAYLORX, chnr_dS.c:9-45 */
+__device__ int S_taylor(const DevTables &T, const Inv &I, double &dg0dy, double &dg0dx,
+                        double &dg0dcb)
+{
+  const int it = bsrch(T.TX, I.y, 0, T.ny_tay);
+  const int iy = bsrch(T.YY, I.y, 0, T.nstpy);
+  if (it == T.ny_tay - 1 || iy == T.nstpy - 1) return 1;
+  const int it2 = it + 1;
+  const double *tyy = T.TX;
+  const double ay = (tyy[it2] - I.y) / (tyy[it2] - tyy[it]);
+  const double xx0 = __ldg(T.XX);
+  const double ax = (xx0 - I.x) / (xx0);
+  const double *g0dx = T.TX + G0dx * T.ny_tay, *g0dy = T.TX + G0dy * T.ny_tay;
+  double f1 = I.cb * lerp(ay, g0dx[it], g0dx[it2]);
+  double f2 = accessv_d(T, 0, 1, 0, iy, dxQG0, 0, 0, I.cb, I.y);
+  dg0dx = lerp(ax, f1, f2);
+  f1 = lerp(ay, g0dy[it], g0dy[it2]);
+  f2 = accessv_d(T, 0, 0, 0, iy, QG0, 1, 0, I.cb, I.y);
+  dg0dy = lerp(ax, f1, f2);
+  f2 = accessv_d(T, 0, 1, 0, iy, QG0, 0, 1, I.cb, I.y);
+  dg0dcb = lerp(ax, 0.0, f2);
+  return 0;
+}
+
+/* TAYLORX_contribution, chnr_dT.c:110-238 */
+__device__ int T_taylor(const DevTables &T, const Inv &I, TS &S)
+{
+  const double ysq = I.flag2 ? I.xmysq : I.ysq;
+  const int it = bsrch(T.TX, I.y, 0, T.ny_tay);
+  const int iy = bsrch(T.YY, I.y, 0, T.nstpy);
+  if (it == T.ny_tay - 1 || iy == T.nstpy - 1) return 1;
+  const int it2 = it + 1;
+  const double Y = I.y, cb = I.cb;
+  const double *tx = T.TX;
+  const int ny = T.ny_tay;
+  const double ay = (tx[it2] - Y) / (tx[it2] - tx[it]);
+  const double xb = __ldg(T.XX);
+  const double ax = (xb - I.x) / (xb);
+  const double xbsq = xb * xb;
+#define TXL(row) lerp(ay, tx[(row)*ny + it], tx[(row)*ny + it2])
+  const double ell2b = accessv_d(T, 0, 1, 0, iy, QL2, 0, 0, cb, Y);
+  S.ell2 = lerp(ax, TXL(Gl2), ell2b);
+  const double dell2bdx = accessv_d(T, 0, 1, 0, iy, dxQL2, 0, 0, cb, Y);
+  S.d2x = lerp(ax, TXL(Gl21) * cb, dell2bdx);
+  const double dell2bdy = accessv_d(T, 0, 0, 0, iy, QL2, 1, 0, cb, Y);
+  S.d2y = lerp(ax, TXL(Gl2dy), dell2bdy);
+  const double dell2bdcb = accessv_d(T, 0, 1, 0, iy, QL2, 0, 1, cb, Y);
+  S.d2cb = lerp(ax, 0.0, dell2bdcb);
+  const double v1b = accessv_d(T, 0, 1, 0, iy, QG1, 0, 0, cb, Y);
+  const double dv1bdx = accessv_d(T, 0, 1, 0, iy, dxQG1, 0, 0, cb, Y);
+  const double dv1bdy = accessv_d(T, 0, 0, 0, iy, QG1, 1, 0, cb, Y);
+  const double dv1bdcb = accessv_d(T, 0, 1, 0, iy, QG1, 0, 1, cb, Y);
+  const double ell4b = accessv_d(T, 0, 1, 0, iy, QL4, 0, 0, cb, Y);
+  const double dell4bdx = accessv_d(T, 0, 1, 0, iy, dxQL4, 0, 0, cb, Y);
+  const double dell4bdy = accessv_d(T, 0, 0, 0, iy, QL4, 1, 0, cb, Y);
+  const double dell4bdcb = accessv_d(T, 0, 1, 0, iy, QL4, 0, 1, cb, Y);
+  const double ell3b = ell4b / (2.0 * xbsq * ysq) - Y * cb * ell2b / xb;
+  S.ell3 = lerp(ax, TXL(Gl3), ell3b);
+  const double ell1b = 4.0 / (3.0 * xbsq * xbsq) *
+                       (v1b - xbsq * ysq * (cb * cb - 0.25) * ell2b - 1.5 * xbsq * xb * Y * cb * ell3b);
+  S.ell1 = ell1b;
+  const double dell3bdy =
+      (-ell4b / (ysq * Y) + dell4bdy / (2.0 * ysq) - cb * xb * ell2b - Y * xb * cb * dell2bdy) / (xbsq);
+  S.d3y = lerp(ax, TXL(Gl3dy), dell3bdy);
+  const double dell3bdcb = (dell4bdcb / (2.0 * xb * ysq) - Y * ell2b - Y * cb * dell2bdcb) / xb;
+  S.d3cb = lerp(ax, 0.0, dell3bdcb);
+  const double dell3bdx =
+      (-ell4b / (xb * ysq) + dell4bdx / (2.0 * ysq) + Y * cb * ell2b - Y * xb * cb * dell2bdx) / xbsq;
+  S.d3x = dell3bdx;
+  S.d1y = 4.0 / (3.0 * xbsq * xbsq) *
+          (dv1bdy - 2.0 * xbsq * Y * (cb * cb - 0.25) * ell2b - xbsq * ysq * (cb * cb - 0.25) * dell2bdy -
+           1.5 * xbsq * xb * cb * ell3b - 1.5 * xbsq * xb * Y * cb * dell3bdy);
+  S.d1cb = 4.0 / (3.0 * xbsq * xbsq) *
+           (dv1bdcb - 2.0 * xbsq * ysq * cb * ell2b - xbsq * ysq * (cb * cb - 0.25) * dell2bdcb -
+            1.5 * xbsq * xb * Y * ell3b - 1.5 * xbsq * xb * Y * cb * dell3bdcb);
+  S.d1x = -4.0 * ell1b / xb +
+          4.0 / (3.0 * xbsq * xbsq) *
+              (dv1bdx - 2.0 * xb * ysq * (cb * cb - 0.25) * ell2b - xbsq * ysq * (cb * cb - 0.25) * dell2bdx -
+               4.5 * xbsq * Y * cb * ell3b - 1.5 * xbsq * xb * Y * cb * dell3bdx);
+#undef TXL
+  return 0;
+}
+
+/* taylorx_contrib, chnr_dV.c:18-174 */
+__device__ int V_taylor(const DevTables &T, VS &D, double x, double y, double xsq, int flag2,
+                        double cb)
+{
+  const int it = bsrch(T.TX, y, 0, T.ny_tay);
+  const int iy = bsrch(T.YY, y, 0, T.nstpy);
+  if (it == T.ny_tay - 1 || iy == T.nstpy - 1) return 1;
+  const int it2 = it + 1;
+  const double *tx = T.TX;
+  const int ny = T.ny_tay;
+  const double ay = (tx[it2] - y) / (tx[it2] - tx[it]);
+  const double xb = __ldg(T.XX);
+  const double ax = (xb - x) / (xb);
+  const double xbsq = xb * xb;
+#define TXL(row) lerp(ay, tx[(row)*ny + it], tx[(row)*ny + it2])
+  const double g2b = accessv_d(T, 0, 1, 0, iy, QG2, 0, 0, cb, y);
+  D.g2 = lerp(ax, 0.0, g2b);
+  const double ddg2bdxdcb = accessv_d(T, 0, 1, 0, iy, dxQG2, 0, 1, cb, y);
+  D.ddg2dxdcb = lerp(ax, TXL(G21), ddg2bdxdcb);
+  const double dg2bdx = accessv_d(T, 0, 1, 0, iy, dxQG2, 0, 0, cb, y);
+  D.dg2dx = D.ddg2dxdcb * cb;
+  const double dg2bdcb = accessv_d(T, 0, 1, 0, iy, QG2, 0, 1, cb, y);
+  D.dg2dcb = D.ddg2dxdcb * x;
+  const double dg2bdy = accessv_d(T, 0, 0, 0, iy, QG2, 1, 0, cb, y);
+  D.dg2dy = lerp(ax, 0.0, dg2bdy);
+  const double ddg2bdxdy = accessv_d(T, 0, 0, 0, iy, dxQG2, 1, 0, cb, y);
+  D.ddg2dxdy = lerp(ax, cb * TXL(G21dy), ddg2bdxdy);
+  const double ddg2adxdx = 2.0 * (TXL(G22A) + TXL(G22B) * (0.4 + 0.6 * (2.0 * cb * cb - 1)));
+  const double ddg2bdxdx = accessv_d(T, 0, 1, 0, iy, d2xQG2, 0, 0, cb, y);
+  D.ddg2dxdx = lerp(ax, ddg2adxdx, ddg2bdxdx);
+  const double ddg2bdcbdcb = accessv_d(T, 0, 1, 0, iy, QG2, 0, 2, cb, y);
+  D.ddg2dcbdcb = ddg2bdcbdcb * xsq / xbsq;
+  const double ddg2bdydcb = accessv_d(T, 0, 0, 0, iy, QG2, 1, 1, cb, y);
+  D.ddg2dydcb = lerp(ax, 0.0, ddg2bdydcb);
+  const double dg3bdy = accessv_d(T, 0, 0, 0, iy, QG3, 1, 0, cb, y);
+  const double ddg3bdxdy = accessv_d(T, 0, 0, 0, iy, dxQG3, 1, 0, cb, y);
+  const double ddg3bdxdcb = accessv_d(T, 0, 1, 0, iy, dxQG3, 0, 1, cb, y);
+  const double ddg3bdxdx = accessv_d(T, 0, 1, 0, iy, d2xQG3, 0, 0, cb, y);
+  const double ddg3bdcbdcb = accessv_d(T, 0, 1, 0, iy, QG3, 0, 2, cb, y);
+  const double ddg3bdydcb = accessv_d(T, 0, 0, 0, iy, QG3, 1, 1, cb, y);
+  const double dg1bdy = dg3bdy - cb / xb * g2b - (y / xb) * cb * dg2bdy;
+  const double ddg1bdxdx = ddg3bdxdx - 2.0 * y / (xbsq * xb) * cb * g2b + y / xbsq * cb * dg2bdx +
+                           y / xbsq * cb * dg2bdx - y / xb * cb * ddg2bdxdx;
+  const double ddg1bdxdy = ddg3bdxdy + cb / xbsq * g2b + y * cb / xbsq * dg2bdy - cb / xb * dg2bdx -
+                           y / xb * cb * ddg2bdxdy;
+  const double ddg1bdxdcb = ddg3bdxdcb + y / xbsq * g2b + y / xbsq * cb * dg2bdcb - y / xb * dg2bdx -
+                            y / xb * cb * ddg2bdxdcb;
+  const double ddg1bdydcb = ddg3bdydcb - g2b / xb - cb / xb * dg2bdcb - y / xb * dg2bdy -
+                            y / xb * cb * ddg2bdydcb;
+  const double ddg1bdcbdcb = ddg3bdcbdcb - 2.0 * y / xb * dg2bdcb - y / xb * cb * ddg2bdcbdcb;
+  const double dg1ady = TXL(G3Ady) - TXL(G3Bdy);
+  const double ddg1adxdy = cb * (TXL(G31Ady) - (2 / 3.) * TXL(G31Bdy) - TXL(G22A) - y * TXL(G22Ady));
+  const double ddg1adxdcb = TXL(G31A) - (2 / 3.) * TXL(G31B) - y * TXL(G22A);
+  D.ddg1dxdcb = lerp(ax, ddg1adxdcb, ddg1bdxdcb);
+  D.dg1dx = D.ddg1dxdcb * cb;
+  D.dg1dcb = D.ddg1dxdcb * x;
+  D.dg1dy = lerp(ax, dg1ady, dg1bdy);
+  D.ddg1dxdy = lerp(ax, ddg1adxdy, ddg1bdxdy);
+  D.ddg1dxdx = lerp(ax, ddg1bdxdx, ddg1bdxdx);
+  D.ddg1dcbdcb = ddg1bdcbdcb * xsq / xbsq;
+  D.ddg1dydcb = lerp(ax, 0.0, ddg1bdydcb);
+  D.ddg2dydy = 0.0; D.ddg1dydy = 0.0;
+  if (flag2) {
+    const double ya = __ldg(T.YY + iy), ybn = __ldg(T.YY + iy + 1);
+    const double ystp = T.ystp;
+    const double dg2bdy_ya = accessv_d(T, 0, 0, 0, iy, QG2, 1, 0, cb, ya);
+    const double dg2bdy_yb = accessv_d(T, 0, 0, 0, iy, QG2, 1, 0, cb, ybn);
+    const double ddg2bdydy = (dg2bdy_yb - dg2bdy_ya) / ystp;
+    D.ddg2dydy = ax * 0.0 + (1.0 - ax) * ddg2bdydy;
+    const double ddg1adydy = (tx[G3Ady * ny + it2] - tx[G3Bdy * ny + it2] -
+                              (tx[G3Ady * ny + it] - tx[G3Bdy * ny + it])) / (tx[it2] - tx[it]);
+    const double dg3bdy_ya = accessv_d(T, 0, 0, 0, iy, QG3, 1, 0, cb, ya);
+    const double dg3bdy_yb = accessv_d(T, 0, 0, 0, iy, QG3, 1, 0, cb, ybn);
+    const double ddg3bdydy = (dg3bdy_yb - dg3bdy_ya) / ystp;
+    const double ddg1bdydy = ddg3bdydy - (y * ddg2bdydy + 2.0 * dg2bdy) * cb / x;
+    D.ddg1dydy = ax * ddg1adydy + (1.0 - ax) * ddg1bdydy;
+  }
+#undef TXL
+  return 0;
+}
+
+/* --------------------------------------------------- records (phase A) */
+
+/* everything phase B needs about a generic pair, given its S/T/V scalars
+   (post swap): the per-index vectors of chnr_dS/dT loops and get_dv
+   (chnr_dV.c:277-325) */
+__device__ void fill_generic_record(double *R, const double *xv, const double *yv, const Inv &I,
+                                    double dg0dx, double dg0dy, double dg0dcb, const TS &T,
+                                    const VS &D)
+{
+  const double x = I.x, y = I.yorig, cb = I.cborig;
+  for (int m = 0; m < 4; m++) {
+    R[R_XV + m] = xv[m];
+    R[R_YV + m] = yv[m];
+    const double xh = xv[m] / x, yh = yv[m] / y;
+    R[R_XH + m] = xh;
+    R[R_YH + m] = yh;
+    R[R_C2 + m] = (xh - cb * yh) / y;
+    R[R_C4 + m] = (yh - cb * xh) / x;
+  }
+  R[R_X] = x; R[R_YO] = y; R[R_CB] = cb; R[R_XSQ] = I.xsq; R[R_YSQ] = I.ysq; R[R_XDY] = I.xdoty;
+  R[R_RX] = 1.0 / x; R[R_RY] = 1.0 / y;
+  R[R_S + 0] = dg0dx; R[R_S + 1] = dg0dy; R[R_S + 2] = dg0dcb;
+  R[R_T + 0] = T.ell1; R[R_T + 1] = T.ell2; R[R_T + 2] = T.ell3;
+  R[R_T + 3] = T.d1x; R[R_T + 4] = T.d1y; R[R_T + 5] = T.d1cb;
+  R[R_T + 6] = T.d2x; R[R_T + 7] = T.d2y; R[R_T + 8] = T.d2cb;
+  R[R_T + 9] = T.d3x; R[R_T + 10] = T.d3y; R[R_T + 11] = T.d3cb;
+  for (int m = 0; m < 4; m++) {
+    R[R_VD + 0 + m] = xv[m] * D.ddg1dxdx + yv[m] * D.ddg2dxdx;
+    R[R_VD + 4 + m] = xv[m] * D.ddg1dxdy + yv[m] * D.ddg2dxdy;
+    R[R_VD + 8 + m] = xv[m] * D.ddg1dxdcb + yv[m] * D.ddg2dxdcb;
+    R[R_VD + 12 + m] = xv[m] * D.ddg1dydcb + yv[m] * D.ddg2dydcb;
+    R[R_VD + 16 + m] = xv[m] * D.ddg1dxdcb + yv[m] * D.ddg2dxdcb;
+    R[R_VD + 20 + m] = xv[m] * D.ddg1dcbdcb + yv[m] * D.ddg2dcbdcb;
+    R[R_VD + 24 + m] = (xv[m] * D.dg1dx + yv[m] * D.dg2dx) / x;
+    R[R_VD + 28 + m] = (xv[m] * D.dg1dcb + yv[m] * D.dg2dcb) / x;
+  }
+  for (int m = 0; m < 4; m++) {
+    const double xh = R[R_XH + m], yh = R[R_YH + m];
+    R[R_VA + m] = (D.dg1dx + D.dg2dx) * xh + (D.dg1dcb + D.dg2dcb) * R[R_C4 + m];
+    R[R_VB + m] = (D.dg1dx * xh + D.dg1dy * yh + D.dg1dcb * (xh / y + yh / x - cb * (xh / x + yh / y)));
+  }
+}
+
+/* Tabd_xeq0 scalars, src/LIBFILES/Tabd.c:22-84; returns 1 when |y| is above
+   the TAYLORX grid (zero kernel) */
+__device__ int fill_x0_record(const DevTables &T, double *R, const double *yv)
+{
+  const double ysq = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
+  const double y = sqrt(fabs(ysq));
+  const int it = bsrch(T.TX, y, 0, T.ny_tay);
+  if (it == T.ny_tay - 1) return 1;
+  const int it2 = it + 1;
+  const double *tx = T.TX;
+  const int ny = T.ny_tay;
+  const double ay = (tx[it2] - y) / (tx[it2] - tx[it]);
+#define TXL(row) lerp(ay, tx[(row)*ny + it], tx[(row)*ny + it2])
+  const double fx = 0.5 * TXL(G0dx);
+  const double fy = 0.5 * TXL(G0dy);
+  const double ell2 = TXL(Gl2), dell2adx = TXL(Gl21), dell2ady = TXL(Gl2dy), ell3a = TXL(Gl3);
+  const double dg2dx = TXL(G21), ddg2dxdy = TXL(G21dy);
+  const double dg1dx = (TXL(G31A) - (2. / 3) * (TXL(G31B)) - y * (TXL(G22A)));
+  const double dg1dy = (TXL(G3Ady) - TXL(G3Bdy));
+  const double phi1 = (TXL(G22A) - TXL(G22B) / 5.);
+  const double phi2 = (TXL(G22B)) * 1.2;
+#undef TXL
+  const double ysq_4 = ysq / 4.;
+  const double E = (ell3a + ell2), D2 = (dell2adx + dell2ady), D1 = (dg1dy + dg1dx),
+               D12 = (dg1dx + dg2dx), D3 = (y * ddg2dxdy - dg2dx);
+  for (int m = 0; m < 4; m++) {
+    const double yh = yv[m] / y;
+    const double dg0dy = yh * fy / 2, dg0dx = yh * fx / 2;
+    R[X0_Q + m] = yv[m];
+    R[X0_QH + m] = yh;
+    R[X0_YVE + m] = yv[m] * E;
+    R[X0_YVL3 + m] = yv[m] * ell3a;
+    R[X0_YHD1 + m] = yh * D1;
+    R[X0_YHD2 + m] = yh * D2;
+    R[X0_YHD3 + m] = yh * D3;
+    R[X0_YHG2 + m] = yh * dg2dx;
+    const double yalf2dx = yh * (dell2adx);
+    R[X0_YA2 + m] = yalf2dx;
+    R[X0_TII + m] = dg0dx - 0.5 * R[X0_YVL3 + m] - ysq_4 * yalf2dx;
+    R[X0_TIII + m] = (dg0dx + dg0dy) - 0.5 * R[X0_YVE + m] - ysq_4 * R[X0_YHD2 + m];
+    R[X0_YD12 + m] = yh * D12;
+  }
+  R[X0_PHI1] = phi1;
+  R[X0_PHI2] = phi2;
+  return 0;
+}
+
+/* Tabd_yeq0 scalars, src/LIBFILES/Tabd.c:116-195; returns 1 when |x| is
+   beyond the grid (zero kernel) */
+__device__ int fill_y0_record(const DevTables &T, double *R, const double *xv)
+{
+  const double xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
+  const double x = sqrt(fabs(xsq));
+  int ix = bsrch(T.XX, x, 0, T.nstpx);
+  if (x > __ldg(T.XX + T.nstpx - 1)) return 1;
+  /* |x| exactly on the last node: interpolate from the last interval (the
+     reference would read one node past its grid here) */
+  if (ix == T.nstpx - 1) ix = T.nstpx - 2;
+  const int ix2 = ix + 1;
+  const double xa = __ldg(T.XX + ix), xb = __ldg(T.XX + ix2);
+  const double ax = (xb - x) / (xb - xa);
+  const double *ty = T.TY;
+  const int nx = T.nx_tay;
+#define TY(row, i) __ldg(ty + (row)*nx + (i))
+  const double fx = 0.5 * lerp(ax, TY(alpha0dx_0p, ix), TY(alpha0dx_0p, ix2));
+  const double fy = (lerp(ax, TY(alpha0_1p, ix), TY(alpha0_1p, ix2)));
+  const double xa2 = xa * xa, xa3 = xa2 * xa, xa4 = xa3 * xa;
+  const double xb2 = xb * xb, xb3 = xb2 * xb, xb4 = xb3 * xb;
+  const double ell1 = 4 * (lerp(ax, TY(alpha1_0p, ix) / (xa4), TY(alpha1_0p, ix2) / (xb4))) / 3.;
+  const double ell3 = lerp(ax, TY(beta4_1p, ix) / (xa2), TY(beta4_1p, ix2) / (xb2));
+  const double dell1dx = 4 * lerp(ax, (TY(alpha1dx_0p, ix) - 4. * TY(alpha1_0p, ix) / xa) / xa4,
+                                  (TY(alpha1dx_0p, ix2) - 4. * TY(alpha1_0p, ix2) / xb) / xb4) / 3.;
+  const double dell1dycb = 2 * lerp(ax, (4. * TY(alpha1_1p, ix) / (3 * xa) - TY(beta4_1p, ix)) / xa3,
+                                    (4. * TY(alpha1_1p, ix2) / (3 * xb) - TY(beta4_1p, ix2)) / xb3);
+  const double dg1dx = lerp(ax, TY(alpha3dx_0p, ix), TY(alpha3dx_0p, ix2));
+  const double ddg1dxdx = lerp(ax, TY(alpha3dxdx_0p, ix), TY(alpha3dxdx_0p, ix2));
+  const double dg2dx = 2 * lerp(ax, TY(beta2dx_1p, ix), TY(beta2dx_1p, ix2));
+  const double dg1dycb = 2 * lerp(ax, TY(alpha3_1p, ix) - TY(beta2_1p, ix) / xa,
+                                  TY(alpha3_1p, ix2) - TY(beta2_1p, ix2) / xb);
+  const double ddg1dxdycb = 2 * lerp(ax, TY(beta2_1p, ix) / (xa2) - TY(beta2dx_1p, ix) / xa + TY(alpha3dx_1p, ix),
+                                     TY(beta2_1p, ix2) / (xb2) - TY(beta2dx_1p, ix2) / xb + TY(alpha3dx_1p, ix2));
+#undef TY
+  const double xsq_4 = xsq / 4., E = ell1 + ell3, D1 = dell1dx + dell1dycb,
+               D2 = (ddg1dxdx + ddg1dxdycb), D3 = (dg1dycb - dg2dx), D4 = (dg1dx + dg1dycb);
+  for (int m = 0; m < 4; m++) {
+    const double xh = xv[m] / x;
+    const double dg0dy = xh * fy / 2, dg0dx = xh * fx / 2;
+    R[Y0_X + m] = xv[m];
+    R[Y0_XH + m] = xh;
+    R[Y0_XVE + m] = xv[m] * E;
+    R[Y0_XVL1 + m] = xv[m] * ell1;
+    R[Y0_XHD + m] = xh * (dell1dx);
+    R[Y0_TII + m] = (dg0dx - 0.5 * R[Y0_XVL1 + m]);
+    R[Y0_DG0 + m] = (dg0dx + dg0dy - 0.5 * R[Y0_XVE + m]);
+  }
+  R[Y0_XSQ4] = xsq_4; R[Y0_D1] = D1; R[Y0_D2] = D2; R[Y0_D3] = D3; R[Y0_D4] = D4;
+  return 0;
+}
+
+__device__ __forceinline__ bool is_zero4(const double *v)
+{
+  return (v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3]) < 1E-28;
+}
+
+/* Phase A for one pair: classify (QED_kernel_L0, kernels.c:81-115), fill the
+   record, return the kind and status bits. */
+__device__ int phase_a(const DevTables &T, const double *xv, const double *yv, double *R,
+                       int &status)
+{
+  status = 0;
+  /* non-finite input: the reference's grid search would run off the tables;
+     here it is reported as out of grid with a zero kernel */
+  if (!isfinite(fabs(xv[0]) + fabs(xv[1]) + fabs(xv[2]) + fabs(xv[3]) + fabs(yv[0]) +
+                fabs(yv[1]) + fabs(yv[2]) + fabs(yv[3]))) {
+    status |= 1;
+    return K_NONE;
+  }
+  const bool x0 = is_zero4(xv), y0 = is_zero4(yv);
+  if (x0 && y0) return K_NONE;
+  if (x0) {
+    status |= 8;
+    if (fill_x0_record(T, R, yv)) { status |= 1; return K_NONE; }
+    return K_X0;
+  }
+  if (y0) {
+    status |= 8;
+    if (fill_y0_record(T, R, xv)) { status |= 1; return K_NONE; }
+    return K_Y0;
+  }
+  const double d[4] = {xv[0] - yv[0], xv[1] - yv[1], xv[2] - yv[2], xv[3] - yv[3]};
+  if (is_zero4(d)) {
+    status |= 8;
+    if (fill_y0_record(T, R, xv)) { status |= 1; return K_NONE; }
+    return K_Y0PERM;
+  }
+  Inv I;
+  invariants(T, xv, yv, I);
+  if (I.flag2) status |= 4;
+  const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
+  if (I.x > xhi) { status |= 1; return K_NONE; }
+  double dg0dx, dg0dy, dg0dcb;
+  TS Ts;
+  VS D;
+  if (I.x < xlo) {
+    status |= 2;
+    if (S_taylor(T, I, dg0dy, dg0dx, dg0dcb) || T_taylor(T, I, Ts) ||
+        V_taylor(T, D, I.x, I.y, I.xsq, I.flag2, I.cb)) {
+      status |= 1;
+      return K_NONE;
+    }
+  } else {
+    /* grid position and interpolation weights (extractff's flag_hx/flag_hy
+       edges, getff-new.c:218-219) */
+    const int flag_hx = (I.x >= xhi);
+    const int flag_hy = (I.y >= __ldg(T.YY + T.nstpy - 1));
+    const int ix0 = I.ix, ix1 = flag_hx ? I.ix : I.ix + 1;
+    const int iy0 = I.iy, iy1 = flag_hy ? I.iy : I.iy + 1;
+    Wts w;
+    if (flag_hx) {
+      w.xA = 1.0; w.xB = 0.0; w.xC1 = 0.0; w.xC2 = 0.0; w.lAx = 1.0;
+    } else {
+      const Herm h = herm(I.x, __ldg(T.XX + ix0), __ldg(T.XX + ix1));
+      w.xA = h.A * h.D; w.xB = h.B * h.D; w.xC1 = h.C1 * h.D; w.xC2 = h.C2 * h.D; w.lAx = h.lA;
+    }
+    if (flag_hy) {
+      w.yA = 1.0; w.yB = 0.0; w.yC1 = 0.0; w.yC2 = 0.0; w.lAy = 1.0;
+    } else {
+      const Herm h = herm(I.y, __ldg(T.YY + iy0), __ldg(T.YY + iy1));
+      w.yA = h.A * h.D; w.yB = h.B * h.D; w.yC1 = h.C1 * h.D; w.yC2 = h.C2 * h.D; w.lAy = h.lA;
+    }
+    /* second y-derivative of the swap branch: zero when the upper node is the
+       last one (its extractff then sees flag_hy and repeats the lower node) */
+    w.dd = (I.flag2 && !flag_hy && iy0 + 1 < T.nstpy - 1) ? 1.0 : 0.0;
+    const int NK = T.NK;
+    const double *b00 = T.node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow;
+    const double *b01 = T.node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow;
+    const double *b10 = T.node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow;
+    const double *b11 = T.node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow;
+    const int Ktop = max(__ldg(T.nfx + ix0), __ldg(T.nfx + ix1)) + 2;
+    double W[39];
+    interp_generic(T, b00, b01, b10, b11, Ktop, w, 2.0 * I.cb, W);
+    dg0dcb = W[0]; dg0dx = W[1]; dg0dy = W[2];
+    T_generic(I, W, Ts);
+    V_generic(I, W, T.ystp, D);
+  }
+  if (I.flag2) {
+    swap3(I, dg0dx, dg0dcb, dg0dy);
+    T_swap(I, Ts);
+    V_swap(&D, I.x, I.xmy, I.yorig, I.xsq, I.xmysq, I.ysq, I.cb, I.cborig);
+  }
+  fill_generic_record(R, xv, yv, I, dg0dx, dg0dy, dg0dcb, Ts, D);
+  return K_GEN;
+}
+
+/* ------------------------------------------------ phases B and C (warp) */
+
+/* 200 STV components of one generic pair into stv[] (lane-parallel):
+   chnr_dS.c:85-93, chnr_dT.c:353-385, get_dv chnr_dV.c:326-357 */
+__device__ __forceinline__ void stv_generic(const double *R, double *stv, int lane)
+{
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const int idx = r * 32 + lane;
+    const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
+    const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
+    const double *xv = R + R_XV, *yv = R + R_YV;
+    const double c1 = R[R_YH + b], c3 = R[R_XH + b], c2 = R[R_C2 + b], c4 = R[R_C4 + b];
+    const double t1 = (d_ab ? yv[d] : 0.0) + (d_bd ? yv[a] : 0.0) - (d_ad ? 0.5 * yv[b] : 0.0);
+    const double t2 = (d_ab ? xv[d] : 0.0) + (d_bd ? xv[a] : 0.0) - (d_ad ? 0.5 * xv[b] : 0.0);
+    const double t3 = xv[a] * xv[d] - (d_ad ? R[R_XSQ] / 4 : 0.0);
+    const double t4 = yv[a] * yv[d] - (d_ad ? R[R_YSQ] / 4 : 0.0);
+    const double t5 = xv[a] * yv[d] + yv[a] * xv[d] - (d_ad ? 0.5 * R[R_XDY] : 0.0);
+    const double *T = R + R_T;
+    stv[72 + idx] = t1 * T[1] + t2 * T[2] + t3 * (c1 * T[4] + c2 * T[5]) +
+                    t4 * (c1 * T[7] + c2 * T[8]) + t5 * (c1 * T[10] + c2 * T[11]);
+    stv[8 + idx] = t2 * T[0] + t1 * T[2] + t3 * (c3 * T[3] + c4 * T[5]) +
+                   t4 * (c3 * T[6] + c4 * T[8]) + t5 * (c3 * T[9] + c4 * T[11]);
+  }
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const int idx = r * 32 + lane;
+    const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
+    const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
+    const double xa = R[R_XH + a], xb = R[R_XH + b], ya = R[R_YH + a], yb = R[R_YH + b];
+    const double cb = R[R_CB];
+    const double c4a = R[R_C4 + a];
+    const double c2c4 = R[R_C2 + b] + R[R_C4 + b];
+    const double xaxb = xa * xb, yayb = ya * yb, xayb = xa * yb, yaxb = ya * xb;
+    const double dab = d_ab ? 1.0 : 0.0;
+    const double c1 = ((cb * (3.0 * xaxb - dab) - xayb - yaxb) * R[R_RX] +
+                       (dab + xayb * cb - xaxb - yayb) * R[R_RY]);
+    const double *Dv = R + R_VD;
+    double f = d_bd ? R[R_VA + a] : 0.0;
+    if (d_ad) f += R[R_VB + b];
+    f += Dv[0 + d] * xaxb + Dv[4 + d] * xayb;
+    f += (Dv[8 + d] * xb + Dv[12 + d] * yb) * c4a;
+    f += (Dv[16 + d] * xa + Dv[20 + d] * c4a) * c2c4;
+    f += Dv[24 + d] * (dab - xaxb);
+    stv[136 + idx] = f + Dv[28 + d] * c1;
+  }
+  if (lane < 8) {
+    const int b = lane & 3;
+    stv[lane] = lane < 4 ? R[R_XH + b] * R[R_S + 0] + R[R_C4 + b] * R[R_S + 2]
+                         : R[R_YH + b] * R[R_S + 1] + R[R_C2 + b] * R[R_S + 2];
+  }
+}
+
+/* x = 0: tI -> V, tII -> Tx, tIII -> Ty (Tabd.c:87-111) */
+__device__ __forceinline__ void stv_x0(const double *R, double *stv, int lane)
+{
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const int idx = r * 32 + lane;
+    const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
+    const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
+    const double *yv = R + X0_Q, *yh = R + X0_QH;
+    double tIII = yv[a] * yv[d] * R[X0_YHD2 + b];
+    if (d_ab) tIII += R[X0_YVE + d];
+    if (d_bd) tIII += R[X0_YVE + a];
+    if (d_ad) tIII += R[X0_TIII + b];
+    double tII = yv[b] * yv[d] * R[X0_YA2 + a];
+    if (d_bd) tII += R[X0_TII + a];
+    tII += ((d_ab ? R[X0_YVL3 + d] : 0.0) + (d_ad ? R[X0_YVL3 + b] : 0.0));
+    const double tIsum = 2 * ((d_ab ? R[X0_PHI1] : 0.0) + yh[a] * yh[b] * R[X0_PHI2]);
+    double tI = d_bd ? R[X0_YD12 + a] : 0.0;
+    if (d_ab) tI += R[X0_YHG2 + d];
+    tI += R[X0_YHD3 + b] * yh[a] * yh[d];
+    if (d_ad) tI += R[X0_YHD1 + b];
+    tI += yv[d] * tIsum;
+    stv[136 + idx] = tI;
+    stv[8 + idx] = tII;
+    stv[72 + idx] = tIII;
+  }
+}
+
+/* y = 0 (and x = y): Tabd.c:196-217 */
+__device__ __forceinline__ void stv_y0(const double *R, double *stv, int lane)
+{
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const int idx = r * 32 + lane;
+    const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
+    const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
+    const double *xv = R + Y0_X, *xh = R + Y0_XH;
+    const double xsq_4 = R[Y0_XSQ4];
+    const double xad = (xv[a] * xv[d] - (d_ad ? xsq_4 : 0.0));
+    double tIII = xad * xh[b] * R[Y0_D1];
+    if (d_ab) tIII += R[Y0_XVE + d];
+    if (d_bd) tIII += R[Y0_XVE + a];
+    if (d_ad) tIII += R[Y0_DG0 + b];
+    double tII = (xv[b] * xv[d] - (d_bd ? xsq_4 : 0.0)) * R[Y0_XHD + a];
+    if (d_ab) tII += R[Y0_XVL1 + d];
+    if (d_ad) tII += R[Y0_XVL1 + b];
+    if (d_bd) tII += R[Y0_TII + a];
+    double s = 0.0;
+    if (d_ad) s += xh[b];
+    if (d_bd) s += xh[a];
+    if (d_ab) s += xh[d];
+    const double tI = (s - xh[a] * xh[b] * xh[d]) * R[Y0_D4] +
+                      xh[a] * (xh[b] * xv[d] * R[Y0_D2] - (d_bd ? R[Y0_D3] : 0.0));
+    stv[136 + idx] = tI;
+    stv[8 + idx] = tII;
+    stv[72 + idx] = tIII;
+  }
+}
+
+/* the STV -> 384 map for the current pair, rows dealt to lanes; result into
+   tbuf (natural row order) */
+__device__ __forceinline__ void apply_map_warp(const uint16_t *ent, const uint16_t *rows,
+                                               const MapSched &S, const double *coef,
+                                               const double *stv, double *tbuf, int lane)
+{
+#pragma unroll 1
+  for (int r = 0; r < kMapRounds; r++) {
+    const uint16_t *e = ent + S.off[r] + lane;
+    double acc = 0.0;
+    const int len = S.len[r];
+#pragma unroll 4
+    for (int s = 0; s < len; s++) {
+      const uint16_t v = e[s * 32];
+      acc = fma(coef[v >> 8], stv[v & 0xff], acc);
+    }
+    tbuf[rows[r * 32 + lane]] = acc;
+  }
+}
+
+__device__ __forceinline__ int mulam(int i)
+{
+  const int rs = i >> 6, mu = (i >> 4) & 3, nu = (i >> 2) & 3, la = i & 3;
+  return rs * 64 + la * 16 + nu * 4 + mu;
+}
+
+/* ------------------------------------------------------------ kernels */
+
+struct WarpSmem {
+  double *rec;   /* [32][REC] */
+  double *stv;   /* [200] components, [200] = 0 (padding target of the map) */
+  double *tbuf;  /* [384] */
+  int *kind;     /* [32] */
+};
+
+__host__ __device__ constexpr size_t warp_smem_doubles() { return 32 * REC + 202 + 384; }
+
+size_t smem_bytes_l0(int wpb)
+{
+  return (size_t)wpb * (warp_smem_doubles() * sizeof(double) + 32 * sizeof(int)) + 8 * sizeof(double) +
+         (size_t)(2 * 3072 + 2 * 384) * sizeof(uint16_t);
+}
+
+/* block prologue: coefficient LUT and the two map schedules into shared memory */
+__device__ __forceinline__ void load_maps(const DevMaps &M, double *coef, uint16_t *eg,
+                                          uint16_t *ez, uint16_t *rg, uint16_t *rz)
+{
+  if (threadIdx.x < 8) {
+    const double c[8] = {-2.0, -1.0, -0.5, 0.5, 1.0, 2.0, 0.0, 0.0};
+    coef[threadIdx.x] = c[threadIdx.x];
+  }
+  for (int i = threadIdx.x; i < M.gen.total; i += blockDim.x) eg[i] = M.ent_gen[i];
+  for (int i = threadIdx.x; i < M.zero.total; i += blockDim.x) ez[i] = M.ent_zero[i];
+  for (int i = threadIdx.x; i < 384; i += blockDim.x) { rg[i] = M.row_gen[i]; rz[i] = M.row_zero[i]; }
+  __syncthreads();
+}
+
+struct SmemLayout {
+  double *coef;
+  uint16_t *eg, *ez, *rg, *rz;
+  WarpSmem w;
+};
+
+__device__ __forceinline__ SmemLayout carve(int wpb, const DevMaps &M)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemLayout L;
+  const int warp = threadIdx.x >> 5;
+  double *wbase = reinterpret_cast<double *>(smem_raw) + (size_t)warp * warp_smem_doubles();
+  L.w.rec = wbase;
+  L.w.stv = wbase + 32 * REC;
+  L.w.tbuf = L.w.stv + 202;
+  double *after = reinterpret_cast<double *>(smem_raw) + (size_t)wpb * warp_smem_doubles();
+  L.coef = after;
+  int *kinds = reinterpret_cast<int *>(after + 8);
+  L.w.kind = kinds + warp * 32;
+  uint16_t *u = reinterpret_cast<uint16_t *>(kinds + wpb * 32);
+  L.eg = u;
+  L.ez = u + 3072;
+  L.rg = L.ez + 3072;
+  L.rz = L.rg + 384;
+  return L;
+}
+
+/* assemble the 384 components of the warp's pair q into tbuf; returns false
+   for a zero kernel */
+__device__ __forceinline__ bool assemble_pair(const SmemLayout &L, const DevMaps &M, int q,
+                                              int lane, bool &perm)
+{
+  const int kind = L.w.kind[q];
+  perm = (kind == K_Y0PERM);
+  if (kind == K_NONE) return false;
+  const double *R = L.w.rec + q * REC;
+  if (kind == K_GEN) stv_generic(R, L.w.stv, lane);
+  else if (kind == K_X0) stv_x0(R, L.w.stv, lane);
+  else stv_y0(R, L.w.stv, lane);
+  __syncwarp();
+  if (kind == K_GEN) apply_map_warp(L.eg, L.rg, M.gen, L.coef, L.w.stv, L.w.tbuf, lane);
+  else apply_map_warp(L.ez, L.rz, M.zero, L.coef, L.w.stv, L.w.tbuf, lane);
+  __syncwarp();
+  return true;
+}
+
+/* Batched L0: out[i][384] */
+__global__ void __launch_bounds__(128) l0_fp64_kernel(DevTables T, DevMaps M, L0Args A, int wpb)
+{
+  SmemLayout L = carve(wpb, M);
+  if ((threadIdx.x & 31) == 0) { L.w.stv[200] = 0.0; L.w.stv[201] = 0.0; }
+  load_maps(M, L.coef, L.eg, L.ez, L.rg, L.rz);
+  const int lane = threadIdx.x & 31;
+  const size_t tile = (size_t)wpb * 32;
+  for (size_t base = (size_t)blockIdx.x * tile; base < A.n; base += (size_t)gridDim.x * tile) {
+    const size_t wbase = base + (threadIdx.x & ~31);
+    const size_t p = wbase + lane;
+    int kind = K_NONE, status = 0;
+    if (p < A.n) {
+      double xv[4], yv[4];
+      for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * p + m]; yv[m] = A.y[4 * p + m]; }
+      kind = phase_a(T, xv, yv, L.w.rec + lane * REC, status);
+      if (A.status) A.status[p] = (uint8_t)status;
+    }
+    L.w.kind[lane] = kind;
+    __syncwarp();
+    const int nq = (int)min((size_t)32, A.n > wbase ? A.n - wbase : (size_t)0);
+    for (int q = 0; q < nq; q++) {
+      bool perm;
+      const bool live = assemble_pair(L, M, q, lane, perm);
+      double *o = A.out + (wbase + q) * 384;
+#pragma unroll
+      for (int r = 0; r < 12; r++) {
+        const int i = r * 32 + lane;
+        o[i] = live ? (perm ? -L.w.tbuf[mulam(i)] : L.w.tbuf[i]) : 0.0;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+/* Neumaier compensated add */
+__device__ __forceinline__ void kadd(double &s, double &c, double v)
+{
+  const double t = s + v;
+  c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
+  s = t;
+}
+
+/* Fused lattice integrand: block (tile, k) sums pairs (x_k, y_n), n in the
+   tile; writes partial[k][tile] = (sum, compensation). */
+__global__ void __launch_bounds__(128) lattice_fp64_kernel(DevTables T, DevMaps M, LatticeArgs A,
+                                                           int wpb)
+{
+  SmemLayout L = carve(wpb, M);
+  if ((threadIdx.x & 31) == 0) { L.w.stv[200] = 0.0; L.w.stv[201] = 0.0; }
+  load_maps(M, L.coef, L.eg, L.ez, L.rg, L.rz);
+  __shared__ double red_s[8], red_c[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t tile = (size_t)wpb * 32;
+  const size_t nunits = A.nx * (size_t)A.tiles;
+  for (size_t u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const size_t k = u / A.tiles, t = u % A.tiles;
+    const size_t wbase = t * tile + (size_t)warp * 32;
+    const size_t n = wbase + lane;
+    double xv[4];
+    for (int m = 0; m < 4; m++) xv[m] = A.x[4 * k + m];
+    int kind = K_NONE, status = 0;
+    if (n < A.ny) {
+      double yv[4];
+      for (int m = 0; m < 4; m++) yv[m] = A.y[4 * n + m];
+      kind = phase_a(T, xv, yv, L.w.rec + lane * REC, status);
+    }
+    L.w.kind[lane] = kind;
+    __syncwarp();
+    double s = 0.0, c = 0.0;
+    const int nq = (int)min((size_t)32, A.ny > wbase ? A.ny - wbase : (size_t)0);
+    for (int q = 0; q < nq; q++) {
+      bool perm;
+      const bool live = assemble_pair(L, M, q, lane, perm);
+      const size_t nn = wbase + q;
+      const double *pi = A.pi + (k * A.ny + nn) * 384;
+      const double *ky = A.Ky ? A.Ky + nn * 384 : nullptr;
+      const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
+      double acc = 0.0;
+#pragma unroll
+      for (int r = 0; r < 12; r++) {
+        const int i = r * 32 + lane;
+        double kv = live ? (perm ? -L.w.tbuf[mulam(i)] : L.w.tbuf[i]) : 0.0;
+        if (ky) kv += __ldg(ky + i);
+        if (bx) kv += __ldg(bx + i);
+        acc = fma(kv, __ldg(pi + i), acc);
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      kadd(s, c, acc);
+      __syncwarp();
+    }
+    if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bs = 0.0, bc = 0.0;
+      for (int w2 = 0; w2 < wpb; w2++) { kadd(bs, bc, red_s[w2]); bc += red_c[w2]; }
+      A.partial[(k * A.tiles + t) * 2 + 0] = bs;
+      A.partial[(k * A.tiles + t) * 2 + 1] = bc;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void reduce_partials_kernel(const double *partial, size_t nx, int tiles, double *sums)
+{
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nx) return;
+  double s = 0.0, c = 0.0;
+  for (int t = 0; t < tiles; t++) {
+    kadd(s, c, partial[(k * tiles + t) * 2 + 0]);
+    c += partial[(k * tiles + t) * 2 + 1];
+  }
+  sums[k] = s + c;
+}
+
+__global__ void axpy_kernel(double *y, const double *x, double a, size_t n)
+{
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] += x[i] * a;
+}
+
+__global__ void scale_kernel(double *y, double a, size_t n)
+{
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] *= a;
+}
+
+/* y[p][i] += a * x[p][mulam(i)] */
+__global__ void mulam_axpy_kernel(double *y, const double *x, double a, size_t npairs)
+{
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < npairs * 384;
+       j += (size_t)gridDim.x * blockDim.x) {
+    const size_t p = j / 384;
+    const int i = (int)(j % 384);
+    y[j] += x[p * 384 + mulam(i)] * a;
+  }
+}
+
+/* dst[i] = mode 0: zero vector, 1: copy of src[i] (pairs of 4-vectors) */
+__global__ void fill_pairs_kernel(const double *src, size_t n, int mode, double *dst)
+{
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n * 4; j += (size_t)gridDim.x * blockDim.x)
+    dst[j] = mode ? src[j] : 0.0;
+}
+
+static int num_sms()
+{
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+static cudaError_t prep_kernel_smem(const void *fn, size_t bytes)
+{
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a,
+                           const LaunchCfg &cfg, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
+  const size_t smem = smem_bytes_l0(wpb);
+  cudaError_t e = prep_kernel_smem((const void *)l0_fp64_kernel, smem);
+  if (e != cudaSuccess) return e;
+  const size_t tiles = (a.n + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32);
+  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : (size_t)num_sms() * 2;
+  if (blocks > tiles) blocks = tiles;
+  l0_fp64_kernel<<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                const LaunchCfg &cfg, cudaStream_t s)
+{
+  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
+  const size_t smem = smem_bytes_l0(wpb);
+  cudaError_t e = prep_kernel_smem((const void *)lattice_fp64_kernel, smem);
+  if (e != cudaSuccess) return e;
+  const size_t units = a.nx * (size_t)a.tiles;
+  if (units == 0) return cudaSuccess;
+  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : (size_t)num_sms() * 2;
+  if (blocks > units) blocks = units;
+  lattice_fp64_kernel<<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,
+                                   cudaStream_t s)
+{
+  if (nx == 0) return cudaSuccess;
+  reduce_partials_kernel<<<(unsigned)((nx + 127) / 128), 128, 0, s>>>(partial, nx, tiles, sums);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  const size_t b = min((n + 255) / 256, (size_t)num_sms() * 8);
+  axpy_kernel<<<(unsigned)b, 256, 0, s>>>(y, x, a, n);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale(double *y, double a, size_t n, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  const size_t b = min((n + 255) / 256, (size_t)num_sms() * 8);
+  scale_kernel<<<(unsigned)b, 256, 0, s>>>(y, a, n);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mulam_axpy(double *y, const double *x, double a, size_t npairs, cudaStream_t s)
+{
+  if (npairs == 0) return cudaSuccess;
+  const size_t b = min((npairs * 384 + 255) / 256, (size_t)num_sms() * 8);
+  mulam_axpy_kernel<<<(unsigned)b, 256, 0, s>>>(y, x, a, npairs);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_pairs(const double *src, size_t n, int mode, double *dst, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  const size_t b = min((n * 4 + 255) / 256, (size_t)num_sms() * 8);
+  fill_pairs_kernel<<<(unsigned)b, 256, 0, s>>>(src, n, mode, dst);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+} // namespace kqed

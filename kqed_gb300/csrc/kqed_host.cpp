@@ -1,0 +1,694 @@
+/*
+ * Host layer of libkqed_gb300.so: the reference-compatible C API
+ * (initialise / free_QED_temps / QED_kernel_L0..L3) and the batched and fused
+ * entry points, over the sm_103a kernels in kqed_fp64.cu.
+ *
+ * Tables are read from the reference's own files and formats
+ * (src/LIBFILES/io.c:42-289), checksummed the same way
+ * (src/UTILS/crc32c.c:160-172), and precomputed once into the device layout
+ * described in kqed_internal.h.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/kqed.h"
+#include "kqed_crc32c.h"
+#include "kqed_internal.h"
+#include "kqed_stv_map.h"
+
+#ifndef KQED_DEFAULT_LIB_PATH
+#define KQED_DEFAULT_LIB_PATH "."
+#endif
+
+using namespace kqed;
+
+/* ------------------------------------------------------------- errors */
+
+static thread_local std::string tl_err;
+
+static int fail(const char *fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  tl_err = buf;
+  return 1;
+}
+
+extern "C" const char *kqed_last_error(void) { return tl_err.c_str(); }
+extern "C" uint64_t kqed_launch_count(void) { return kqed::g_launches; }
+
+#define CUDA_OK(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail("%s: %s", #call, cudaGetErrorString(e_));           \
+  } while (0)
+
+/* ---------------------------------------------------------- context */
+
+namespace {
+
+struct Scratch {
+  double *buf = nullptr;
+  size_t cap = 0; /* doubles */
+  double *get(size_t n)
+  {
+    if (n > cap) {
+      if (buf) cudaFree(buf);
+      buf = nullptr;
+      cap = 0;
+      if (cudaMalloc(&buf, n * sizeof(double)) != cudaSuccess) return nullptr;
+      cap = n;
+    }
+    return buf;
+  }
+  void release()
+  {
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    cap = 0;
+  }
+};
+
+struct Ctx {
+  int device = 0;
+  DevTables T{};
+  DevMaps M{};
+  LaunchCfg cfg{2, 0};
+  std::vector<void *> allocs;
+};
+
+/* per-thread staging for the per-pair legacy calls and batched host calls */
+struct ThreadStage {
+  Ctx *owner = nullptr;
+  cudaStream_t stream = nullptr;
+  double *h_pin = nullptr;   /* 8 + 384 doubles */
+  Scratch d_io, d_tmp, d_aux, d_aux2;
+  ~ThreadStage() { reset(); }
+  void reset()
+  {
+    if (stream) cudaStreamDestroy(stream);
+    if (h_pin) cudaFreeHost(h_pin);
+    d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release();
+    stream = nullptr;
+    h_pin = nullptr;
+    owner = nullptr;
+  }
+};
+
+thread_local ThreadStage tl_stage;
+
+Ctx *ctx_of(const struct QED_kernel_temps *t)
+{
+  if (!t || !t->Grid.PC) return nullptr;
+  return static_cast<Ctx *>(t->Grid.PC->Fm);
+}
+
+} // namespace
+
+/* ------------------------------------------------------------- loading */
+
+static int rd(void *p, size_t sz, size_t n, FILE *f) { return fread(p, sz, n, f) != n; }
+
+static std::string lib_path()
+{
+  const char *e = getenv("KQED_LIB_PATH");
+  return e && *e ? std::string(e) : std::string(KQED_DEFAULT_LIB_PATH);
+}
+
+/* read_ff, src/LIBFILES/io.c:42-176, filling the reference's Grid fields */
+static int load_ff(const std::string &lib, struct Grid_coeffs *G)
+{
+  const std::string path = lib + "/PRECOMP/FFxy_single_cksum.bin";
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return fail("Cannot find %s", path.c_str());
+  int magic = 0, n = 0;
+  uint32_t ck[2], a, b;
+  std::string why;
+  if (rd(&magic, 4, 1, f) || magic != 816968) { why = "missing magic number"; goto bad; }
+  if (rd(&n, 4, 1, f) || n < 2 || n > 100000) { why = "bad nstpx"; goto bad; }
+  G->nstpx = n;
+  G->XX = (double *)malloc(sizeof(double) * n);
+  if (rd(G->XX, 8, n, f) || rd(ck, 4, 2, f)) { why = "truncated XX"; goto bad; }
+  a = b = 0;
+  kqed_cksum_accum(&a, &b, 0, G->XX, sizeof(double) * n);
+  if (a != ck[0] || b != ck[1]) { why = "XX checksum mismatch"; goto bad; }
+  if (rd(&n, 4, 1, f) || n < 2 || n > 100000) { why = "bad nstpy"; goto bad; }
+  G->nstpy = n;
+  G->YY = (double *)malloc(sizeof(double) * n);
+  if (rd(G->YY, 8, n, f) || rd(ck, 4, 2, f)) { why = "truncated YY"; goto bad; }
+  a = b = 0;
+  kqed_cksum_accum(&a, &b, 0, G->YY, sizeof(double) * n);
+  if (a != ck[0] || b != ck[1]) { why = "YY checksum mismatch"; goto bad; }
+  G->xstp = G->XX[1] - G->XX[0];
+  G->ystp = G->YY[1] - G->YY[0];
+  if (rd(&G->Nffa, 4, 1, f) || G->Nffa != NFFA) { why = "bad Nffa"; goto bad; }
+  G->nfx = (int *)calloc(G->nstpx, sizeof(int));
+  G->Ffm = (float ****)calloc(G->Nffa, sizeof(float ***));
+  G->Ffp = (float ****)calloc(G->Nffa, sizeof(float ***));
+  {
+    uint32_t ma = 0, mb = 0, pa = 0, pb = 0, rank = 0;
+    for (int ia = 0; ia < G->Nffa; ia++) {
+      if (rd(&n, 4, 1, f) || n != G->nstpx) { why = "file is funny nstpx"; goto bad; }
+      G->Ffm[ia] = (float ***)calloc(G->nstpx, sizeof(float **));
+      G->Ffp[ia] = (float ***)calloc(G->nstpx, sizeof(float **));
+      for (int ix = 0; ix < G->nstpx; ix++) {
+        if (rd(&n, 4, 1, f) || n != G->nstpy) { why = "file is funny nstpy"; goto bad; }
+        G->Ffm[ia][ix] = (float **)calloc(G->nstpy, sizeof(float *));
+        G->Ffp[ia][ix] = (float **)calloc(G->nstpy, sizeof(float *));
+        for (int iy = 0; iy < G->nstpy; iy++) {
+          int nf = 0;
+          if (rd(&nf, 4, 1, f) || nf < 1 || nf > kNKMax - 2) { why = "bad coefficient count"; goto bad; }
+          if (G->nfx[ix] && G->nfx[ix] != nf) { why = "ragged coefficient count within an x node"; goto bad; }
+          G->nfx[ix] = nf;
+          float *fm = (float *)malloc(sizeof(float) * nf), *fp = (float *)malloc(sizeof(float) * nf);
+          G->Ffm[ia][ix][iy] = fm;
+          G->Ffp[ia][ix][iy] = fp;
+          if (rd(fm, 4, nf, f)) { why = "truncated coefficients"; goto bad; }
+          kqed_cksum_accum(&ma, &mb, rank, fm, sizeof(float) * nf);
+          if (rd(fp, 4, nf, f)) { why = "truncated coefficients"; goto bad; }
+          kqed_cksum_accum(&pa, &pb, rank, fp, sizeof(float) * nf);
+          rank++;
+        }
+      }
+    }
+    uint32_t tail[4];
+    if (rd(tail, 4, 4, f)) { why = "truncated checksums"; goto bad; }
+    if (tail[0] != ma || tail[1] != mb || tail[2] != pa || tail[3] != pb) {
+      why = "Computed and read ff checksums do not match";
+      goto bad;
+    }
+  }
+  fclose(f);
+  return 0;
+bad:
+  fclose(f);
+  return fail("|IO| %s: %s", path.c_str(), why.c_str());
+}
+
+/* read_TAYLORX / read_TAYLORY, src/LIBFILES/io.c:179-289 */
+static int load_taylor(const std::string &lib, const char *name, int nrows, int ncols,
+                       double ***rows_out, int *nrows_out, int *ncols_out)
+{
+  const std::string path = lib + "/PRECOMP/" + name;
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return fail("|IO| cannot open %s", path.c_str());
+  int magic = 0, n = 0;
+  uint32_t a = 0, b = 0, ck[2];
+  double **rows = (double **)calloc(nrows, sizeof(double *));
+  *rows_out = rows;
+  *nrows_out = nrows;
+  if (rd(&magic, 4, 1, f) || magic != 816968 || rd(&n, 4, 1, f) || n != nrows) goto bad;
+  for (int i = 0; i < nrows; i++) {
+    int m = 0;
+    if (rd(&m, 4, 1, f) || m != ncols) goto bad;
+    rows[i] = (double *)malloc(sizeof(double) * m);
+    if (rd(rows[i], 8, m, f)) goto bad;
+    kqed_cksum_accum(&a, &b, (uint32_t)i, rows[i], sizeof(double) * m);
+  }
+  if (rd(ck, 4, 2, f) || ck[0] != a || ck[1] != b) goto bad;
+  *ncols_out = ncols;
+  fclose(f);
+  return 0;
+bad:
+  fclose(f);
+  return fail("|IO| %s malformed or checksums do not match", path.c_str());
+}
+
+/* the reference's per-call y-power scaling (getff2, src/LIBFILES/getff-new.c:103-152),
+   applied once per node; out arrays are indexed by Chebyshev index U_K */
+static void scale_node(int nm, double y, int nf, const float *fm, const float *fp, double *fval,
+                       double *fvalD)
+{
+  const double y1 = 1.0 / y;
+  double yp = 1;
+  int mshm = 2;
+  switch (nm) {
+  case QG2: case dxQG2: case d2xQG2: yp = y1; mshm = 3; break;
+  case QL4: case dxQL4: yp = y; mshm = 1; break;
+  case QL2: case dxQL2: yp = y1 * y1; mshm = 4; break;
+  default: yp = 1.0; mshm = 2; break;
+  }
+  int mshp = 2 - mshm;
+  const int mm = abs(mshp);
+  double facm = y1 * y1 * yp, facp = yp;
+  for (int j = 0; j < mm; j++) { facm *= y1; facp *= y; }
+  mshm += mm; mshp += mm;
+  for (int j = 0; j < nf; j++) {
+    fvalD[mm + j] = y1 * mshp * facp * (double)fp[j] - y1 * mshm * facm * (double)fm[j];
+    fval[mm + j] = facm * (double)fm[j] + facp * (double)fp[j];
+    facm *= y1; facp *= y;
+    mshm++; mshp++;
+  }
+}
+
+static void *dev_upload(Ctx *c, const void *h, size_t bytes)
+{
+  void *d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice) != cudaSuccess) { cudaFree(d); return nullptr; }
+  c->allocs.push_back(d);
+  return d;
+}
+
+/* deal the rows of a sparse map to (round, lane) by length */
+static int build_sched(const unsigned short *row, const unsigned char *col, const signed char *q4,
+                       MapSched &S, std::vector<uint16_t> &ent, std::vector<uint16_t> &rows)
+{
+  std::vector<int> order(384);
+  for (int i = 0; i < 384; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (row[a + 1] - row[a]) > (row[b + 1] - row[b]);
+  });
+  rows.assign(384, 0);
+  ent.clear();
+  int off = 0;
+  for (int r = 0; r < kMapRounds; r++) {
+    int len = 0;
+    for (int l = 0; l < 32; l++) {
+      const int i = order[r * 32 + l];
+      len = std::max(len, (int)(row[i + 1] - row[i]));
+      rows[r * 32 + l] = (uint16_t)i;
+    }
+    S.len[r] = len;
+    S.off[r] = off;
+    for (int s = 0; s < len; s++)
+      for (int l = 0; l < 32; l++) {
+        const int i = order[r * 32 + l];
+        const int nz = row[i + 1] - row[i];
+        uint16_t e = (uint16_t)(200 | (6 << 8)); /* padding: zero slot, coefficient 0 */
+        if (s < nz) {
+          const int k = row[i] + s;
+          int code;
+          switch (q4[k]) {
+          case -8: code = 0; break;
+          case -4: code = 1; break;
+          case -2: code = 2; break;
+          case 2: code = 3; break;
+          case 4: code = 4; break;
+          case 8: code = 5; break;
+          default: return 1;
+          }
+          e = (uint16_t)(col[k] | (code << 8));
+        }
+        ent.push_back(e);
+      }
+    off += len * 32;
+  }
+  S.total = off;
+  return off > 3072 ? 1 : 0;
+}
+
+static int setup_device(struct Grid_coeffs *G, Ctx *c)
+{
+  CUDA_OK(cudaGetDevice(&c->device));
+  if (upload_map_constants()) return fail("cannot upload Clenshaw constants");
+  int nfmax = 0;
+  for (int i = 0; i < G->nstpx; i++) nfmax = std::max(nfmax, G->nfx[i]);
+  const int NK = nfmax + 2;
+  if (NK > kNKMax) return fail("Chebyshev length %d exceeds %d", NK, kNKMax);
+  /* node table */
+  const size_t nrow = (size_t)G->nstpx * G->nstpy * NK;
+  std::vector<double> node(nrow * kRow, 0.0);
+  std::vector<double> fval(kNKMax + 2), fvalD(kNKMax + 2);
+  for (int a = 0; a < NFFA; a++)
+    for (int ix = 0; ix < G->nstpx; ix++)
+      for (int iy = 0; iy < G->nstpy; iy++) {
+        std::fill(fval.begin(), fval.end(), 0.0);
+        std::fill(fvalD.begin(), fvalD.end(), 0.0);
+        const int nf = G->nfx[ix];
+        scale_node(a, G->YY[iy], nf, G->Ffm[a][ix][iy], G->Ffp[a][ix][iy], fval.data(), fvalD.data());
+        const int len = nf + kShiftOfTable[a];
+        double *base = node.data() + ((size_t)ix * G->nstpy + iy) * NK * kRow + 2 * kSlotOfTable[a];
+        for (int K = 0; K < len; K++) {
+          base[(size_t)K * kRow + 0] = fval[K];
+          base[(size_t)K * kRow + 1] = fvalD[K];
+        }
+      }
+  std::vector<double> tx(23 * (size_t)G->NY_tay), ty(14 * (size_t)G->NX_tay);
+  for (int r = 0; r < 23; r++) memcpy(&tx[(size_t)r * G->NY_tay], G->TX[r], sizeof(double) * G->NY_tay);
+  for (int r = 0; r < 14; r++) memcpy(&ty[(size_t)r * G->NX_tay], G->TY[r], sizeof(double) * G->NX_tay);
+  DevTables &T = c->T;
+  T.XX = (const double *)dev_upload(c, G->XX, sizeof(double) * G->nstpx);
+  T.YY = (const double *)dev_upload(c, G->YY, sizeof(double) * G->nstpy);
+  T.TX = (const double *)dev_upload(c, tx.data(), sizeof(double) * tx.size());
+  T.TY = (const double *)dev_upload(c, ty.data(), sizeof(double) * ty.size());
+  T.node = (const double *)dev_upload(c, node.data(), sizeof(double) * node.size());
+  T.nfx = (const int *)dev_upload(c, G->nfx, sizeof(int) * G->nstpx);
+  if (!T.XX || !T.YY || !T.TX || !T.TY || !T.node || !T.nfx) return fail("device table upload failed");
+  T.nstpx = G->nstpx; T.nstpy = G->nstpy; T.ny_tay = G->NY_tay; T.nx_tay = G->NX_tay; T.NK = NK;
+  T.ystp = G->ystp;
+  /* map schedules */
+  std::vector<uint16_t> eg, rg, ez, rz;
+  if (build_sched(KQ_MAP_GEN_ROW, KQ_MAP_GEN_COL, KQ_MAP_GEN_Q4, c->M.gen, eg, rg) ||
+      build_sched(KQ_MAP_ZERO_ROW, KQ_MAP_ZERO_COL, KQ_MAP_ZERO_Q4, c->M.zero, ez, rz))
+    return fail("map schedule does not fit");
+  c->M.ent_gen = (const uint16_t *)dev_upload(c, eg.data(), eg.size() * 2);
+  c->M.ent_zero = (const uint16_t *)dev_upload(c, ez.data(), ez.size() * 2);
+  c->M.row_gen = (const uint16_t *)dev_upload(c, rg.data(), rg.size() * 2);
+  c->M.row_zero = (const uint16_t *)dev_upload(c, rz.data(), rz.size() * 2);
+  if (!c->M.ent_gen || !c->M.ent_zero || !c->M.row_gen || !c->M.row_zero) return fail("map upload failed");
+  const char *wpb = getenv("KQED_WARPS_PER_BLOCK");
+  const char *blk = getenv("KQED_BLOCKS");
+  if (wpb) c->cfg.warps_per_block = std::max(1, std::min(4, atoi(wpb)));
+  if (blk) c->cfg.blocks = std::max(0, atoi(blk));
+  return 0;
+}
+
+static void free_grid(struct Grid_coeffs *G)
+{
+  if (G->Ffm) {
+    for (int a = 0; a < G->Nffa; a++) {
+      if (!G->Ffm[a]) continue;
+      for (int i = 0; i < G->nstpx; i++) {
+        if (!G->Ffm[a][i]) continue;
+        for (int j = 0; j < G->nstpy; j++) free(G->Ffm[a][i][j]);
+        free(G->Ffm[a][i]);
+      }
+      free(G->Ffm[a]);
+    }
+    free(G->Ffm);
+  }
+  if (G->Ffp) {
+    for (int a = 0; a < G->Nffa; a++) {
+      if (!G->Ffp[a]) continue;
+      for (int i = 0; i < G->nstpx; i++) {
+        if (!G->Ffp[a][i]) continue;
+        for (int j = 0; j < G->nstpy; j++) free(G->Ffp[a][i][j]);
+        free(G->Ffp[a][i]);
+      }
+      free(G->Ffp[a]);
+    }
+    free(G->Ffp);
+  }
+  if (G->TX) { for (int i = 0; i < 23; i++) free(G->TX[i]); free(G->TX); }
+  if (G->TY) { for (int i = 0; i < 14; i++) free(G->TY[i]); free(G->TY); }
+  free(G->XX); free(G->YY); free(G->nfx);
+}
+
+extern "C" void free_QED_temps(struct QED_kernel_temps *t)
+{
+  if (!t) return;
+  Ctx *c = ctx_of(t);
+  if (c) {
+    if (tl_stage.owner == c) tl_stage.reset();
+    for (void *p : c->allocs) cudaFree(p);
+    delete c;
+    free(t->Grid.PC);
+  }
+  free_grid(&t->Grid);
+  free(t->G8);
+  memset(t, 0, sizeof(*t));
+}
+
+extern "C" int initialise(struct QED_kernel_temps *t)
+{
+  if (!t) return 1;
+  memset(t, 0, sizeof(*t));
+  const std::string lib = lib_path();
+  struct Grid_coeffs *G = &t->Grid;
+  int ntx = 0, nty = 0;
+  if (load_ff(lib, G) ||
+      load_taylor(lib, "taylorx_cksum.bin", 23, 810, &G->TX, &ntx, &G->NY_tay) ||
+      load_taylor(lib, "taylory_cksum.bin", 14, 100, &G->TY, &nty, &G->NX_tay)) {
+    fprintf(stderr, "%s\n", tl_err.c_str());
+    free_grid(G);
+    memset(t, 0, sizeof(*t));
+    return 1;
+  }
+  /* the reference names the TAYLORX row count NtayY and TAYLORY's NtayX
+     (io.c:195, :252) */
+  G->NtayY = ntx;
+  G->NtayX = nty;
+  Ctx *c = new Ctx();
+  if (setup_device(G, c)) {
+    fprintf(stderr, "%s\n", tl_err.c_str());
+    for (void *p : c->allocs) cudaFree(p);
+    delete c;
+    free_grid(G);
+    memset(t, 0, sizeof(*t));
+    return 1;
+  }
+  G->PC = (struct AVX_precomps *)calloc(1, sizeof(struct AVX_precomps));
+  G->PC->Fm = c;
+  t->G8 = nullptr;
+  return 0;
+}
+
+extern "C" int initialize_QED_kernel_temps(struct QED_kernel_temps *t) { return initialise(t); }
+
+/* ------------------------------------------------------ batched kernels */
+
+static int check_variant_precision(int variant, int precision)
+{
+  if (variant < 0 || variant > 3) return fail("variant %d not in 0..3", variant);
+  if (precision != KQED_FP64) return fail("precision mode %d is not available in this build", precision);
+  return 0;
+}
+
+/* L0 over n pairs on the device */
+static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *dout,
+                  uint8_t *dstatus, cudaStream_t s)
+{
+  L0Args a{dx, dy, n, dout, dstatus};
+  CUDA_OK(launch_l0_fp64(c->T, c->M, a, c->cfg, s));
+  return 0;
+}
+
+/* QED_kernel_L1/L2/L3 (src/LIBFILES/kernels.c:117-177) as L0 terms */
+static int run_variant(Ctx *c, int variant, const double *dx, const double *dy, size_t n,
+                       double *dout, uint8_t *dstatus, cudaStream_t s, ThreadStage &st)
+{
+  if (run_l0(c, dx, dy, n, dout, dstatus, s)) return 1;
+  if (variant == 0) return 0;
+  double *tmp = st.d_tmp.get(n * 384);
+  double *zero = st.d_aux.get(n * 4);
+  if (!tmp || !zero) return fail("out of device memory for %zu pairs", n);
+  CUDA_OK(launch_fill_pairs(nullptr, n, 0, zero, s));
+  switch (variant) {
+  case 1:
+    if (run_l0(c, dx, dx, n, tmp, nullptr, s)) return 1;
+    CUDA_OK(launch_axpy(dout, tmp, -0.5, n * 384, s));
+    if (run_l0(c, dy, dy, n, tmp, nullptr, s)) return 1;
+    CUDA_OK(launch_axpy(dout, tmp, -0.5, n * 384, s));
+    break;
+  case 2:
+    if (run_l0(c, zero, dy, n, tmp, nullptr, s)) return 1;
+    CUDA_OK(launch_axpy(dout, tmp, -1.0, n * 384, s));
+    if (run_l0(c, dx, zero, n, tmp, nullptr, s)) return 1;
+    CUDA_OK(launch_axpy(dout, tmp, -1.0, n * 384, s));
+    break;
+  case 3:
+    if (run_l0(c, dx, dx, n, tmp, nullptr, s)) return 1;
+    CUDA_OK(launch_axpy(dout, tmp, -1.0, n * 384, s));
+    if (run_l0(c, zero, dx, n, tmp, nullptr, s)) return 1;
+    CUDA_OK(launch_axpy(dout, tmp, +1.0, n * 384, s));
+    if (run_l0(c, zero, dy, n, tmp, nullptr, s)) return 1;
+    CUDA_OK(launch_axpy(dout, tmp, -1.0, n * 384, s));
+    break;
+  }
+  return 0;
+}
+
+static ThreadStage &stage_for(Ctx *c)
+{
+  ThreadStage &st = tl_stage;
+  if (st.owner != c) {
+    st.reset();
+    st.owner = c;
+  }
+  return st;
+}
+
+extern "C" int kqed_kernel_batch_dev(const struct QED_kernel_temps *t, int variant, size_t n,
+                                     const double *d_x, const double *d_y, double *d_kerv,
+                                     uint8_t *d_status, int precision, void *stream)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (check_variant_precision(variant, precision)) return 1;
+  if (n && (!d_x || !d_y || !d_kerv)) return fail("null buffer");
+  return run_variant(c, variant, d_x, d_y, n, d_kerv, d_status, (cudaStream_t)stream, stage_for(c));
+}
+
+extern "C" int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, size_t n,
+                                 const double *x, const double *y, double *kerv, uint8_t *status,
+                                 int precision)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (check_variant_precision(variant, precision)) return 1;
+  if (n == 0) return 0;
+  if (!x || !y || !kerv) return fail("null buffer");
+  ThreadStage &st = stage_for(c);
+  if (!st.stream) CUDA_OK(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking));
+  double *io = st.d_io.get(n * (8 + 384) + (n + 7) / 8);
+  if (!io) return fail("out of device memory for %zu pairs", n);
+  double *dx = io, *dy = io + 4 * n, *dk = io + 8 * n;
+  uint8_t *dst = status ? reinterpret_cast<uint8_t *>(io + n * (8 + 384)) : nullptr;
+  CUDA_OK(cudaMemcpyAsync(dx, x, n * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
+  CUDA_OK(cudaMemcpyAsync(dy, y, n * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
+  if (run_variant(c, variant, dx, dy, n, dk, dst, st.stream, st)) return 1;
+  CUDA_OK(cudaMemcpyAsync(kerv, dk, n * 384 * sizeof(double), cudaMemcpyDeviceToHost, st.stream));
+  if (status) CUDA_OK(cudaMemcpyAsync(status, dst, n, cudaMemcpyDeviceToHost, st.stream));
+  CUDA_OK(cudaStreamSynchronize(st.stream));
+  return 0;
+}
+
+/* ---------------------------------------------------- legacy per pair */
+
+static void legacy(int variant, const double xv[4], const double yv[4],
+                   const struct QED_kernel_temps &t, double kerv[6][4][4][4])
+{
+  double *out = &kerv[0][0][0][0];
+  Ctx *c = ctx_of(&t);
+  if (!c) {
+    fprintf(stderr, "QED_kernel_L%d: tables not initialised\n", variant);
+    memset(out, 0, 384 * sizeof(double));
+    return;
+  }
+  ThreadStage &st = stage_for(c);
+  if (!st.h_pin) {
+    if (cudaMallocHost(&st.h_pin, (8 + 384) * sizeof(double)) != cudaSuccess) st.h_pin = nullptr;
+  }
+  if (!st.stream) cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking);
+  double *io = st.d_io.get(8 + 384 + 1);
+  if (!st.h_pin || !st.stream || !io) {
+    fprintf(stderr, "QED_kernel_L%d: GPU staging unavailable\n", variant);
+    memset(out, 0, 384 * sizeof(double));
+    return;
+  }
+  memcpy(st.h_pin, xv, 4 * sizeof(double));
+  memcpy(st.h_pin + 4, yv, 4 * sizeof(double));
+  int err = cudaMemcpyAsync(io, st.h_pin, 8 * sizeof(double), cudaMemcpyHostToDevice, st.stream) != cudaSuccess;
+  if (!err) err = run_variant(c, variant, io, io + 4, 1, io + 8, nullptr, st.stream, st);
+  if (!err)
+    err = cudaMemcpyAsync(st.h_pin + 8, io + 8, 384 * sizeof(double), cudaMemcpyDeviceToHost, st.stream) != cudaSuccess;
+  if (!err) err = cudaStreamSynchronize(st.stream) != cudaSuccess;
+  if (err) {
+    fprintf(stderr, "QED_kernel_L%d: %s\n", variant, tl_err.c_str());
+    memset(out, 0, 384 * sizeof(double));
+    return;
+  }
+  memcpy(out, st.h_pin + 8, 384 * sizeof(double));
+}
+
+extern "C" void QED_kernel_L0(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                              double kerv[6][4][4][4])
+{
+  legacy(0, xv, yv, t, kerv);
+}
+extern "C" void QED_kernel_L1(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                              double kerv[6][4][4][4])
+{
+  legacy(1, xv, yv, t, kerv);
+}
+extern "C" void QED_kernel_L2(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                              double kerv[6][4][4][4])
+{
+  legacy(2, xv, yv, t, kerv);
+}
+extern "C" void QED_kernel_L3(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                              double kerv[6][4][4][4])
+{
+  legacy(3, xv, yv, t, kerv);
+}
+
+/* ------------------------------------------------------- lattice sums */
+
+/* per-site and per-x additive kernel terms of L1..L3 for the fused sum:
+   Lv(x,y) = L0(x,y) + Ky(y) + Bx(x) */
+static int lattice_terms(Ctx *c, int variant, const double *dx, size_t nx, const double *dy,
+                         size_t ny, double **Ky, double **Bx, cudaStream_t s, ThreadStage &st)
+{
+  *Ky = *Bx = nullptr;
+  if (variant == 0) return 0;
+  double *ky = st.d_aux.get(ny * 384 + ny * 4);
+  double *bx = st.d_aux2.get(nx * 384 * 2 + nx * 4);
+  if (!ky || !bx) return fail("out of device memory for lattice terms");
+  double *zy = ky + ny * 384;          /* ny zero vectors */
+  double *bt = bx + nx * 384;          /* nx*384 temporary */
+  double *zx = bt + nx * 384;          /* nx zero vectors */
+  CUDA_OK(launch_fill_pairs(nullptr, ny, 0, zy, s));
+  CUDA_OK(launch_fill_pairs(nullptr, nx, 0, zx, s));
+  switch (variant) {
+  case 1: /* L1 = L0(x,y) - L0(x,x)/2 - L0(y,y)/2 */
+    if (run_l0(c, dy, dy, ny, ky, nullptr, s) || run_l0(c, dx, dx, nx, bx, nullptr, s)) return 1;
+    CUDA_OK(launch_scale(ky, -0.5, ny * 384, s));
+    CUDA_OK(launch_scale(bx, -0.5, nx * 384, s));
+    break;
+  case 2: /* L2 = L0(x,y) - L0(0,y) - L0(x,0) */
+    if (run_l0(c, zy, dy, ny, ky, nullptr, s) || run_l0(c, dx, zx, nx, bx, nullptr, s)) return 1;
+    CUDA_OK(launch_scale(ky, -1.0, ny * 384, s));
+    CUDA_OK(launch_scale(bx, -1.0, nx * 384, s));
+    break;
+  case 3: /* L3 = L0(x,y) - L0(x,x) + L0(0,x) - L0(0,y) */
+    if (run_l0(c, zy, dy, ny, ky, nullptr, s) || run_l0(c, dx, dx, nx, bx, nullptr, s) ||
+        run_l0(c, zx, dx, nx, bt, nullptr, s))
+      return 1;
+    CUDA_OK(launch_scale(ky, -1.0, ny * 384, s));
+    CUDA_OK(launch_scale(bx, -1.0, nx * 384, s));
+    CUDA_OK(launch_axpy(bx, bt, 1.0, nx * 384, s));
+    break;
+  }
+  *Ky = ky;
+  *Bx = bx;
+  return 0;
+}
+
+extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t nx,
+                                    const double *d_x, size_t ny, const double *d_y,
+                                    const double *d_pi, double *d_sums, int precision, void *stream)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (check_variant_precision(variant, precision)) return 1;
+  if (nx == 0) return 0;
+  if (!d_x || !d_y || !d_pi || !d_sums) return fail("null buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  ThreadStage &st = stage_for(c);
+  double *Ky, *Bx;
+  if (lattice_terms(c, variant, d_x, nx, d_y, ny, &Ky, &Bx, s, st)) return 1;
+  const int wpb = c->cfg.warps_per_block;
+  const int tiles = (int)((ny + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32));
+  double *partial = st.d_tmp.get(nx * (size_t)std::max(tiles, 1) * 2);
+  if (!partial) return fail("out of device memory for partial sums");
+  LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, tiles};
+  CUDA_OK(launch_lattice_fp64(c->T, c->M, a, c->cfg, s));
+  CUDA_OK(launch_reduce_partials(partial, nx, tiles, d_sums, s));
+  return 0;
+}
+
+extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, size_t nx,
+                                const double *x, size_t ny, const double *y, const double *pi,
+                                double *sums, int precision)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (check_variant_precision(variant, precision)) return 1;
+  if (nx == 0) return 0;
+  if (!x || !y || !pi || !sums) return fail("null buffer");
+  ThreadStage &st = stage_for(c);
+  if (!st.stream) CUDA_OK(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking));
+  double *io = st.d_io.get(nx * 5 + ny * 4 + nx * ny * 384);
+  if (!io) return fail("out of device memory for %zu x %zu pairs", nx, ny);
+  double *dx = io, *dy = io + nx * 4, *ds = dy + ny * 4, *dpi = ds + nx;
+  CUDA_OK(cudaMemcpyAsync(dx, x, nx * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
+  CUDA_OK(cudaMemcpyAsync(dy, y, ny * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
+  CUDA_OK(cudaMemcpyAsync(dpi, pi, nx * ny * 384 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
+  if (kqed_lattice_sum_dev(t, variant, nx, dx, ny, dy, dpi, ds, precision, st.stream)) return 1;
+  CUDA_OK(cudaMemcpyAsync(sums, ds, nx * sizeof(double), cudaMemcpyDeviceToHost, st.stream));
+  CUDA_OK(cudaStreamSynchronize(st.stream));
+  return 0;
+}

@@ -1,0 +1,114 @@
+/*
+ * Internal interface between the host layer (kqed_host.cpp) and the CUDA
+ * kernels (kqed_fp64.cu).  Not installed; the public ABI is include/kqed.h.
+ */
+#ifndef KQED_INTERNAL_H
+#define KQED_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include <atomic>
+#include <stdint.h>
+
+namespace kqed {
+
+/* Weight-function tables, in the reference's FFidx order
+   (src/HEADERS/KQED.h:50-53). */
+enum {
+  QG0, QG1, QG2, QG3, QL4, QL2, dxQG0, dxQG1, dxQG2, dxQG3, dxQL4, dxQL2, d2xQG2, d2xQG3,
+  NFFA = 14
+};
+
+/* Slot of each table inside one 28-double node row.  Slots 0..7 are read by
+   interpolation pass 1 (QG0,QL2,QL4,QG1 with their x-derivative partners),
+   slots 8..13 by pass 2 (the QG2 and QG3 chains). */
+static const int kSlotOfTable[NFFA] = {
+    /*QG0*/ 0, /*QG1*/ 6, /*QG2*/ 8, /*QG3*/ 11, /*QL4*/ 4, /*QL2*/ 2,
+    /*dxQG0*/ 1, /*dxQG1*/ 7, /*dxQG2*/ 9, /*dxQG3*/ 12, /*dxQL4*/ 5, /*dxQL2*/ 3,
+    /*d2xQG2*/ 10, /*d2xQG3*/ 13};
+
+/* number of leading zero Chebyshev coefficients a table carries: the "mm"
+   shift of the reference's y-power scaling, src/LIBFILES/getff-new.c:126-128 */
+static const int kShiftOfTable[NFFA] = {0, 0, 1, 0, 1, 2, 0, 0, 1, 0, 1, 2, 1, 0};
+
+constexpr int kRow = 28;     /* doubles per (node, U-index) row: 14 tables x (value, y-derivative) */
+constexpr int kNKMax = 64;   /* max Chebyshev length incl. the shift (nfx + 2) */
+
+/* Device-resident tables.  `node` holds, for every grid node (ix, iy) and
+   Chebyshev index K (0..NK-1, U_K), the y-power-scaled coefficient of every
+   table and its y-derivative, precomputed once at load time:
+     node[((ix*nstpy + iy)*NK + K)*kRow + 2*slot + {0,1}]
+   This is the value/derivative pair the reference recomputes inside every
+   call (getff2, src/LIBFILES/getff-new.c:103-152); entries beyond a node's
+   length are zero. */
+struct DevTables {
+  const double *XX, *YY; /* grids */
+  const double *TX;      /* [23][ny_tay] TAYLORX */
+  const double *TY;      /* [14][nx_tay] TAYLORY */
+  const double *node;
+  const int *nfx;
+  int nstpx, nstpy, ny_tay, nx_tay, NK;
+  double ystp;
+};
+
+/* Warp schedule of one STV -> 384 linear map: rows sorted by length and dealt
+   to (round, lane) so the 32 lanes of a round do equal work. */
+constexpr int kMapRounds = 12;
+struct MapSched {
+  int len[kMapRounds];      /* steps in each round */
+  int off[kMapRounds];      /* first entry of each round (entries are [step][lane]) */
+  int total;                /* entries in total (multiple of 32) */
+};
+
+struct DevMaps {
+  const uint16_t *ent_gen, *ent_zero;   /* col | code<<8 */
+  const uint16_t *row_gen, *row_zero;   /* [round*32 + lane] -> output row */
+  MapSched gen, zero;
+};
+
+/* Launch parameters chosen by the host (and the autotuner). */
+struct LaunchCfg {
+  int warps_per_block;
+  int blocks;
+};
+
+/* Batched plain-FP64 L0: out[i][384] (or, when pi != NULL, the fused
+   contraction; see kqed_fp64.cu). */
+struct L0Args {
+  const double *x, *y;  /* [n][4] */
+  size_t n;
+  double *out;          /* [n][384] or NULL */
+  uint8_t *status;      /* [n] or NULL */
+};
+
+struct LatticeArgs {
+  const double *x;      /* [nx][4] */
+  const double *y;      /* [ny][4] */
+  size_t nx, ny;
+  const double *pi;     /* [nx][ny][384] */
+  const double *Ky;     /* [ny][384] per-site additive kernel terms or NULL */
+  const double *Bx;     /* [nx][384] per-x additive kernel terms or NULL */
+  double *partial;      /* [nx][tiles][2]  (sum, compensation) */
+  int tiles;            /* y tiles per x */
+};
+
+int upload_map_constants();
+cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a,
+                           const LaunchCfg &cfg, cudaStream_t s);
+cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                const LaunchCfg &cfg, cudaStream_t s);
+cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,
+                                   cudaStream_t s);
+cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStream_t s);
+cudaError_t launch_scale(double *y, double a, size_t n, cudaStream_t s);
+cudaError_t launch_mulam_axpy(double *y, const double *x, double a, size_t npairs,
+                              cudaStream_t s);
+cudaError_t launch_fill_pairs(const double *src, size_t n, int mode, double *dst,
+                              cudaStream_t s);
+size_t smem_bytes_l0(int warps_per_block);
+extern std::atomic<uint64_t> g_launches;
+
+} // namespace kqed
+
+#endif

@@ -1037,8 +1037,11 @@ static int tabd_y0(const double xv[4], double *tI, double *tII, double *tIII)
 {
   const double xsq = dot4(xv, xv);
   const double x = sqrt(fabs(xsq));
-  const int ix = bsrch(G.XX, x, 0, G.nstpx);
+  int ix = bsrch(G.XX, x, 0, G.nstpx);
   if (x > G.XX[G.nstpx - 1]) return 1;
+  /* |x| exactly on the last node: the reference reads XX[nstpx] here
+     (one past its grid); interpolate from the last interval instead */
+  if (ix == G.nstpx - 1) ix = G.nstpx - 2;
   const int ix2 = ix + 1;
   const double ax = (G.XX[ix2] - x) / (G.XX[ix2] - G.XX[ix]);
   const double xa = G.XX[ix], xb = G.XX[ix2];
@@ -1105,8 +1108,13 @@ static inline int is_zero(const double *v) { return (v[0] * v[0] + v[1] * v[1] +
 /* QED_kernel_L0, src/LIBFILES/kernels.c:81-115; returns the branch code */
 static int L0(const double xv[4], const double yv[4], double *out)
 {
-  const int x0 = is_zero(xv), y0 = is_zero(yv);
   memset(out, 0, 384 * sizeof(double));
+  /* non-finite input: zero kernel, reported as out of grid (the reference's
+     grid search would run off its tables) */
+  if (!isfinite(fabs(xv[0]) + fabs(xv[1]) + fabs(xv[2]) + fabs(xv[3]) + fabs(yv[0]) +
+                fabs(yv[1]) + fabs(yv[2]) + fabs(yv[3])))
+    return 16 | 4;
+  const int x0 = is_zero(xv), y0 = is_zero(yv);
   if (x0 && y0) return 0;
   if (x0) return kernel_axis(yv, 1, out) ? 16 | 1 : 1;
   if (y0) return kernel_axis(xv, 0, out) ? 16 | 2 : 2;

@@ -1,0 +1,150 @@
+"""The C-ABI library: it loads, exports every entry point include/kqed.h
+declares, keeps the reference's struct layout, and reports load errors the
+way the reference does (return 1, message).  CPU only: no kernel runs."""
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HDR = os.path.join(ROOT, "include", "kqed.h")
+REF_HDR = "/root/reference/src/HEADERS/KQED.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from kqed_gb300 import build as B
+    B.build()
+    import kqed_gb300
+    return kqed_gb300.lib()
+
+
+def declared_functions():
+    src = open(HDR).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\**\s*([A-Za-z_][A-Za-z0-9_]*)\s*\(", src,
+                       flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_reference_api():
+    names = declared_functions()
+    for n in ["initialise", "free_QED_temps", "QED_kernel_L0", "QED_kernel_L1", "QED_kernel_L2",
+              "QED_kernel_L3", "kqed_kernel_batch", "kqed_lattice_sum"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib._name], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(l.split()[-1] for l in out.splitlines() if l.strip())
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+
+
+def _offsets_c(include_dir, header, tmpdir):
+    prog = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "%s"
+int main(void){
+  printf("%%zu %%zu %%zu %%zu %%zu %%zu %%zu %%zu\n", sizeof(struct QED_kernel_temps),
+    offsetof(struct QED_kernel_temps, G8), offsetof(struct Grid_coeffs, XX),
+    offsetof(struct Grid_coeffs, nstpx), offsetof(struct Grid_coeffs, TX),
+    offsetof(struct Grid_coeffs, TY), offsetof(struct Grid_coeffs, PC),
+    offsetof(struct Grid_coeffs, nfx));
+  return 0; }
+''' % header
+    c = os.path.join(tmpdir, "off.c")
+    open(c, "w").write(prog)
+    exe = os.path.join(tmpdir, "off")
+    subprocess.run(["gcc", "-I", include_dir, "-o", exe, c], check=True, capture_output=True)
+    return subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+
+
+def test_struct_layout_matches_ctypes(tmp_path):
+    import kqed_gb300 as K
+    got = _offsets_c(os.path.dirname(HDR), "kqed.h", str(tmp_path))
+    T, G = K.QED_kernel_temps, K.Grid_coeffs
+    want = [ctypes.sizeof(T), T.G8.offset, G.XX.offset, G.nstpx.offset, G.TX.offset,
+            G.TY.offset, G.PC.offset, G.nfx.offset]
+    assert [int(v) for v in got] == want
+
+
+@pytest.mark.skipif(not os.path.exists(REF_HDR), reason="reference headers not present")
+def test_struct_layout_matches_reference(tmp_path):
+    """sizeof/offsets of struct QED_kernel_temps equal the reference's
+    (src/HEADERS/KQED.h:69-93), so it can be passed by value unchanged"""
+    inc = tmp_path / "inc"
+    inc.mkdir()
+    shutil.copy(os.path.join(ROOT, "oracle", "ref", "config.h"), inc / "config.h")
+    prog_inc = "-I" + os.path.dirname(REF_HDR)
+    ours = _offsets_c(os.path.dirname(HDR), "kqed.h", str(tmp_path))
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "KQED.h"
+int main(void){
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(struct QED_kernel_temps),
+    offsetof(struct QED_kernel_temps, G8), offsetof(struct Grid_coeffs, XX),
+    offsetof(struct Grid_coeffs, nstpx), offsetof(struct Grid_coeffs, TX),
+    offsetof(struct Grid_coeffs, TY), offsetof(struct Grid_coeffs, PC),
+    offsetof(struct Grid_coeffs, nfx));
+  return 0; }
+'''
+    (tmp_path / "r.c").write_text(src)
+    subprocess.run(["gcc", "-I", str(inc), prog_inc, "-o", str(tmp_path / "r"),
+                    str(tmp_path / "r.c")], check=True, capture_output=True)
+    ref = subprocess.run([str(tmp_path / "r")], capture_output=True, text=True,
+                         check=True).stdout.split()
+    assert ours == ref
+
+
+def test_initialise_rejects_a_corrupt_table(lib, tmp_path):
+    import kqed_gb300 as K
+    pkg = os.path.dirname(K.__file__)
+    d = tmp_path / "PRECOMP"
+    d.mkdir()
+    for n in ["taylorx_cksum.bin", "taylory_cksum.bin"]:
+        shutil.copy(os.path.join(pkg, "PRECOMP", n), d / n)
+    b = bytearray(open(os.path.join(pkg, "PRECOMP", "FFxy_single_cksum.bin"), "rb").read())
+    b[-100] ^= 1
+    (d / "FFxy_single_cksum.bin").write_bytes(bytes(b))
+    old = os.environ.get("KQED_LIB_PATH")
+    os.environ["KQED_LIB_PATH"] = str(tmp_path)
+    try:
+        t = K.QED_kernel_temps()
+        assert lib.initialise(ctypes.byref(t)) == 1
+        assert b"checksum" in lib.kqed_last_error()
+        assert not t.Grid.PC
+    finally:
+        if old is None:
+            del os.environ["KQED_LIB_PATH"]
+        else:
+            os.environ["KQED_LIB_PATH"] = old
+
+
+def test_initialise_reports_missing_table(lib, tmp_path):
+    import kqed_gb300 as K
+    old = os.environ.get("KQED_LIB_PATH")
+    os.environ["KQED_LIB_PATH"] = str(tmp_path)
+    try:
+        t = K.QED_kernel_temps()
+        assert lib.initialise(ctypes.byref(t)) == 1
+        assert b"Cannot find" in lib.kqed_last_error()
+    finally:
+        if old is None:
+            del os.environ["KQED_LIB_PATH"]
+        else:
+            os.environ["KQED_LIB_PATH"] = old
+
+
+def test_batch_rejects_uninitialised_tables(lib):
+    import kqed_gb300 as K
+    t = K.QED_kernel_temps()
+    dp = ctypes.POINTER(ctypes.c_double)
+    assert lib.kqed_kernel_batch(ctypes.byref(t), 0, 0, None, None, None, None, 0) == 1
+    assert b"not initialised" in lib.kqed_last_error()
