@@ -1,0 +1,376 @@
+#!/usr/bin/env python3
+"""Benchmark: (x,y) kernel evaluations/s of the fused lattice integrand.
+
+Workload (one step): periodic 24^4 lattice, spacing 0.1, 32 points x_k along
+the (1,1,1,1) diagonal, y over all 331,776 sites, kernel L2, synthetic
+Pi(x,y) = N(0,1) exp(-|y|/2) exp(-|x-y|/2) of 384 float64 components, and
+the fused sum_y sum_c L2_c(x,y) Pi_c(x,y) per x.  One evaluation = one (x,y)
+term.  Pi is 32.6 GB per step, far larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` times the device entry point with
+inputs resident in HBM; `e2e` times the host entry point (Pi copied from
+pinned host memory every step).  --impl reference times the reference's CPU
+implementation of the same computation on the host cores (the reference
+library compiled from its sources when it is available here, else the CPU
+restatement under oracle/).
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("(x,y) kernel evals/s on 1 GB300: plain FP64 vs FP32/surrogate at "
+          "≤1e-6 rel err")
+UNIT = "evals/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--precision", default="fp64", choices=["fp64"])
+    p.add_argument("--L", type=int, default=24)
+    p.add_argument("--spacing", type=float, default=0.1)
+    p.add_argument("--nx", type=int, default=32)
+    p.add_argument("--variant", type=int, default=2)
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def x_direction(rank):
+    """Weak scaling: rank r evaluates the same number of x points along its own
+    diagonal (sign pattern of r), so every rank carries identical work."""
+    s = [1.0, 1.0, 1.0, 1.0]
+    for b in range(4):
+        if (rank >> b) & 1:
+            s[3 - b] = -1.0
+    return np.array(s)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.dev)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_impl():
+    """(ctypes lib, kind): the reference library built from its sources when
+    present (x86 only), else the CPU restatement."""
+    ref = os.path.join(ROOT, "oracle", "_ref", "libkqedref_avx.so")
+    if os.path.exists(ref):
+        try:
+            os.environ["KQEDREF_PATH"] = os.path.join(ROOT, "kqed_gb300")
+            L = ctypes.CDLL(ref)
+            if L.ref_init() == 0:
+                def contract(v, x, y, pi, nt):
+                    dp = ctypes.POINTER(ctypes.c_double)
+                    d = np.zeros(len(x))
+                    L.ref_contract(v, len(x), x.ctypes.data_as(dp), y.ctypes.data_as(dp),
+                                   pi.ctypes.data_as(dp), d.ctypes.data_as(dp), nt)
+                    return d
+                return contract, "reference"
+        except OSError:
+            pass
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _helpers import oracle_contract
+
+    def contract(v, x, y, pi, nt):
+        return oracle_contract(v, x, y, pi, nt)
+    return contract, "port"
+
+
+def cpu_sample(args, xs, ys, pi_host_fn, steps=1):
+    """Time the CPU implementation on a bounded sample of the workload: a few
+    x points against all sites.  Returns (evals/s, cores, kind, sample)."""
+    contract, kind = cpu_impl()
+    cores = os.cpu_count() or 1
+    ks = [len(xs) // 4, len(xs) // 2, (3 * len(xs)) // 4] if len(xs) >= 4 else [0]
+    best = None
+    for _ in range(steps):
+        t_tot, n_tot = 0.0, 0
+        for k in ks:
+            pik = pi_host_fn(k)
+            X = np.ascontiguousarray(np.repeat(xs[k:k + 1], len(ys), 0))
+            t0 = time.perf_counter()
+            contract(args.variant, X, ys, pik, cores)
+            t_tot += time.perf_counter() - t0
+            n_tot += len(ys)
+        rate = n_tot / t_tot
+        best = rate if best is None else max(best, rate)
+    sample = "%d x points (k=%s) x %d sites, L%d contraction, %d threads" % (
+        len(ks), ",".join(str(k) for k in ks), len(ys), args.variant, cores)
+    return best, cores, kind, sample
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from kqed_gb300 import build as B
+    from kqed_gb300.workloads import diagonal_x, lattice_sites, pi_envelope
+    os.makedirs(B.OUT, exist_ok=True)
+    B.ensure_table(B.build_synth())
+    xs = diagonal_x(args.nx, args.spacing)
+    ys = lattice_sites(args.L, args.spacing)
+
+    def pi_host(k):
+        rng = np.random.default_rng(1000 + k)
+        env = pi_envelope(xs[k:k + 1], ys)[0]
+        return rng.standard_normal((len(ys), 384)) * env[:, None]
+
+    cache = {}
+
+    def pi_cached(k):
+        if k not in cache:
+            cache[k] = pi_host(k)
+        return cache[k]
+
+    for _ in range(args.warmup):
+        cpu_sample(args, xs, ys, pi_cached, steps=1)
+    rates = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, cores, kind, sample = cpu_sample(args, xs, ys, pi_cached, steps=1)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * wall / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(args, len(ys)),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, ny):
+    return {"workload": "fused lattice integrand: kernel L%d, periodic %d^4 lattice, spacing %g, "
+                        "%d x points on the diagonal, sum over all sites of L.Pi"
+                        % (args.variant, args.L, args.spacing, args.nx),
+            "lattice_L": args.L, "spacing": args.spacing, "nx": args.nx, "ny": ny,
+            "variant": "L%d" % args.variant, "precision": args.precision,
+            "l2": "inputs larger than L2 (Pi is %.1f GB per step)" % (args.nx * ny * 384 * 8 / 1e9)}
+
+
+def run_gb300(args):
+    import torch
+
+    import kqed_gb300 as K
+    from kqed_gb300 import flops as F
+    from kqed_gb300.workloads import diagonal_x, lattice_sites, pi_synth_torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    t = K.KernelTemps()
+    g = t.grid()
+    prec = {"fp64": K.KQED_FP64}[args.precision]
+
+    xs = diagonal_x(args.nx, args.spacing) * x_direction(rank)[None, :]
+    ys = lattice_sites(args.L, args.spacing)
+    nx, ny = len(xs), len(ys)
+    dx = torch.as_tensor(xs, dtype=torch.float64, device=dev)
+    dy = torch.as_tensor(ys, dtype=torch.float64, device=dev)
+    pi = pi_synth_torch(xs, ys, seed=2 + rank, device=dev)
+    sums = torch.empty(nx, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        K.lattice_sum_dev(t, args.variant, dx.data_ptr(), nx, dy.data_ptr(), ny, pi.data_ptr(),
+                          sums.data_ptr(), prec, stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+
+    # ---- device-resident timing
+    clocks = ClockSampler(dev.index if dev.index is not None else 0)
+    barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    time.sleep(0.3)
+    K.profile(True)
+    l0 = K.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    clk = clocks.stop()
+    launches = K.launch_count() - l0
+    ms_total = e0.elapsed_time(e1)
+    kern_ms, kern_n = K.profile_read()
+    K.profile(False)
+    ms_step = ms_total / args.steps
+    if world > 1:
+        mt = torch.tensor([ms_step], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(mt, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(mt.item())
+    value = world * nx * ny / (ms_step / 1e3)
+
+    # ---- roofline of the dominant kernel (the fused lattice kernel)
+    peak_gflops = K.fp64_peak_gflops()
+    flops_launch = F.lattice_flops(xs, ys, g["XX"], g["nfx"], args.variant)
+    kavg_ms = kern_ms / max(kern_n, 1)
+    achieved = flops_launch / (kavg_ms / 1e3) / 1e12
+
+    # ---- end to end through the host entry point (Pi from pinned memory)
+    pi_host = torch.empty(pi.shape, dtype=torch.float64, pin_memory=True)
+    pi_host.copy_(pi)
+    del pi
+    torch.cuda.empty_cache()
+    xh = np.ascontiguousarray(xs)
+    yh = np.ascontiguousarray(ys)
+    sh = np.zeros(nx)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib = K.lib()
+
+    def e2e_step():
+        rc = lib.kqed_lattice_sum(t.ptr, args.variant, nx, xh.ctypes.data_as(dp), ny,
+                                  yh.ctypes.data_as(dp),
+                                  ctypes.cast(pi_host.data_ptr(), dp), sh.ctypes.data_as(dp), prec)
+        if rc != 0:
+            raise RuntimeError(lib.kqed_last_error().decode())
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    if world > 1:
+        mt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(mt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(mt.item())
+    e2e = {"value": world * nx * ny / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(pi_host.numel() * 8 + xh.nbytes + yh.nbytes),
+           "d2h_bytes_per_step": int(sh.nbytes)}
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        def pi_k(k):
+            return pi_host[k].numpy()
+        r, cores, kind, sample = cpu_sample(args, xs, ys, pi_k, steps=1)
+        cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp64": "f64"}[args.precision], "data": "synthetic",
+            "config": workload_config(args, ny),
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_gflops / 1e3,
+                         "unit": "TFLOP/s", "frac": achieved / (peak_gflops / 1e3),
+                         "traffic": None,
+                         "kernel": "lattice_fp64_kernel", "kernel_ms": kavg_ms,
+                         "flops_per_launch": flops_launch,
+                         "flops_source": F.table().get("source"),
+                         "peak_source": "FP64 FMA-chain probe run by this bench (not in "
+                                        "MEASURED_PEAKS.json)"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "checksum": [float(v) for v in sh[:4]],
+        }
+        print(json.dumps(line), flush=True)
+    t.free()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -91,6 +91,12 @@ def lib():
         L.kqed_lattice_sum_dev.restype = ctypes.c_int
         L.kqed_last_error.restype = ctypes.c_char_p
         L.kqed_launch_count.restype = ctypes.c_uint64
+        L.kqed_profile.argtypes = [ctypes.c_int]
+        L.kqed_profile.restype = None
+        L.kqed_profile_read.argtypes = [dp, ctypes.POINTER(ctypes.c_uint64)]
+        L.kqed_profile_read.restype = ctypes.c_int
+        L.kqed_fp64_peak_gflops.argtypes = [dp]
+        L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -221,3 +227,22 @@ def lattice_sum_dev(t, variant, x_ptr, nx, y_ptr, ny, pi_ptr, sums_ptr, precisio
 
 def launch_count():
     return int(lib().kqed_launch_count())
+
+
+def profile(enable):
+    """Start (True) or stop (False) event timing of the main kernels."""
+    lib().kqed_profile(1 if enable else 0)
+
+
+def profile_read():
+    """(total milliseconds, launches) of the main kernels since profile(True)."""
+    ms = ctypes.c_double()
+    n = ctypes.c_uint64()
+    _check(lib().kqed_profile_read(ctypes.byref(ms), ctypes.byref(n)))
+    return ms.value, int(n.value)
+
+
+def fp64_peak_gflops():
+    g = ctypes.c_double()
+    _check(lib().kqed_fp64_peak_gflops(ctypes.byref(g)))
+    return g.value

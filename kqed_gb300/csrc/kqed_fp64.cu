@@ -1278,6 +1278,22 @@ __global__ void fill_pairs_kernel(const double *src, size_t n, int mode, double 
     dst[j] = mode ? src[j] : 0.0;
 }
 
+/* FP64 FMA throughput probe: 8 independent FMA chains per thread */
+__global__ void dfma_probe_kernel(double *out, int iters, double a, double b)
+{
+  double v[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) v[c] = threadIdx.x * 1e-3 + c;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) v[c] = fma(v[c], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) s += v[c];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 static int num_sms()
 {
   static int n = 0;
@@ -1343,6 +1359,36 @@ cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStre
   axpy_kernel<<<(unsigned)b, 256, 0, s>>>(y, x, a, n);
   g_launches++;
   return cudaGetLastError();
+}
+
+cudaError_t probe_fp64_peak(double *gflops)
+{
+  const int blocks = num_sms() * 8, threads = 256, iters = 256;
+  double *out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(double) * blocks * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  dfma_probe_kernel<<<blocks, threads>>>(out, 16, 0.999999, 1e-7);
+  cudaDeviceSynchronize();
+  float best = 1e30f;
+  for (int r = 0; r < 5; r++) {
+    cudaEventRecord(e0);
+    dfma_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  g_launches += 6;
+  *gflops = 2.0 * 8 * (double)iters * blocks * threads / best / 1e6;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  e = cudaGetLastError();
+  cudaFree(out);
+  return e;
 }
 
 cudaError_t launch_scale(double *y, double a, size_t n, cudaStream_t s)

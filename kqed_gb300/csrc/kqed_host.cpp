@@ -46,14 +46,72 @@ static int fail(const char *fmt, ...)
   return 1;
 }
 
-extern "C" const char *kqed_last_error(void) { return tl_err.c_str(); }
-extern "C" uint64_t kqed_launch_count(void) { return kqed::g_launches; }
-
 #define CUDA_OK(call)                                                                      \
   do {                                                                                     \
     cudaError_t e_ = (call);                                                               \
     if (e_ != cudaSuccess) return fail("%s: %s", #call, cudaGetErrorString(e_));           \
   } while (0)
+
+extern "C" const char *kqed_last_error(void) { return tl_err.c_str(); }
+extern "C" uint64_t kqed_launch_count(void) { return kqed::g_launches; }
+
+/* ------------------------------------------------------ kernel timing */
+
+/* CUDA events recorded on the launching stream around every main kernel
+   (the fused lattice kernel and the batched L0 kernel) while enabled */
+namespace {
+struct TimedLaunch { cudaEvent_t a, b; };
+std::mutex g_prof_mu;
+std::vector<TimedLaunch> g_prof;
+std::atomic<int> g_prof_on{0};
+} // namespace
+
+static void prof_begin(cudaStream_t s, TimedLaunch &tl)
+{
+  tl.a = tl.b = nullptr;
+  if (!g_prof_on) return;
+  cudaEventCreate(&tl.a);
+  cudaEventCreate(&tl.b);
+  cudaEventRecord(tl.a, s);
+}
+
+static void prof_end(cudaStream_t s, TimedLaunch &tl)
+{
+  if (!tl.a) return;
+  cudaEventRecord(tl.b, s);
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  g_prof.push_back(tl);
+}
+
+extern "C" void kqed_profile(int enable)
+{
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  for (auto &t : g_prof) { cudaEventDestroy(t.a); cudaEventDestroy(t.b); }
+  g_prof.clear();
+  g_prof_on = enable ? 1 : 0;
+}
+
+extern "C" int kqed_profile_read(double *total_ms, uint64_t *launches)
+{
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  double tot = 0;
+  for (auto &t : g_prof) {
+    if (cudaEventSynchronize(t.b) != cudaSuccess) return fail("event sync failed");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t.a, t.b);
+    tot += ms;
+  }
+  *total_ms = tot;
+  *launches = g_prof.size();
+  return 0;
+}
+
+extern "C" int kqed_fp64_peak_gflops(double *gflops)
+{
+  CUDA_OK(probe_fp64_peak(gflops));
+  return 0;
+}
+
 
 /* ---------------------------------------------------------- context */
 
@@ -459,10 +517,13 @@ static int check_variant_precision(int variant, int precision)
 
 /* L0 over n pairs on the device */
 static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *dout,
-                  uint8_t *dstatus, cudaStream_t s)
+                  uint8_t *dstatus, cudaStream_t s, bool timed = true)
 {
   L0Args a{dx, dy, n, dout, dstatus};
+  TimedLaunch tl{nullptr, nullptr};
+  if (timed) prof_begin(s, tl);
   CUDA_OK(launch_l0_fp64(c->T, c->M, a, c->cfg, s));
+  prof_end(s, tl);
   return 0;
 }
 
@@ -624,18 +685,18 @@ static int lattice_terms(Ctx *c, int variant, const double *dx, size_t nx, const
   CUDA_OK(launch_fill_pairs(nullptr, nx, 0, zx, s));
   switch (variant) {
   case 1: /* L1 = L0(x,y) - L0(x,x)/2 - L0(y,y)/2 */
-    if (run_l0(c, dy, dy, ny, ky, nullptr, s) || run_l0(c, dx, dx, nx, bx, nullptr, s)) return 1;
+    if (run_l0(c, dy, dy, ny, ky, nullptr, s, false) || run_l0(c, dx, dx, nx, bx, nullptr, s, false)) return 1;
     CUDA_OK(launch_scale(ky, -0.5, ny * 384, s));
     CUDA_OK(launch_scale(bx, -0.5, nx * 384, s));
     break;
   case 2: /* L2 = L0(x,y) - L0(0,y) - L0(x,0) */
-    if (run_l0(c, zy, dy, ny, ky, nullptr, s) || run_l0(c, dx, zx, nx, bx, nullptr, s)) return 1;
+    if (run_l0(c, zy, dy, ny, ky, nullptr, s, false) || run_l0(c, dx, zx, nx, bx, nullptr, s, false)) return 1;
     CUDA_OK(launch_scale(ky, -1.0, ny * 384, s));
     CUDA_OK(launch_scale(bx, -1.0, nx * 384, s));
     break;
   case 3: /* L3 = L0(x,y) - L0(x,x) + L0(0,x) - L0(0,y) */
-    if (run_l0(c, zy, dy, ny, ky, nullptr, s) || run_l0(c, dx, dx, nx, bx, nullptr, s) ||
-        run_l0(c, zx, dx, nx, bt, nullptr, s))
+    if (run_l0(c, zy, dy, ny, ky, nullptr, s, false) || run_l0(c, dx, dx, nx, bx, nullptr, s, false) ||
+        run_l0(c, zx, dx, nx, bt, nullptr, s, false))
       return 1;
     CUDA_OK(launch_scale(ky, -1.0, ny * 384, s));
     CUDA_OK(launch_scale(bx, -1.0, nx * 384, s));
@@ -665,7 +726,10 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
   double *partial = st.d_tmp.get(nx * (size_t)std::max(tiles, 1) * 2);
   if (!partial) return fail("out of device memory for partial sums");
   LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, tiles};
+  TimedLaunch tl;
+  prof_begin(s, tl);
   CUDA_OK(launch_lattice_fp64(c->T, c->M, a, c->cfg, s));
+  prof_end(s, tl);
   CUDA_OK(launch_reduce_partials(partial, nx, tiles, d_sums, s));
   return 0;
 }

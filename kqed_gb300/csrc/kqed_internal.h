@@ -107,6 +107,7 @@ cudaError_t launch_mulam_axpy(double *y, const double *x, double a, size_t npair
 cudaError_t launch_fill_pairs(const double *src, size_t n, int mode, double *dst,
                               cudaStream_t s);
 size_t smem_bytes_l0(int warps_per_block);
+cudaError_t probe_fp64_peak(double *gflops);
 extern std::atomic<uint64_t> g_launches;
 
 } // namespace kqed
