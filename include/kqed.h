@@ -136,6 +136,21 @@ int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t n
                          const double *d_x, size_t ny, const double *d_y, const double *d_pi,
                          double *d_sums, int precision, void *stream);
 
+/* The fused lattice sum for callers that cannot allocate GPU memory (codes
+   whose own pool owns the device; loops where cudaMalloc's implicit device
+   synchronisation would stall other streams).  It has no counterpart in the
+   reference.  Same arguments and results as kqed_lattice_sum_dev, but its
+   scratch comes from a static 16 MiB device array compiled into the library
+   (held by every GPU that loads it), so problems needing more scratch are
+   rejected with an error: nx * ceil(ny / 64) * 2 doubles, plus, for L1..L3,
+   388 * ny + 772 * nx doubles, must not exceed 2,097,152.  The first call on
+   a device looks up the array's device address; make it before any stream
+   capture.  Calls share the array: calls that overlap on the GPU race and
+   must be serialised by the caller.  Allocates nothing. */
+int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int variant, size_t nx,
+                             const double *d_x, size_t ny, const double *d_y, const double *d_pi,
+                             double *d_sums, void *stream);
+
 /* Message of the last error on the calling thread ("" if none). */
 const char *kqed_last_error(void);
 

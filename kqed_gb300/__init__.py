@@ -89,6 +89,10 @@ def lib():
                                            ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.kqed_lattice_sum_dev.restype = ctypes.c_int
+        L.kqed_lattice_sum_noalloc.argtypes = [T, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
+                                               ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p]
+        L.kqed_lattice_sum_noalloc.restype = ctypes.c_int
         L.kqed_last_error.restype = ctypes.c_char_p
         L.kqed_launch_count.restype = ctypes.c_uint64
         L.kqed_profile.argtypes = [ctypes.c_int]
@@ -223,6 +227,13 @@ def lattice_sum_dev(t, variant, x_ptr, nx, y_ptr, ny, pi_ptr, sums_ptr, precisio
                     stream=None):
     _check(lib().kqed_lattice_sum_dev(t.ptr, variant, nx, x_ptr, ny, y_ptr, pi_ptr, sums_ptr,
                                       precision, stream))
+
+
+def lattice_sum_noalloc(t, variant, x_ptr, nx, y_ptr, ny, pi_ptr, sums_ptr, stream=None):
+    """kqed_lattice_sum_noalloc: the device-pointer lattice sum with its scratch
+    in a static 16 MiB device array (for callers that cannot allocate)."""
+    _check(lib().kqed_lattice_sum_noalloc(t.ptr, variant, nx, x_ptr, ny, y_ptr, pi_ptr,
+                                          sums_ptr, stream))
 
 
 def launch_count():

@@ -76,14 +76,16 @@ def ensure_table(exe):
 def build_lib(verbose=False):
     so = os.path.join(OUT, "libkqed_gb300.so")
     cu = os.path.join(CSRC, "kqed_fp64.cu")
+    cu2 = os.path.join(CSRC, "kqed_noalloc.cu")
     host = os.path.join(CSRC, "kqed_host.cpp")
     crc = os.path.join(CSRC, "kqed_crc32c.c")
     hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
     hdrs.append(os.path.join(ROOT, "include", "kqed.h"))
-    if _newer(so, [cu, host, crc] + hdrs):
+    if _newer(so, [cu, cu2, host, crc] + hdrs):
         return so
     lib_default = '-DKQED_DEFAULT_LIB_PATH="%s"' % HERE
     o_cu = os.path.join(OUT, "kqed_fp64.o")
+    o_cu2 = os.path.join(OUT, "kqed_noalloc.o")
     o_host = os.path.join(OUT, "kqed_host.o")
     o_crc = os.path.join(OUT, "kqed_crc32c.o")
     jobs = [
@@ -92,12 +94,14 @@ def build_lib(verbose=False):
         ["g++"] + HOST_FLAGS + [lib_default, "-I" + os.path.join(CUDA_HOME, "include"),
                                 "-c", host, "-o", o_host],
         ["gcc", "-O2", "-fPIC", "-std=gnu11", "-c", crc, "-o", o_crc],
+        [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu2,
+                         "-o", o_cu2],
     ]
-    with cf.ThreadPoolExecutor(3) as ex:
+    with cf.ThreadPoolExecutor(4) as ex:
         results = list(ex.map(_run, jobs))
     if verbose:
         sys.stderr.write(results[0].stderr)
-    _run([NVCC] + ARCH + ["-shared", "-o", so, o_cu, o_host, o_crc, "-lcudart"])
+    _run([NVCC] + ARCH + ["-shared", "-o", so, o_cu, o_cu2, o_host, o_crc, "-lcudart"])
     return so
 
 

@@ -756,3 +756,25 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
   CUDA_OK(cudaStreamSynchronize(st.stream));
   return 0;
 }
+
+/* ---------------------------------------------- internal accessors */
+
+namespace kqed {
+
+int ctx_handles(const struct QED_kernel_temps *t, DevTables *T, DevMaps *M, LaunchCfg *cfg)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return 1;
+  *T = c->T;
+  *M = c->M;
+  *cfg = c->cfg;
+  return 0;
+}
+
+int set_error(const char *msg)
+{
+  tl_err = msg;
+  return 1;
+}
+
+} // namespace kqed

@@ -11,6 +11,8 @@
 #include <atomic>
 #include <stdint.h>
 
+struct QED_kernel_temps;
+
 namespace kqed {
 
 /* Weight-function tables, in the reference's FFidx order
@@ -109,6 +111,11 @@ cudaError_t launch_fill_pairs(const double *src, size_t n, int mode, double *dst
 size_t smem_bytes_l0(int warps_per_block);
 cudaError_t probe_fp64_peak(double *gflops);
 extern std::atomic<uint64_t> g_launches;
+
+/* device handles of an initialised struct QED_kernel_temps (0 on success) */
+int ctx_handles(const struct QED_kernel_temps *t, DevTables *T, DevMaps *M, LaunchCfg *cfg);
+/* record an error message for kqed_last_error(); returns 1 */
+int set_error(const char *msg);
 
 } // namespace kqed
 

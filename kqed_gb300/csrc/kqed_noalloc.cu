@@ -1,0 +1,149 @@
+/*
+ * kqed_lattice_sum_noalloc: the fused lattice sum without any device memory
+ * allocation.
+ *
+ * Some callers of this library cannot allocate GPU memory at the moment they
+ * need the lattice sum: lattice QCD codes that hand the whole device to their
+ * own memory pool at start-up and forbid foreign allocations, and tight loops
+ * in which cudaMalloc/cudaFree would synchronise the device and stall the
+ * caller's other streams.  kqed_lattice_sum_dev obtains its scratch (partial
+ * sums per tile, the per-site and per-x kernel terms of L1..L3) with
+ * cudaMalloc on first use; this entry point takes it from a fixed array
+ * compiled into the library instead:
+ *
+ *   - the scratch is a file-scope static __device__ array of
+ *     kNoallocDoubles doubles (16 MiB); every GPU that loads the library
+ *     holds it until the process exits;
+ *   - host code never uses the array's name as a device address (on the host
+ *     it is only a stand-in symbol): the device address is obtained once per
+ *     device with cudaGetSymbolAddress, with that device current, on the
+ *     first call made on that device.  Make that first call before any
+ *     stream capture;
+ *   - problems whose scratch does not fit are rejected with an error that
+ *     states the need and the limit; nothing is allocated, here or in any
+ *     library routine this function calls;
+ *   - all calls share the one array and it keeps the last call's contents.
+ *     Everything a call reads from it is first written by the same call (the
+ *     zero vectors are cleared by a kernel, partial sums and kernel terms are
+ *     fully overwritten), but calls that overlap on the GPU -- on different
+ *     streams, or from different host threads -- race on the array and must
+ *     be serialised by the caller.
+ *
+ * Results are those of kqed_lattice_sum_dev: the same kernels, the same
+ * reduction order.
+ */
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/kqed.h"
+#include "kqed_internal.h"
+
+namespace {
+
+constexpr size_t kNoallocDoubles = (size_t)2 << 20; /* 2,097,152 doubles = 16 MiB */
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoallocDoubles];
+
+constexpr int kMaxDevices = 64;
+double *g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mu;
+
+/* device address of the static scratch on the current device (set up once
+   per device with cudaGetSymbolAddress) */
+int scratch_on_current_device(double **out)
+{
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return kqed::set_error("kqed_lattice_sum_noalloc: no usable current CUDA device");
+  std::lock_guard<std::mutex> g(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      char msg[256];
+      snprintf(msg, sizeof(msg), "kqed_lattice_sum_noalloc: cudaGetSymbolAddress failed: %s",
+               cudaGetErrorString(e));
+      return kqed::set_error(msg);
+    }
+    g_scratch_addr[dev] = static_cast<double *>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return 0;
+}
+
+int l0(const kqed::DevTables &T, const kqed::DevMaps &M, const kqed::LaunchCfg &cfg,
+       const double *dx, const double *dy, size_t n, double *out, cudaStream_t s)
+{
+  kqed::L0Args a{dx, dy, n, out, nullptr};
+  return kqed::launch_l0_fp64(T, M, a, cfg, s) != cudaSuccess;
+}
+
+} // namespace
+
+extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int variant, size_t nx,
+                                        const double *d_x, size_t ny, const double *d_y,
+                                        const double *d_pi, double *d_sums, void *stream)
+{
+  kqed::DevTables T;
+  kqed::DevMaps M;
+  kqed::LaunchCfg cfg;
+  if (kqed::ctx_handles(t, &T, &M, &cfg)) return kqed::set_error("tables not initialised");
+  if (variant < 0 || variant > 3) return kqed::set_error("variant not in 0..3");
+  if (nx == 0) return 0;
+  if (!d_x || !d_y || !d_pi || !d_sums) return kqed::set_error("null buffer");
+  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
+  const size_t tiles = (ny + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32);
+  const size_t n_partial = nx * (tiles ? tiles : 1) * 2;
+  const size_t n_terms = variant ? ny * 384 + ny * 4 + nx * 384 * 2 + nx * 4 : 0;
+  const size_t need = n_partial + n_terms;
+  if (need > kNoallocDoubles) {
+    char msg[320];
+    snprintf(msg, sizeof(msg),
+             "kqed_lattice_sum_noalloc: %zu x points x %zu sites (L%d) need %zu doubles of "
+             "scratch; the static limit is %zu doubles (16 MiB). Use kqed_lattice_sum_dev.",
+             nx, ny, variant, need, kNoallocDoubles);
+    return kqed::set_error(msg);
+  }
+  double *S = nullptr;
+  if (scratch_on_current_device(&S)) return 1;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double *partial = S;
+  double *Ky = nullptr, *Bx = nullptr;
+  if (variant) {
+    Ky = partial + n_partial;
+    double *zy = Ky + ny * 384;
+    Bx = zy + ny * 4;
+    double *bt = Bx + nx * 384;
+    double *zx = bt + nx * 384;
+    int bad = kqed::launch_fill_pairs(nullptr, ny, 0, zy, s) != cudaSuccess ||
+              kqed::launch_fill_pairs(nullptr, nx, 0, zx, s) != cudaSuccess;
+    /* the per-site and per-x terms of QED_kernel_L1..L3, src/LIBFILES/kernels.c:117-177 */
+    switch (variant) {
+    case 1:
+      bad = bad || l0(T, M, cfg, d_y, d_y, ny, Ky, s) || l0(T, M, cfg, d_x, d_x, nx, Bx, s) ||
+            kqed::launch_scale(Ky, -0.5, ny * 384, s) != cudaSuccess ||
+            kqed::launch_scale(Bx, -0.5, nx * 384, s) != cudaSuccess;
+      break;
+    case 2:
+      bad = bad || l0(T, M, cfg, zy, d_y, ny, Ky, s) || l0(T, M, cfg, d_x, zx, nx, Bx, s) ||
+            kqed::launch_scale(Ky, -1.0, ny * 384, s) != cudaSuccess ||
+            kqed::launch_scale(Bx, -1.0, nx * 384, s) != cudaSuccess;
+      break;
+    default:
+      bad = bad || l0(T, M, cfg, zy, d_y, ny, Ky, s) || l0(T, M, cfg, d_x, d_x, nx, Bx, s) ||
+            l0(T, M, cfg, zx, d_x, nx, bt, s) ||
+            kqed::launch_scale(Ky, -1.0, ny * 384, s) != cudaSuccess ||
+            kqed::launch_scale(Bx, -1.0, nx * 384, s) != cudaSuccess ||
+            kqed::launch_axpy(Bx, bt, 1.0, nx * 384, s) != cudaSuccess;
+      break;
+    }
+    if (bad) return kqed::set_error("kqed_lattice_sum_noalloc: kernel-term launch failed");
+  }
+  kqed::LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, (int)tiles};
+  if (kqed::launch_lattice_fp64(T, M, a, cfg, s) != cudaSuccess ||
+      kqed::launch_reduce_partials(partial, nx, (int)tiles, d_sums, s) != cudaSuccess)
+    return kqed::set_error("kqed_lattice_sum_noalloc: lattice kernel launch failed");
+  return 0;
+}
