@@ -271,6 +271,154 @@ __device__ __noinline__ void interp_generic(const DevTables &T, const double *__
     W[37] = 2.0 * Edo1.b; W[38] = fHd;
   }
 }
+/* Column layout of the per-x tables built by build_columns_kernel: for a
+   fixed x the x-interpolation of extractff (getff-new.c:241-256) has the
+   same weights and the same two grid columns for every y, so it is applied
+   once per (x, iy, K).  Row (iy, K), 28 doubles:
+     A 0-3, B 4-7, C 8-11, D 12-15 : Hermite-x value, Hermite-x y-deriv,
+                                     lerp-x value, lerp-x y-deriv (of the x-derivative table)
+     E 16-17, H 26-27              : Hermite-x value, y-deriv
+     F 18-21, G 22-25              : as A-D
+   families A (QG0,dxQG0) B (QL2,dxQL2) C (QL4,dxQL4) D (QG1,dxQG1)
+            E (QG2,dxQG2) F (dxQG2,d2xQG2) G (dxQG3,d2xQG3) H (QG3,dxQG3) */
+__device__ __noinline__ void interp_column(const double *__restrict__ r0,
+                                           const double *__restrict__ r1, int Ktop, const Wts &w,
+                                           double twox, double *W)
+{
+  {
+    Rc A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
+    Rc B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
+    Rc C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
+    Rc D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
+    double fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
+#pragma unroll 1
+    for (int K = Ktop - 1; K >= 0; --K) {
+      const int o = K * kRow;
+      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
+      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
+      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
+#pragma unroll
+      for (int f = 0; f < 4; f++) {
+        const double2 a3 = ld2(r0 + o + 4 * f), b3 = ld2(r1 + o + 4 * f);
+        const double2 a1 = ld2(r0 + o + 4 * f + 2), b1 = ld2(r1 + o + 4 * f + 2);
+        const double c3 = HY(a3, b3), c2 = LY(a3, b3), c1 = HY(a1, b1);
+        if (f == 0) {
+          if (K >= 1) { st0(A3o0, twox, c3); st0(A2o0, twox, c2); st0(A1o0, twox, c1); stn(A3o1, A1, mB1, c3); }
+          else { fA3 = fin0(A3o0, twox, c3); fA2 = fin0(A2o0, twox, c2); fA1 = fin0(A1o0, twox, c1); }
+        } else if (f == 1) {
+          if (K >= 2) { stn(B3o2, A2, mB2, c3); stn(B2o2, A2, mB2, c2); stn(B1o2, A2, mB2, c1); }
+          if (K >= 3) stn(B3o3, A3, mB3, c3);
+        } else if (f == 2) {
+          if (K >= 1) { stn(C3o1, A1, mB1, c3); stn(C2o1, A1, mB1, c2); stn(C1o1, A1, mB1, c1); }
+          if (K >= 2) stn(C3o2, A2, mB2, c3);
+        } else {
+          if (K >= 1) { st0(D3o0, twox, c3); st0(D2o0, twox, c2); st0(D1o0, twox, c1); stn(D3o1, A1, mB1, c3); }
+          else { fD3 = fin0(D3o0, twox, c3); fD2 = fin0(D2o0, twox, c2); fD1 = fin0(D1o0, twox, c1); }
+        }
+      }
+    }
+    W[0] = 2.0 * A3o1.b; W[1] = fA1; W[2] = fA2; W[3] = fA3;
+    W[4] = 48.0 * B3o3.b; W[5] = 8.0 * B1o2.b; W[6] = 8.0 * B2o2.b; W[7] = 8.0 * B3o2.b;
+    W[8] = 8.0 * C3o2.b; W[9] = 2.0 * C1o1.b; W[10] = 2.0 * C2o1.b; W[11] = 2.0 * C3o1.b;
+    W[12] = 2.0 * D3o1.b; W[13] = fD1; W[14] = fD2; W[15] = fD3;
+  }
+  {
+    Rc E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
+    Rc F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
+    Rc G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
+    Rc H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
+    double fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
+#pragma unroll 1
+    for (int K = Ktop - 1; K >= 0; --K) {
+      const int o = K * kRow;
+      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
+      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
+      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
+      const double2 ea = ld2(r0 + o + 16), eb = ld2(r1 + o + 16);
+      const double2 fa = ld2(r0 + o + 18), fb = ld2(r1 + o + 18);
+      const double2 fa1 = ld2(r0 + o + 20), fb1 = ld2(r1 + o + 20);
+      const double2 ga = ld2(r0 + o + 22), gb = ld2(r1 + o + 22);
+      const double2 ga1 = ld2(r0 + o + 24), gb1 = ld2(r1 + o + 24);
+      const double2 ha = ld2(r0 + o + 26), hb = ld2(r1 + o + 26);
+      const double e3 = HY(ea, eb), e2 = LY(ea, eb), ed = w.dd * (eb.y - ea.y);
+      const double f3 = HY(fa, fb), f2 = LY(fa, fb), f1 = HY(fa1, fb1);
+      const double g3 = HY(ga, gb), g2 = LY(ga, gb), g1 = HY(ga1, gb1);
+      const double h3 = HY(ha, hb), h2 = LY(ha, hb), hd = w.dd * (hb.y - ha.y);
+      if (K >= 1) {
+        stn(E3o1, A1, mB1, e3); stn(E2o1, A1, mB1, e2); stn(Edo1, A1, mB1, ed);
+        stn(F3o1, A1, mB1, f3); stn(F2o1, A1, mB1, f2); stn(F1o1, A1, mB1, f1);
+        st0(G3o0, twox, g3); st0(G2o0, twox, g2); st0(G1o0, twox, g1); stn(G3o1, A1, mB1, g3);
+        stn(H3o1, A1, mB1, h3); st0(H2o0, twox, h2); stn(H2o1, A1, mB1, h2); st0(Hdo0, twox, hd);
+      } else {
+        fG3 = fin0(G3o0, twox, g3); fG2 = fin0(G2o0, twox, g2); fG1 = fin0(G1o0, twox, g1);
+        fH2 = fin0(H2o0, twox, h2); fHd = fin0(Hdo0, twox, hd);
+      }
+      if (K >= 2) {
+        stn(E3o2, A2, mB2, e3); stn(E2o2, A2, mB2, e2); stn(F3o2, A2, mB2, f3); stn(H3o2, A2, mB2, h3);
+      }
+      if (K >= 3) stn(E3o3, A3, mB3, e3);
+    }
+    W[16] = 8.0 * E3o2.b; W[17] = 2.0 * F3o1.b; W[18] = 2.0 * E2o1.b; W[19] = 2.0 * E3o1.b;
+    W[20] = 8.0 * F3o2.b; W[21] = 2.0 * F1o1.b; W[22] = 2.0 * F2o1.b; W[23] = 2.0 * F3o1.b;
+    W[24] = 2.0 * G3o1.b; W[25] = fG1; W[26] = fG2; W[27] = fG3;
+    W[28] = 48.0 * E3o3.b; W[29] = 8.0 * F3o2.b; W[30] = 8.0 * E2o2.b; W[31] = 8.0 * E3o2.b;
+    W[32] = 8.0 * H3o2.b; W[33] = 2.0 * G3o1.b; W[34] = 2.0 * H2o1.b; W[35] = 2.0 * H3o1.b;
+    W[36] = fH2;
+    W[37] = 2.0 * Edo1.b; W[38] = fHd;
+  }
+}
+
+/* Per-x column tables: thread per (x, iy, K) */
+__global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs, size_t nx,
+                                     double *__restrict__ col)
+{
+  const size_t per_x = (size_t)T.nstpy * T.NK;
+  const size_t tot = nx * per_x;
+  for (size_t u = (size_t)blockIdx.x * blockDim.x + threadIdx.x; u < tot;
+       u += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = u / per_x;
+    const int rem = (int)(u % per_x);
+    const int iy = rem / T.NK, K = rem % T.NK;
+    double *out = col + u * kRow;
+    const double *xv = xs + 4 * k;
+    double xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
+    xsq = xsq < 1E-7 ? 1E-7 : xsq;
+    const double X = sqrt(fabs(xsq));
+    const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
+    if (!(X >= xlo && X <= xhi)) {
+#pragma unroll
+      for (int j = 0; j < kRow; j++) out[j] = 0.0;
+      continue;
+    }
+    const int flag_hx = (X >= xhi);
+    const int ix0 = bsrch(T.XX, X, 0, T.nstpx);
+    const int ix1 = flag_hx ? ix0 : ix0 + 1;
+    Wts w;
+    if (flag_hx) {
+      w.xA = 1.0; w.xB = 0.0; w.xC1 = 0.0; w.xC2 = 0.0; w.lAx = 1.0;
+    } else {
+      const Herm h = herm(X, __ldg(T.XX + ix0), __ldg(T.XX + ix1));
+      w.xA = h.A * h.D; w.xB = h.B * h.D; w.xC1 = h.C1 * h.D; w.xC2 = h.C2 * h.D; w.lAx = h.lA;
+    }
+    const double *n0 = T.node + (((size_t)ix0 * T.nstpy + iy) * T.NK + K) * kRow;
+    const double *n1 = T.node + (((size_t)ix1 * T.nstpy + iy) * T.NK + K) * kRow;
+    /* (value slot, partner slot, lerp slot or -1) of families A..H */
+    const int fam[8][3] = {{0, 1, 1}, {2, 3, 3}, {4, 5, 5}, {6, 7, 7},
+                           {8, 9, -1}, {9, 10, 10}, {12, 13, 13}, {11, 12, -1}};
+    const int dst[8] = {0, 4, 8, 12, 16, 18, 22, 26};
+#pragma unroll
+    for (int f = 0; f < 8; f++) {
+      const int sn = 2 * fam[f][0], sp = 2 * fam[f][1];
+      for (int c = 0; c < 2; c++)
+        out[dst[f] + c] = HX(__ldg(n0 + sn + c), __ldg(n1 + sn + c), __ldg(n0 + sp + c), __ldg(n1 + sp + c));
+      if (fam[f][2] >= 0) {
+        const int se = 2 * fam[f][2];
+        for (int c = 0; c < 2; c++) out[dst[f] + 2 + c] = LX(__ldg(n0 + se + c), __ldg(n1 + se + c));
+      }
+    }
+  }
+}
+
 #undef HY
 #undef LY
 #undef HX
@@ -370,15 +518,51 @@ struct VS {
   double ddg1dydy, ddg2dydy;
 };
 
-/* chain rule x <-> (x-y), chnr_dS.c:74-83 / chnr_dT.c:240-275 */
-__device__ __forceinline__ void swap3(const Inv &I, double &dx, double &dcb, double &dy)
+/* Constants of the x <-> (x-y) chain rule (chnr_dS.c:74-83, chnr_dT.c:240-275,
+   chnr_dV.c:194-274), computed once per pair with reciprocals so the many
+   divisions by |x-y| and |x-y|^2 of the reference become multiplications. */
+struct SwapK {
+  double ca, cd, or_, pc, q1, q2;   /* first derivatives */
+  double r, r2, k1, k2, k3, k4, k5, k6, k7, k8, k9, k10, qa, qb;   /* second derivatives */
+};
+
+__device__ __forceinline__ SwapK swap_consts(const Inv &I)
 {
-  const double ca = I.cb;
-  const double cd = (I.yorig - I.x * I.cborig) / I.xmy;
+  SwapK k;
+  const double x = I.x, y = I.yorig, xmy = I.xmy, xmysq = I.xmysq, ysq = I.ysq;
+  const double ca = I.cb, cb = I.cborig;
+  k.r = 1.0 / xmy;
+  k.r2 = 1.0 / xmysq;
+  const double r = k.r, r2 = k.r2, r3 = r2 * r, r4 = r2 * r2;
+  k.ca = ca;
+  k.cd = (y - x * cb) * r;
+  const double cd = k.cd, omc = 1.0 - ca * ca;
+  k.or_ = omc * r;
+  k.pc = -(cb + ca * cd) * r;
+  k.q1 = ysq * cd * r2;
+  k.q2 = x * y * xmy * r2;
+  k.k1 = -3.0 * ca * omc * r2;
+  k.k2 = ysq * r3 * (cb + 3.0 * ca * cd);
+  k.k3 = ysq * r2 * cd;
+  k.k4 = y * r2 * (x * ca - xmy);
+  k.k5 = x * y * r;
+  k.k6 = (2.0 * ca * cb + cd * (3.0 * ca * ca - 1.0)) * r2;
+  k.k7 = y * r3 * ((3.0 * cd * cd - 1.0) * y - 2.0 * xmy * cd);
+  k.k8 = x * r2 * (y * cd - xmy);
+  k.k9 = x * ysq * r4 * (xmy - 3.0 * y * cd);
+  k.k10 = I.xsq * ysq * r3;
+  k.qa = ysq * cd * r2;
+  k.qb = x * y * xmy * r2;
+  return k;
+}
+
+/* derivatives of g(x, ca, |x-y|) -> derivatives of g(x, cb, |y|) */
+__device__ __forceinline__ void swap3(const SwapK &k, double &dx, double &dcb, double &dy)
+{
   const double ox = dx, ocb = dcb, oy = dy;
-  dx = ox + (1.0 - ca * ca) / I.xmy * ocb + ca * oy;
-  dcb = -(I.ysq * cd * ocb + I.x * I.yorig * I.xmy * oy) / I.xmysq;
-  dy = -(I.cborig + ca * cd) / I.xmy * ocb + cd * oy;
+  dx = ox + k.or_ * ocb + k.ca * oy;
+  dcb = -(k.q1 * ocb + k.q2 * oy);
+  dy = k.pc * ocb + k.cd * oy;
 }
 
 /* generic T scalars from the weights, chnr_dT.c:297-347 */
@@ -386,38 +570,38 @@ __device__ void T_generic(const Inv &I, const double *W, TS &T)
 {
   const double X = I.x, Y = I.y, cb = I.cb, xsq = I.xsq;
   const double ysq = I.flag2 ? I.xmysq : I.ysq;
+  const double rX = 1.0 / X, rY = 1.0 / Y, rxsq = rX * rX, rysq = 1.0 / ysq;
+  const double c43 = (4.0 / 3.0) * rxsq * rxsq;
   T.d2x = W[5]; T.d2y = W[6]; T.ell2 = W[7]; T.d2cb = W[4];
   const double ell4 = W[11], d4x = W[9], d4y = W[10], d4cb = W[8];
   const double v1 = W[15], dv1dx = W[13], dv1dy = W[14], dv1dcb = W[12];
   const double ccq = cb * cb - 0.25;
-  T.ell3 = ell4 / (2.0 * xsq * ysq) - Y * cb * T.ell2 / X;
-  T.ell1 = 4.0 / (3.0 * xsq * xsq) * (v1 - xsq * ysq * ccq * T.ell2 - 1.5 * xsq * X * Y * cb * T.ell3);
-  T.d3y = (-ell4 / (ysq * Y) + d4y / (2.0 * ysq) - cb * X * T.ell2 - Y * X * cb * T.d2y) / (xsq);
-  T.d3cb = (d4cb / (2.0 * X * ysq) - Y * T.ell2 - Y * cb * T.d2cb) / X;
-  T.d3x = (-ell4 / (X * ysq) + d4x / (2.0 * ysq) + Y * cb * T.ell2 - Y * X * cb * T.d2x) / xsq;
-  T.d1y = 4.0 / (3.0 * xsq * xsq) *
-          (dv1dy - 2.0 * xsq * Y * ccq * T.ell2 - xsq * ysq * ccq * T.d2y -
-           1.5 * xsq * X * cb * T.ell3 - 1.5 * xsq * X * Y * cb * T.d3y);
-  T.d1cb = 4.0 / (3.0 * xsq * xsq) *
-           (dv1dcb - 2.0 * xsq * ysq * cb * T.ell2 - xsq * ysq * ccq * T.d2cb -
-            1.5 * xsq * X * Y * T.ell3 - 1.5 * xsq * X * Y * cb * T.d3cb);
-  T.d1x = -4.0 * T.ell1 / X +
-          4.0 / (3.0 * xsq * xsq) *
-              (dv1dx - 2.0 * X * ysq * ccq * T.ell2 - xsq * ysq * ccq * T.d2x -
-               4.5 * xsq * Y * cb * T.ell3 - 1.5 * xsq * X * Y * cb * T.d3x);
+  const double xy = X * Y, xsqysq = xsq * ysq;
+  T.ell3 = 0.5 * ell4 * rxsq * rysq - Y * cb * T.ell2 * rX;
+  T.ell1 = c43 * (v1 - xsqysq * ccq * T.ell2 - 1.5 * xsq * xy * cb * T.ell3);
+  T.d3y = (-ell4 * rysq * rY + 0.5 * d4y * rysq - cb * X * T.ell2 - xy * cb * T.d2y) * rxsq;
+  T.d3cb = (0.5 * d4cb * rX * rysq - Y * T.ell2 - Y * cb * T.d2cb) * rX;
+  T.d3x = (-ell4 * rX * rysq + 0.5 * d4x * rysq + Y * cb * T.ell2 - xy * cb * T.d2x) * rxsq;
+  T.d1y = c43 * (dv1dy - 2.0 * xsq * Y * ccq * T.ell2 - xsqysq * ccq * T.d2y -
+                 1.5 * xsq * X * cb * T.ell3 - 1.5 * xsq * xy * cb * T.d3y);
+  T.d1cb = c43 * (dv1dcb - 2.0 * xsqysq * cb * T.ell2 - xsqysq * ccq * T.d2cb -
+                  1.5 * xsq * xy * T.ell3 - 1.5 * xsq * xy * cb * T.d3cb);
+  T.d1x = -4.0 * T.ell1 * rX +
+          c43 * (dv1dx - 2.0 * X * ysq * ccq * T.ell2 - xsqysq * ccq * T.d2x -
+                 4.5 * xsq * Y * cb * T.ell3 - 1.5 * xsq * xy * cb * T.d3x);
 }
 
 /* XMYSWAP_T_contrib, chnr_dT.c:240-275 */
-__device__ void T_swap(const Inv &I, TS &T)
+__device__ void T_swap(const SwapK &k, TS &T)
 {
-  swap3(I, T.d2x, T.d2cb, T.d2y);
+  swap3(k, T.d2x, T.d2cb, T.d2y);
   double e3x = -T.d3x, e3cb = -T.d3cb, e3y = -T.d3y;
   T.ell3 = -T.ell3 - T.ell2;
-  swap3(I, e3x, e3cb, e3y);
+  swap3(k, e3x, e3cb, e3y);
   T.d3x = e3x - T.d2x; T.d3cb = e3cb - T.d2cb; T.d3y = e3y - T.d2y;
   double e1x = T.d1x, e1cb = T.d1cb, e1y = T.d1y;
   T.ell1 = T.ell1 - T.ell2 - 2.0 * T.ell3;
-  swap3(I, e1x, e1cb, e1y);
+  swap3(k, e1x, e1cb, e1y);
   T.d1x = e1x - T.d2x - 2.0 * T.d3x;
   T.d1cb = e1cb - T.d2cb - 2.0 * T.d3cb;
   T.d1y = e1y - T.d2y - 2.0 * T.d3y;
@@ -426,92 +610,72 @@ __device__ void T_swap(const Inv &I, TS &T)
 /* generic V scalars from the weights, chnr_dV.c:380-466 */
 __device__ void V_generic(const Inv &I, const double *W, double ystp, VS &D)
 {
-  const double X = I.x, Y = I.y, cb = I.cb, xsq = I.xsq;
+  const double X = I.x, Y = I.y, cb = I.cb;
+  const double rX = 1.0 / X, rxsq = rX * rX;
+  const double yx = Y * rX, yxx = Y * rxsq, cbx = cb * rX;
   D.dg3dy = W[36];
   D.g2 = W[19]; D.dg2dy = W[18];
   D.ddg2dxdx = W[21]; D.dg2dx = W[23]; D.ddg2dxdy = W[22]; D.ddg2dxdcb = W[20];
   D.ddg3dxdx = W[25]; D.dg3dx = W[27]; D.ddg3dxdy = W[26]; D.ddg3dxdcb = W[24];
   D.dg2dcb = W[31]; D.ddg2dydcb = W[30]; D.ddg2dcbdcb = W[28];
   D.dg3dcb = W[35]; D.ddg3dydcb = W[34]; D.ddg3dcbdcb = W[32];
-  D.dg1dx = D.dg3dx + Y / xsq * cb * D.g2 - Y / X * cb * D.dg2dx;
-  D.dg1dy = D.dg3dy - cb / X * D.g2 - (Y / X) * cb * D.dg2dy;
-  D.dg1dcb = D.dg3dcb - Y / X * D.g2 - Y / X * cb * D.dg2dcb;
-  D.ddg1dxdx = D.ddg3dxdx - 2.0 * Y / (xsq * X) * cb * D.g2 + Y / xsq * cb * D.dg2dx +
-               Y / xsq * cb * D.dg2dx - Y / X * cb * D.ddg2dxdx;
-  D.ddg1dxdy = D.ddg3dxdy + cb / xsq * D.g2 + Y * cb / xsq * D.dg2dy - cb / X * D.dg2dx -
-               Y / X * cb * D.ddg2dxdy;
-  D.ddg1dxdcb = D.ddg3dxdcb + Y / xsq * D.g2 + Y / xsq * cb * D.dg2dcb - Y / X * D.dg2dx -
-                Y / X * cb * D.ddg2dxdcb;
-  D.ddg1dydcb = D.ddg3dydcb - D.g2 / X - cb / X * D.dg2dcb - Y / X * D.dg2dy -
-                Y / X * cb * D.ddg2dydcb;
-  D.ddg1dcbdcb = D.ddg3dcbdcb - 2.0 * Y / X * D.dg2dcb - Y / X * cb * D.ddg2dcbdcb;
+  D.dg1dx = D.dg3dx + yxx * cb * D.g2 - yx * cb * D.dg2dx;
+  D.dg1dy = D.dg3dy - cbx * D.g2 - yx * cb * D.dg2dy;
+  D.dg1dcb = D.dg3dcb - yx * D.g2 - yx * cb * D.dg2dcb;
+  D.ddg1dxdx = D.ddg3dxdx - 2.0 * yxx * rX * cb * D.g2 + 2.0 * yxx * cb * D.dg2dx - yx * cb * D.ddg2dxdx;
+  D.ddg1dxdy = D.ddg3dxdy + cb * rxsq * D.g2 + yxx * cb * D.dg2dy - cbx * D.dg2dx - yx * cb * D.ddg2dxdy;
+  D.ddg1dxdcb = D.ddg3dxdcb + yxx * D.g2 + yxx * cb * D.dg2dcb - yx * D.dg2dx - yx * cb * D.ddg2dxdcb;
+  D.ddg1dydcb = D.ddg3dydcb - D.g2 * rX - cbx * D.dg2dcb - yx * D.dg2dy - yx * cb * D.ddg2dydcb;
+  D.ddg1dcbdcb = D.ddg3dcbdcb - 2.0 * yx * D.dg2dcb - yx * cb * D.ddg2dcbdcb;
   D.ddg2dydy = 0.0; D.ddg1dydy = 0.0;
   if (I.flag2) {
-    D.ddg2dydy = W[37] / ystp;
-    const double ddg3dydy = W[38] / ystp;
-    D.ddg1dydy = ddg3dydy - (Y * D.ddg2dydy + 2.0 * D.dg2dy) * cb / X;
+    const double rs = 1.0 / ystp;
+    D.ddg2dydy = W[37] * rs;
+    const double ddg3dydy = W[38] * rs;
+    D.ddg1dydy = ddg3dydy - (Y * D.ddg2dydy + 2.0 * D.dg2dy) * cbx;
   }
 }
 
-/* XMYSWAP_V_contrib with v_flip2, chnr_dV.c:176-274 */
-__device__ void V_swap(VS *Dp, double x, double xmy, double y, double xsq, double xmysq,
-                       double ysq, double ca, double cborig)
+/* XMYSWAP_V_contrib with v_flip2, chnr_dV.c:176-274, with the per-pair
+   constants of SwapK */
+__device__ void V_swap(VS *Dp, const SwapK &k)
 {
   VS &D = *Dp;
   VS F = D;
   F.g2 = -D.g2; F.dg2dx = -D.dg2dx; F.dg2dy = -D.dg2dy; F.dg2dcb = -D.dg2dcb;
   F.ddg2dxdx = -D.ddg2dxdx; F.ddg2dxdy = -D.ddg2dxdy; F.ddg2dydy = -D.ddg2dydy;
   F.ddg2dxdcb = -D.ddg2dxdcb; F.ddg2dydcb = -D.ddg2dydcb; F.ddg2dcbdcb = -D.ddg2dcbdcb;
-  const double cd = (y - x * cborig) / xmy;
-  const double omc = 1.0 - ca * ca;
+  const double ca = k.ca, cd = k.cd, oR = k.or_, pc = k.pc;
   D.g2 = F.g2;
-  D.dg2dx = F.dg2dx + omc / xmy * F.dg2dcb + ca * F.dg2dy;
-  D.dg2dcb = -(ysq * cd * F.dg2dcb + x * y * xmy * F.dg2dy) / xmysq;
-  D.dg2dy = -(cborig + ca * cd) / xmy * F.dg2dcb + cd * F.dg2dy;
-  D.dg1dx = F.dg1dx + omc / xmy * F.dg1dcb + ca * F.dg1dy - D.dg2dx;
-  D.dg1dcb = -(ysq * cd * F.dg1dcb + x * y * xmy * F.dg1dy) / xmysq - D.dg2dcb;
-  D.dg1dy = -(cborig + ca * cd) / xmy * F.dg1dcb + cd * F.dg1dy - D.dg2dy;
-#define DXDX(g)                                                                                  \
-  ((F.ddg##g##dxdx + omc / xmy * F.ddg##g##dxdcb + ca * F.ddg##g##dxdy) -                        \
-   3.0 * ca * omc / xmysq * F.dg##g##dcb +                                                       \
-   omc / xmy * (F.ddg##g##dxdcb + omc / xmy * F.ddg##g##dcbdcb + ca * F.ddg##g##dydcb) +         \
-   omc / xmy * F.dg##g##dy + ca * (F.ddg##g##dxdy + omc / xmy * F.ddg##g##dydcb + ca * F.ddg##g##dydy))
-#define DXDCB(g)                                                                                 \
-  (ysq / (xmysq * xmy) * (cborig + 3.0 * ca * cd) * F.dg##g##dcb -                                \
-   ysq / xmysq * cd * (F.ddg##g##dxdcb + omc / xmy * F.ddg##g##dcbdcb + ca * F.ddg##g##dydcb) +   \
-   y / xmysq * (x * ca - xmy) * F.dg##g##dy -                                                    \
-   x * y / xmy * (F.ddg##g##dxdy + omc / xmy * F.ddg##g##dydcb + ca * F.ddg##g##dydy))
-#define DXDY(g)                                                                                  \
-  ((-(cborig + ca * cd) / xmy * F.ddg##g##dxdcb + cd * F.ddg##g##dxdy) +                          \
-   (2.0 * ca * cborig + cd * (3.0 * ca * ca - 1.0)) / xmysq * F.dg##g##dcb +                      \
-   omc / xmy * (-(cborig + ca * cd) / xmy * F.ddg##g##dcbdcb + cd * F.ddg##g##dydcb) -            \
-   (cborig + ca * cd) / xmy * F.dg##g##dy +                                                      \
-   ca * (-(cborig + ca * cd) / xmy * F.ddg##g##dydcb + cd * F.ddg##g##dydy))
-#define DYDCB(g)                                                                                 \
-  (y / (xmysq * xmy) * ((3.0 * cd * cd - 1.0) * y - 2 * xmy * cd) * F.dg##g##dcb -                \
-   ysq / (xmysq)*cd * (-(cborig + ca * cd) / xmy * F.ddg##g##dcbdcb + cd * F.ddg##g##dydcb) +     \
-   x / xmysq * (y * cd - xmy) * F.dg##g##dy -                                                    \
-   x * y / xmy * (-(cborig + ca * cd) / xmy * F.ddg##g##dydcb + cd * F.ddg##g##dydy))
-#define DCBDCB(g)                                                                                \
-  (x * ysq / (xmysq * xmysq) * (xmy - 3.0 * y * cd) * F.dg##g##dcb -                              \
-   ysq / (xmysq)*cd * (-(ysq * cd * F.ddg##g##dcbdcb + x * y * xmy * F.ddg##g##dydcb) / xmysq) -  \
-   xsq * ysq / (xmysq * xmy) * F.dg##g##dy -                                                     \
-   x * y / xmy * (-(ysq * cd * F.ddg##g##dydcb + x * y * xmy * F.ddg##g##dydy) / xmysq))
-  D.ddg2dxdx = DXDX(2);
-  D.ddg2dxdcb = DXDCB(2);
-  D.ddg2dxdy = DXDY(2);
-  D.ddg2dydcb = DYDCB(2);
-  D.ddg2dcbdcb = DCBDCB(2);
-  D.ddg1dxdx = DXDX(1) - D.ddg2dxdx;
-  D.ddg1dxdcb = DXDCB(1) - D.ddg2dxdcb;
-  D.ddg1dxdy = DXDY(1) - D.ddg2dxdy;
-  D.ddg1dydcb = DYDCB(1) - D.ddg2dydcb;
-  D.ddg1dcbdcb = DCBDCB(1) - D.ddg2dcbdcb;
-#undef DXDX
-#undef DXDCB
-#undef DXDY
-#undef DYDCB
-#undef DCBDCB
+  D.dg2dx = F.dg2dx + oR * F.dg2dcb + ca * F.dg2dy;
+  D.dg2dcb = -(k.q1 * F.dg2dcb + k.q2 * F.dg2dy);
+  D.dg2dy = pc * F.dg2dcb + cd * F.dg2dy;
+  D.dg1dx = F.dg1dx + oR * F.dg1dcb + ca * F.dg1dy - D.dg2dx;
+  D.dg1dcb = -(k.q1 * F.dg1dcb + k.q2 * F.dg1dy) - D.dg2dcb;
+  D.dg1dy = pc * F.dg1dcb + cd * F.dg1dy - D.dg2dy;
+#define SECOND(g, DXDX, DXDCB, DXDY, DYDCB, DCBDCB)                                           \
+  {                                                                                           \
+    const double a = F.ddg##g##dxdx, b = F.ddg##g##dxdcb, c = F.ddg##g##dxdy;                 \
+    const double e = F.ddg##g##dcbdcb, f = F.ddg##g##dydcb, h = F.ddg##g##dydy;               \
+    const double gcb = F.dg##g##dcb, gy = F.dg##g##dy;                                        \
+    const double Bq = b + oR * e + ca * f, Cq = c + oR * f + ca * h;                          \
+    const double Pe = pc * e + cd * f, Pf = pc * f + cd * h;                                  \
+    const double Qe = k.qa * e + k.qb * f, Qf = k.qa * f + k.qb * h;                          \
+    DXDX = (a + oR * b + ca * c) + k.k1 * gcb + oR * Bq + oR * gy + ca * Cq;                  \
+    DXDCB = k.k2 * gcb - k.k3 * Bq + k.k4 * gy - k.k5 * Cq;                                   \
+    DXDY = (pc * b + cd * c) + k.k6 * gcb + oR * Pe + pc * gy + ca * Pf;                      \
+    DYDCB = k.k7 * gcb - k.k3 * Pe + k.k8 * gy - k.k5 * Pf;                                   \
+    DCBDCB = k.k9 * gcb + k.k3 * Qe - k.k10 * gy + k.k5 * Qf;                                 \
+  }
+  SECOND(2, D.ddg2dxdx, D.ddg2dxdcb, D.ddg2dxdy, D.ddg2dydcb, D.ddg2dcbdcb)
+  double t1, t2, t3, t4, t5;
+  SECOND(1, t1, t2, t3, t4, t5)
+#undef SECOND
+  D.ddg1dxdx = t1 - D.ddg2dxdx;
+  D.ddg1dxdcb = t2 - D.ddg2dxdcb;
+  D.ddg1dxdy = t3 - D.ddg2dxdy;
+  D.ddg1dydcb = t4 - D.ddg2dydcb;
+  D.ddg1dcbdcb = t5 - D.ddg2dcbdcb;
 }
 
 /* ---------------------------------------------------- Taylor-x branches */
@@ -690,17 +854,18 @@ __device__ void fill_generic_record(double *R, const double *xv, const double *y
                                     const VS &D)
 {
   const double x = I.x, y = I.yorig, cb = I.cborig;
+  const double rX = 1.0 / x, rY = 1.0 / y;
   for (int m = 0; m < 4; m++) {
     R[R_XV + m] = xv[m];
     R[R_YV + m] = yv[m];
-    const double xh = xv[m] / x, yh = yv[m] / y;
+    const double xh = xv[m] * rX, yh = yv[m] * rY;
     R[R_XH + m] = xh;
     R[R_YH + m] = yh;
-    R[R_C2 + m] = (xh - cb * yh) / y;
-    R[R_C4 + m] = (yh - cb * xh) / x;
+    R[R_C2 + m] = (xh - cb * yh) * rY;
+    R[R_C4 + m] = (yh - cb * xh) * rX;
   }
   R[R_X] = x; R[R_YO] = y; R[R_CB] = cb; R[R_XSQ] = I.xsq; R[R_YSQ] = I.ysq; R[R_XDY] = I.xdoty;
-  R[R_RX] = 1.0 / x; R[R_RY] = 1.0 / y;
+  R[R_RX] = rX; R[R_RY] = rY;
   R[R_S + 0] = dg0dx; R[R_S + 1] = dg0dy; R[R_S + 2] = dg0dcb;
   R[R_T + 0] = T.ell1; R[R_T + 1] = T.ell2; R[R_T + 2] = T.ell3;
   R[R_T + 3] = T.d1x; R[R_T + 4] = T.d1y; R[R_T + 5] = T.d1cb;
@@ -713,13 +878,13 @@ __device__ void fill_generic_record(double *R, const double *xv, const double *y
     R[R_VD + 12 + m] = xv[m] * D.ddg1dydcb + yv[m] * D.ddg2dydcb;
     R[R_VD + 16 + m] = xv[m] * D.ddg1dxdcb + yv[m] * D.ddg2dxdcb;
     R[R_VD + 20 + m] = xv[m] * D.ddg1dcbdcb + yv[m] * D.ddg2dcbdcb;
-    R[R_VD + 24 + m] = (xv[m] * D.dg1dx + yv[m] * D.dg2dx) / x;
-    R[R_VD + 28 + m] = (xv[m] * D.dg1dcb + yv[m] * D.dg2dcb) / x;
+    R[R_VD + 24 + m] = (xv[m] * D.dg1dx + yv[m] * D.dg2dx) * rX;
+    R[R_VD + 28 + m] = (xv[m] * D.dg1dcb + yv[m] * D.dg2dcb) * rX;
   }
   for (int m = 0; m < 4; m++) {
     const double xh = R[R_XH + m], yh = R[R_YH + m];
     R[R_VA + m] = (D.dg1dx + D.dg2dx) * xh + (D.dg1dcb + D.dg2dcb) * R[R_C4 + m];
-    R[R_VB + m] = (D.dg1dx * xh + D.dg1dy * yh + D.dg1dcb * (xh / y + yh / x - cb * (xh / x + yh / y)));
+    R[R_VB + m] = (D.dg1dx * xh + D.dg1dy * yh + D.dg1dcb * (xh * rY + yh * rX - cb * (xh * rX + yh * rY)));
   }
 }
 
@@ -830,7 +995,7 @@ __device__ __forceinline__ bool is_zero4(const double *v)
 /* Phase A for one pair: classify (QED_kernel_L0, kernels.c:81-115), fill the
    record, return the kind and status bits. */
 __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, double *R,
-                       int &status)
+                       int &status, const double *colx = nullptr)
 {
   status = 0;
   /* non-finite input: the reference's grid search would run off the tables;
@@ -897,21 +1062,27 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, d
        last one (its extractff then sees flag_hy and repeats the lower node) */
     w.dd = (I.flag2 && !flag_hy && iy0 + 1 < T.nstpy - 1) ? 1.0 : 0.0;
     const int NK = T.NK;
-    const double *b00 = T.node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow;
-    const double *b01 = T.node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow;
-    const double *b10 = T.node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow;
-    const double *b11 = T.node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow;
     const int Ktop = max(__ldg(T.nfx + ix0), __ldg(T.nfx + ix1)) + 2;
     double W[39];
-    interp_generic(T, b00, b01, b10, b11, Ktop, w, 2.0 * I.cb, W);
+    if (colx) {
+      interp_column(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, w,
+                    2.0 * I.cb, W);
+    } else {
+      const double *b00 = T.node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow;
+      const double *b01 = T.node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow;
+      const double *b10 = T.node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow;
+      const double *b11 = T.node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow;
+      interp_generic(T, b00, b01, b10, b11, Ktop, w, 2.0 * I.cb, W);
+    }
     dg0dcb = W[0]; dg0dx = W[1]; dg0dy = W[2];
     T_generic(I, W, Ts);
     V_generic(I, W, T.ystp, D);
   }
   if (I.flag2) {
-    swap3(I, dg0dx, dg0dcb, dg0dy);
-    T_swap(I, Ts);
-    V_swap(&D, I.x, I.xmy, I.yorig, I.xsq, I.xmysq, I.ysq, I.cb, I.cborig);
+    const SwapK k = swap_consts(I);
+    swap3(k, dg0dx, dg0dcb, dg0dy);
+    T_swap(k, Ts);
+    V_swap(&D, k);
   }
   fill_generic_record(R, xv, yv, I, dg0dx, dg0dy, dg0dcb, Ts, D);
   return K_GEN;
@@ -1197,7 +1368,8 @@ __global__ void __launch_bounds__(128) lattice_fp64_kernel(DevTables T, DevMaps 
     if (n < A.ny) {
       double yv[4];
       for (int m = 0; m < 4; m++) yv[m] = A.y[4 * n + m];
-      kind = phase_a(T, xv, yv, L.w.rec + lane * REC, status);
+      const double *colx = A.col ? A.col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
+      kind = phase_a(T, xv, yv, L.w.rec + lane * REC, status, colx);
     }
     L.w.kind[lane] = kind;
     __syncwarp();
@@ -1336,9 +1508,20 @@ cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const Latt
   if (e != cudaSuccess) return e;
   const size_t units = a.nx * (size_t)a.tiles;
   if (units == 0) return cudaSuccess;
-  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : (size_t)num_sms() * 2;
+  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : (size_t)num_sms() * 3;
   if (blocks > units) blocks = units;
   lattice_fp64_kernel<<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_columns(const DevTables &T, const double *xs, size_t nx, double *col,
+                                 cudaStream_t s)
+{
+  const size_t tot = nx * (size_t)T.nstpy * T.NK;
+  if (tot == 0) return cudaSuccess;
+  const size_t b = min((tot + 127) / 128, (size_t)num_sms() * 16);
+  build_columns_kernel<<<(unsigned)b, 128, 0, s>>>(T, xs, nx, col);
   g_launches++;
   return cudaGetLastError();
 }

@@ -150,15 +150,23 @@ struct Ctx {
 /* per-thread staging for the per-pair legacy calls and batched host calls */
 struct ThreadStage {
   Ctx *owner = nullptr;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr, copy_stream = nullptr;
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double *h_pin = nullptr;   /* 8 + 384 doubles */
-  Scratch d_io, d_tmp, d_aux, d_aux2;
+  Scratch d_io, d_tmp, d_aux, d_aux2, d_col;
   ~ThreadStage() { reset(); }
   void reset()
   {
     if (stream) cudaStreamDestroy(stream);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    for (int i = 0; i < 2; i++) {
+      if (ev_copied[i]) cudaEventDestroy(ev_copied[i]);
+      if (ev_free[i]) cudaEventDestroy(ev_free[i]);
+      ev_copied[i] = ev_free[i] = nullptr;
+    }
+    copy_stream = nullptr;
     if (h_pin) cudaFreeHost(h_pin);
-    d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release();
+    d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release(); d_col.release();
     stream = nullptr;
     h_pin = nullptr;
     owner = nullptr;
@@ -708,6 +716,45 @@ static int lattice_terms(Ctx *c, int variant, const double *dx, size_t nx, const
   return 0;
 }
 
+/* state of one fused lattice sum between its preparation, its per-x-chunk
+   launches and the final reduction */
+struct LatticeRun {
+  Ctx *c;
+  const double *d_x, *d_y;
+  size_t nx, ny;
+  double *Ky, *Bx, *partial, *col;
+  int tiles;
+};
+
+static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, size_t ny,
+                           const double *d_y, cudaStream_t s, ThreadStage &st, LatticeRun &R)
+{
+  R.c = c; R.d_x = d_x; R.d_y = d_y; R.nx = nx; R.ny = ny;
+  if (lattice_terms(c, variant, d_x, nx, d_y, ny, &R.Ky, &R.Bx, s, st)) return 1;
+  const int wpb = c->cfg.warps_per_block;
+  R.tiles = (int)((ny + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32));
+  R.partial = st.d_tmp.get(nx * (size_t)std::max(R.tiles, 1) * 2);
+  if (!R.partial) return fail("out of device memory for partial sums");
+  R.col = st.d_col.get(nx * (size_t)c->T.nstpy * c->T.NK * kRow);
+  if (!R.col) return fail("out of device memory for x-column tables");
+  CUDA_OK(launch_build_columns(c->T, d_x, nx, R.col, s));
+  return 0;
+}
+
+/* fused kernel for x points [x0, x0+nxc) with their Pi block at d_pi */
+static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const double *d_pi,
+                          cudaStream_t s)
+{
+  const size_t per_x = (size_t)R.c->T.nstpy * R.c->T.NK * kRow;
+  LatticeArgs a{R.d_x + 4 * x0, R.d_y, nxc, R.ny, d_pi, R.Ky, R.Bx ? R.Bx + 384 * x0 : nullptr,
+                R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1), R.tiles, R.col + per_x * x0};
+  TimedLaunch tl;
+  prof_begin(s, tl);
+  CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, R.c->cfg, s));
+  prof_end(s, tl);
+  return 0;
+}
+
 extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t nx,
                                     const double *d_x, size_t ny, const double *d_y,
                                     const double *d_pi, double *d_sums, int precision, void *stream)
@@ -719,21 +766,16 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
   if (!d_x || !d_y || !d_pi || !d_sums) return fail("null buffer");
   cudaStream_t s = (cudaStream_t)stream;
   ThreadStage &st = stage_for(c);
-  double *Ky, *Bx;
-  if (lattice_terms(c, variant, d_x, nx, d_y, ny, &Ky, &Bx, s, st)) return 1;
-  const int wpb = c->cfg.warps_per_block;
-  const int tiles = (int)((ny + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32));
-  double *partial = st.d_tmp.get(nx * (size_t)std::max(tiles, 1) * 2);
-  if (!partial) return fail("out of device memory for partial sums");
-  LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, tiles};
-  TimedLaunch tl;
-  prof_begin(s, tl);
-  CUDA_OK(launch_lattice_fp64(c->T, c->M, a, c->cfg, s));
-  prof_end(s, tl);
-  CUDA_OK(launch_reduce_partials(partial, nx, tiles, d_sums, s));
+  LatticeRun R;
+  if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R)) return 1;
+  if (lattice_launch(R, 0, nx, d_pi, s)) return 1;
+  CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, d_sums, s));
   return 0;
 }
 
+/* Host buffers.  Pi streams to the device in per-x chunks through a double
+   buffer on a copy stream, so the transfer of chunk i+1 overlaps the fused
+   kernel on chunk i (with pinned host memory the copies run asynchronously). */
 extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, size_t nx,
                                 const double *x, size_t ny, const double *y, const double *pi,
                                 double *sums, int precision)
@@ -745,15 +787,40 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
   if (!x || !y || !pi || !sums) return fail("null buffer");
   ThreadStage &st = stage_for(c);
   if (!st.stream) CUDA_OK(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking));
-  double *io = st.d_io.get(nx * 5 + ny * 4 + nx * ny * 384);
+  if (!st.copy_stream) CUDA_OK(cudaStreamCreateWithFlags(&st.copy_stream, cudaStreamNonBlocking));
+  const size_t per_x = ny * 384;
+  /* chunk of about 128 M doubles (1 GB) of Pi, at least one x */
+  size_t nxc = std::max((size_t)1, ((size_t)128 << 20) / std::max(per_x, (size_t)1));
+  nxc = std::min(nxc, nx);
+  double *io = st.d_io.get(nx * 5 + ny * 4 + 2 * nxc * per_x);
   if (!io) return fail("out of device memory for %zu x %zu pairs", nx, ny);
-  double *dx = io, *dy = io + nx * 4, *ds = dy + ny * 4, *dpi = ds + nx;
-  CUDA_OK(cudaMemcpyAsync(dx, x, nx * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
-  CUDA_OK(cudaMemcpyAsync(dy, y, ny * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
-  CUDA_OK(cudaMemcpyAsync(dpi, pi, nx * ny * 384 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
-  if (kqed_lattice_sum_dev(t, variant, nx, dx, ny, dy, dpi, ds, precision, st.stream)) return 1;
-  CUDA_OK(cudaMemcpyAsync(sums, ds, nx * sizeof(double), cudaMemcpyDeviceToHost, st.stream));
-  CUDA_OK(cudaStreamSynchronize(st.stream));
+  double *dx = io, *dy = io + nx * 4, *ds = dy + ny * 4, *slot[2] = {ds + nx, ds + nx + nxc * per_x};
+  cudaStream_t s = st.stream, cs = st.copy_stream;
+  CUDA_OK(cudaMemcpyAsync(dx, x, nx * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CUDA_OK(cudaMemcpyAsync(dy, y, ny * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
+  LatticeRun R;
+  if (lattice_prepare(c, variant, nx, dx, ny, dy, s, st, R)) return 1;
+  if (!st.ev_copied[0]) {
+    for (int i = 0; i < 2; i++) {
+      CUDA_OK(cudaEventCreateWithFlags(&st.ev_copied[i], cudaEventDisableTiming));
+      CUDA_OK(cudaEventCreateWithFlags(&st.ev_free[i], cudaEventDisableTiming));
+    }
+  }
+  const size_t nchunks = (nx + nxc - 1) / nxc;
+  for (size_t ch = 0; ch < nchunks; ch++) {
+    const int b = (int)(ch & 1);
+    const size_t x0 = ch * nxc, n = std::min(nxc, nx - x0);
+    if (ch >= 2) CUDA_OK(cudaStreamWaitEvent(cs, st.ev_free[b], 0));
+    CUDA_OK(cudaMemcpyAsync(slot[b], pi + x0 * per_x, n * per_x * sizeof(double),
+                            cudaMemcpyHostToDevice, cs));
+    CUDA_OK(cudaEventRecord(st.ev_copied[b], cs));
+    CUDA_OK(cudaStreamWaitEvent(s, st.ev_copied[b], 0));
+    if (lattice_launch(R, x0, n, slot[b], s)) return 1;
+    CUDA_OK(cudaEventRecord(st.ev_free[b], s));
+  }
+  CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, ds, s));
+  CUDA_OK(cudaMemcpyAsync(sums, ds, nx * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CUDA_OK(cudaStreamSynchronize(s));
   return 0;
 }
 

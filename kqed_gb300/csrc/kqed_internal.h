@@ -93,6 +93,7 @@ struct LatticeArgs {
   const double *Bx;     /* [nx][384] per-x additive kernel terms or NULL */
   double *partial;      /* [nx][tiles][2]  (sum, compensation) */
   int tiles;            /* y tiles per x */
+  const double *col;    /* per-x column tables [nx][nstpy][NK][kRow] or NULL */
 };
 
 int upload_map_constants();
@@ -100,6 +101,8 @@ cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a
                            const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                 const LaunchCfg &cfg, cudaStream_t s);
+cudaError_t launch_build_columns(const DevTables &T, const double *xs, size_t nx, double *col,
+                                 cudaStream_t s);
 cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,
                                    cudaStream_t s);
 cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStream_t s);

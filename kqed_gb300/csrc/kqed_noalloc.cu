@@ -141,7 +141,7 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
     }
     if (bad) return kqed::set_error("kqed_lattice_sum_noalloc: kernel-term launch failed");
   }
-  kqed::LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, (int)tiles};
+  kqed::LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, (int)tiles, nullptr};
   if (kqed::launch_lattice_fp64(T, M, a, cfg, s) != cudaSuccess ||
       kqed::launch_reduce_partials(partial, nx, (int)tiles, d_sums, s) != cudaSuccess)
     return kqed::set_error("kqed_lattice_sum_noalloc: lattice kernel launch failed");
