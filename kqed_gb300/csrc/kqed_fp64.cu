@@ -41,6 +41,8 @@ std::atomic<uint64_t> g_launches{0};
    order d step j: yb = 2x*Ra[d][j]*yb - Rb[d][j]*ya + c_j */
 __constant__ double cRa[4][kNKMax];
 __constant__ double cRb[4][kNKMax];
+__constant__ float cRaf[4][kNKMax];
+__constant__ float cRbf[4][kNKMax];
 
 int upload_map_constants()
 {
@@ -52,6 +54,11 @@ int upload_map_constants()
   }
   if (cudaMemcpyToSymbol(cRa, ra, sizeof(ra)) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(cRb, rb, sizeof(rb)) != cudaSuccess) return 1;
+  float raf[4][kNKMax], rbf[4][kNKMax];
+  for (int o = 0; o < 4; o++)
+    for (int j = 0; j < kNKMax; j++) { raf[o][j] = (float)ra[o][j]; rbf[o][j] = (float)rb[o][j]; }
+  if (cudaMemcpyToSymbol(cRaf, raf, sizeof(raf)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(cRbf, rbf, sizeof(rbf)) != cudaSuccess) return 1;
   return 0;
 }
 
@@ -123,26 +130,47 @@ __device__ __forceinline__ Herm herm(double y, double y1, double y2)
   return h;
 }
 
-struct Rc { double a, b; };
-__device__ __forceinline__ void st0(Rc &r, double twox, double c)
+/* Clenshaw state and steps, in the arithmetic type S (double for the plain
+   FP64 form, float for the mixed form) */
+template <typename S> struct Rc { S a, b; };
+template <typename S> __device__ __forceinline__ void st0(Rc<S> &r, S twox, S c)
 {
-  const double t = fma(twox, r.b, c - r.a);
+  const S t = fma(twox, r.b, c - r.a);
   r.a = r.b; r.b = t;
 }
-__device__ __forceinline__ void stn(Rc &r, double A, double mB, double c)
+template <typename S> __device__ __forceinline__ void stn(Rc<S> &r, S A, S mB, S c)
 {
-  const double t = fma(A, r.b, fma(mB, r.a, c));
+  const S t = fma(A, r.b, fma(mB, r.a, c));
   r.a = r.b; r.b = t;
 }
-__device__ __forceinline__ double fin0(const Rc &r, double twox, double c0) { return c0 + fma(twox, r.b, -r.a); }
+template <typename S> __device__ __forceinline__ S fin0(const Rc<S> &r, S twox, S c0) { return c0 + fma(twox, r.b, -r.a); }
 
-__device__ __forceinline__ double2 ld2(const double *p) { return __ldg(reinterpret_cast<const double2 *>(p)); }
+template <typename S> struct V2T;
+template <> struct V2T<double> { typedef double2 t; };
+template <> struct V2T<float> { typedef float2 t; };
+template <typename S> __device__ __forceinline__ typename V2T<S>::t ld2(const S *p)
+{
+  return __ldg(reinterpret_cast<const typename V2T<S>::t *>(p));
+}
+
+/* Clenshaw ratio constants in the arithmetic type */
+template <typename S> __device__ __forceinline__ S cra(int o, int K);
+template <typename S> __device__ __forceinline__ S crb(int o, int K);
+template <> __device__ __forceinline__ double cra<double>(int o, int K) { return cRa[o][K]; }
+template <> __device__ __forceinline__ double crb<double>(int o, int K) { return cRb[o][K]; }
+template <> __device__ __forceinline__ float cra<float>(int o, int K) { return cRaf[o][K]; }
+template <> __device__ __forceinline__ float crb<float>(int o, int K) { return cRbf[o][K]; }
+
+/* node table in the arithmetic type */
+template <typename S> __device__ __forceinline__ const S *node_table(const DevTables &T);
+template <> __device__ __forceinline__ const double *node_table<double>(const DevTables &T) { return T.node; }
+template <> __device__ __forceinline__ const float *node_table<float>(const DevTables &T) { return T.node32; }
 
 /* interpolation weights of one generic pair */
-struct Wts {
-  double xA, xB, xC1, xC2, lAx;   /* Hermite in x (D folded in), lerp in x */
-  double yA, yB, yC1, yC2, lAy;   /* Hermite in y, lerp in y */
-  double dd;                      /* 1 when the flag2 y-difference is live, else 0 */
+template <typename S> struct Wts {
+  S xA, xB, xC1, xC2, lAx;   /* Hermite in x (D folded in), lerp in x */
+  S yA, yB, yC1, yC2, lAy;   /* Hermite in y, lerp in y */
+  S dd;                      /* 1 when the flag2 y-difference is live, else 0 */
 };
 
 /* Hermite-y of a (value, y-derivative) node pair at iy0/iy1; lerp-y of the
@@ -159,39 +187,40 @@ struct Wts {
    [28..31] QG2 d1     [32..35] QG3 d1    [36] QG3 d/dy      chnr_dV.c:383-411
    [37],[38] y-derivative differences of QG2, QG3 between the two y nodes
              (the flag2 second y-derivative, chnr_dV.c:444-466) */
-__device__ __noinline__ void interp_generic(const DevTables &T, const double *__restrict__ b00,
-                                            const double *__restrict__ b01,
-                                            const double *__restrict__ b10,
-                                            const double *__restrict__ b11, int Ktop,
-                                            const Wts &w, double twox, double *W)
+template <typename S>
+__device__ __noinline__ void interp_generic(const S *__restrict__ b00,
+                                            const S *__restrict__ b01,
+                                            const S *__restrict__ b10,
+                                            const S *__restrict__ b11, int Ktop,
+                                            const Wts<S> &w, S twox, double *W)
 {
   /* ---- pass 1: (QG0,dxQG0) (QL2,dxQL2) (QL4,dxQL4) (QG1,dxQG1) ---- */
   {
-    Rc A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
-    Rc B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
-    Rc C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
-    Rc D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
-    double fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
+    Rc<S> A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
+    Rc<S> B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
+    Rc<S> C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
+    Rc<S> D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
+    S fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
-      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
-      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
-      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
+      const S A1 = twox * cra<S>(1, K), mB1 = -crb<S>(1, K);
+      const S A2 = twox * cra<S>(2, K), mB2 = -crb<S>(2, K);
+      const S A3 = twox * cra<S>(3, K), mB3 = -crb<S>(3, K);
 #pragma unroll
       for (int f = 0; f < 4; f++) {
         const int sn = 2 * (2 * f), sp = 2 * (2 * f + 1);
-        const double2 n00 = ld2(b00 + o + sn), n01 = ld2(b01 + o + sn);
-        const double2 n10 = ld2(b10 + o + sn), n11 = ld2(b11 + o + sn);
-        const double2 p00 = ld2(b00 + o + sp), p01 = ld2(b01 + o + sp);
-        const double2 p10 = ld2(b10 + o + sp), p11 = ld2(b11 + o + sp);
-        const double hN0 = HY(n00, n01), hN1 = HY(n10, n11);
-        const double hP0 = HY(p00, p01), hP1 = HY(p10, p11);
-        const double lN0 = LY(n00, n01), lN1 = LY(n10, n11);
-        const double lP0 = LY(p00, p01), lP1 = LY(p10, p11);
-        const double c3 = HX(hN0, hN1, hP0, hP1);
-        const double c2 = HX(lN0, lN1, lP0, lP1);
-        const double c1 = LX(hP0, hP1);
+        const auto n00 = ld2<S>(b00 + o + sn), n01 = ld2<S>(b01 + o + sn);
+        const auto n10 = ld2<S>(b10 + o + sn), n11 = ld2<S>(b11 + o + sn);
+        const auto p00 = ld2<S>(b00 + o + sp), p01 = ld2<S>(b01 + o + sp);
+        const auto p10 = ld2<S>(b10 + o + sp), p11 = ld2<S>(b11 + o + sp);
+        const S hN0 = HY(n00, n01), hN1 = HY(n10, n11);
+        const S hP0 = HY(p00, p01), hP1 = HY(p10, p11);
+        const S lN0 = LY(n00, n01), lN1 = LY(n10, n11);
+        const S lP0 = LY(p00, p01), lP1 = LY(p10, p11);
+        const S c3 = HX(hN0, hN1, hP0, hP1);
+        const S c2 = HX(lN0, lN1, lP0, lP1);
+        const S c1 = LX(hP0, hP1);
         if (f == 0) { /* QG0, shift 0: c3 {0,1}, c2 0, c1 0 */
           if (K >= 1) { st0(A3o0, twox, c3); st0(A2o0, twox, c2); st0(A1o0, twox, c1); stn(A3o1, A1, mB1, c3); }
           else { fA3 = fin0(A3o0, twox, c3); fA2 = fin0(A2o0, twox, c2); fA1 = fin0(A1o0, twox, c1); }
@@ -207,47 +236,47 @@ __device__ __noinline__ void interp_generic(const DevTables &T, const double *__
         }
       }
     }
-    W[0] = 2.0 * A3o1.b; W[1] = fA1; W[2] = fA2; W[3] = fA3;
-    W[4] = 48.0 * B3o3.b; W[5] = 8.0 * B1o2.b; W[6] = 8.0 * B2o2.b; W[7] = 8.0 * B3o2.b;
-    W[8] = 8.0 * C3o2.b; W[9] = 2.0 * C1o1.b; W[10] = 2.0 * C2o1.b; W[11] = 2.0 * C3o1.b;
-    W[12] = 2.0 * D3o1.b; W[13] = fD1; W[14] = fD2; W[15] = fD3;
+    W[0] = S(2) * A3o1.b; W[1] = fA1; W[2] = fA2; W[3] = fA3;
+    W[4] = S(48) * B3o3.b; W[5] = S(8) * B1o2.b; W[6] = S(8) * B2o2.b; W[7] = S(8) * B3o2.b;
+    W[8] = S(8) * C3o2.b; W[9] = S(2) * C1o1.b; W[10] = S(2) * C2o1.b; W[11] = S(2) * C3o1.b;
+    W[12] = S(2) * D3o1.b; W[13] = fD1; W[14] = fD2; W[15] = fD3;
   }
   /* ---- pass 2: QG2 (8), dxQG2 (9), d2xQG2 (10), QG3 (11), dxQG3 (12), d2xQG3 (13) ---- */
   {
-    Rc E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
-    Rc F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
-    Rc G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
-    Rc H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
-    double fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
+    Rc<S> E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
+    Rc<S> F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
+    Rc<S> G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
+    Rc<S> H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
+    S fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
-      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
-      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
-      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
-      double hy0[6], hy1[6], ly0[6], ly1[6], dl0[6], dl1[6];
+      const S A1 = twox * cra<S>(1, K), mB1 = -crb<S>(1, K);
+      const S A2 = twox * cra<S>(2, K), mB2 = -crb<S>(2, K);
+      const S A3 = twox * cra<S>(3, K), mB3 = -crb<S>(3, K);
+      S hy0[6], hy1[6], ly0[6], ly1[6], dl0[6], dl1[6];
 #pragma unroll
       for (int s = 0; s < 6; s++) {
         const int so = 2 * (8 + s);
-        const double2 q00 = ld2(b00 + o + so), q01 = ld2(b01 + o + so);
-        const double2 q10 = ld2(b10 + o + so), q11 = ld2(b11 + o + so);
+        const auto q00 = ld2<S>(b00 + o + so), q01 = ld2<S>(b01 + o + so);
+        const auto q10 = ld2<S>(b10 + o + so), q11 = ld2<S>(b11 + o + so);
         hy0[s] = HY(q00, q01); hy1[s] = HY(q10, q11);
         ly0[s] = LY(q00, q01); ly1[s] = LY(q10, q11);
         dl0[s] = q01.y - q00.y; dl1[s] = q11.y - q10.y;
       }
       /* s: 0 QG2, 1 dxQG2, 2 d2xQG2, 3 QG3, 4 dxQG3, 5 d2xQG3 */
-      const double e3 = HX(hy0[0], hy1[0], hy0[1], hy1[1]);
-      const double e2 = HX(ly0[0], ly1[0], ly0[1], ly1[1]);
-      const double ed = w.dd * HX(dl0[0], dl1[0], dl0[1], dl1[1]);
-      const double f3 = HX(hy0[1], hy1[1], hy0[2], hy1[2]);
-      const double f2 = HX(ly0[1], ly1[1], ly0[2], ly1[2]);
-      const double f1 = LX(hy0[2], hy1[2]);
-      const double g3 = HX(hy0[4], hy1[4], hy0[5], hy1[5]);
-      const double g2 = HX(ly0[4], ly1[4], ly0[5], ly1[5]);
-      const double g1 = LX(hy0[5], hy1[5]);
-      const double h3 = HX(hy0[3], hy1[3], hy0[4], hy1[4]);
-      const double h2 = HX(ly0[3], ly1[3], ly0[4], ly1[4]);
-      const double hd = w.dd * HX(dl0[3], dl1[3], dl0[4], dl1[4]);
+      const S e3 = HX(hy0[0], hy1[0], hy0[1], hy1[1]);
+      const S e2 = HX(ly0[0], ly1[0], ly0[1], ly1[1]);
+      const S ed = w.dd * HX(dl0[0], dl1[0], dl0[1], dl1[1]);
+      const S f3 = HX(hy0[1], hy1[1], hy0[2], hy1[2]);
+      const S f2 = HX(ly0[1], ly1[1], ly0[2], ly1[2]);
+      const S f1 = LX(hy0[2], hy1[2]);
+      const S g3 = HX(hy0[4], hy1[4], hy0[5], hy1[5]);
+      const S g2 = HX(ly0[4], ly1[4], ly0[5], ly1[5]);
+      const S g1 = LX(hy0[5], hy1[5]);
+      const S h3 = HX(hy0[3], hy1[3], hy0[4], hy1[4]);
+      const S h2 = HX(ly0[3], ly1[3], ly0[4], ly1[4]);
+      const S hd = w.dd * HX(dl0[3], dl1[3], dl0[4], dl1[4]);
       if (K >= 1) {
         stn(E3o1, A1, mB1, e3); stn(E2o1, A1, mB1, e2); stn(Edo1, A1, mB1, ed);
         stn(F3o1, A1, mB1, f3); stn(F2o1, A1, mB1, f2); stn(F1o1, A1, mB1, f1);
@@ -262,13 +291,13 @@ __device__ __noinline__ void interp_generic(const DevTables &T, const double *__
       }
       if (K >= 3) stn(E3o3, A3, mB3, e3);
     }
-    /* QG2 d0 */ W[16] = 8.0 * E3o2.b; W[17] = 2.0 * F3o1.b; W[18] = 2.0 * E2o1.b; W[19] = 2.0 * E3o1.b;
-    /* dxQG2 d0 */ W[20] = 8.0 * F3o2.b; W[21] = 2.0 * F1o1.b; W[22] = 2.0 * F2o1.b; W[23] = 2.0 * F3o1.b;
-    /* dxQG3 d0 */ W[24] = 2.0 * G3o1.b; W[25] = fG1; W[26] = fG2; W[27] = fG3;
-    /* QG2 d1 */ W[28] = 48.0 * E3o3.b; W[29] = 8.0 * F3o2.b; W[30] = 8.0 * E2o2.b; W[31] = 8.0 * E3o2.b;
-    /* QG3 d1 */ W[32] = 8.0 * H3o2.b; W[33] = 2.0 * G3o1.b; W[34] = 2.0 * H2o1.b; W[35] = 2.0 * H3o1.b;
+    /* QG2 d0 */ W[16] = S(8) * E3o2.b; W[17] = S(2) * F3o1.b; W[18] = S(2) * E2o1.b; W[19] = S(2) * E3o1.b;
+    /* dxQG2 d0 */ W[20] = S(8) * F3o2.b; W[21] = S(2) * F1o1.b; W[22] = S(2) * F2o1.b; W[23] = S(2) * F3o1.b;
+    /* dxQG3 d0 */ W[24] = S(2) * G3o1.b; W[25] = fG1; W[26] = fG2; W[27] = fG3;
+    /* QG2 d1 */ W[28] = S(48) * E3o3.b; W[29] = S(8) * F3o2.b; W[30] = S(8) * E2o2.b; W[31] = S(8) * E3o2.b;
+    /* QG3 d1 */ W[32] = S(8) * H3o2.b; W[33] = S(2) * G3o1.b; W[34] = S(2) * H2o1.b; W[35] = S(2) * H3o1.b;
     W[36] = fH2;
-    W[37] = 2.0 * Edo1.b; W[38] = fHd;
+    W[37] = S(2) * Edo1.b; W[38] = fHd;
   }
 }
 /* Column layout of the per-x tables built by build_columns_kernel: for a
@@ -281,27 +310,28 @@ __device__ __noinline__ void interp_generic(const DevTables &T, const double *__
      F 18-21, G 22-25              : as A-D
    families A (QG0,dxQG0) B (QL2,dxQL2) C (QL4,dxQL4) D (QG1,dxQG1)
             E (QG2,dxQG2) F (dxQG2,d2xQG2) G (dxQG3,d2xQG3) H (QG3,dxQG3) */
-__device__ __noinline__ void interp_column(const double *__restrict__ r0,
-                                           const double *__restrict__ r1, int Ktop, const Wts &w,
-                                           double twox, double *W)
+template <typename S>
+__device__ __noinline__ void interp_column(const S *__restrict__ r0,
+                                           const S *__restrict__ r1, int Ktop, const Wts<S> &w,
+                                           S twox, double *W)
 {
   {
-    Rc A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
-    Rc B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
-    Rc C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
-    Rc D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
-    double fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
+    Rc<S> A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
+    Rc<S> B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
+    Rc<S> C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
+    Rc<S> D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
+    S fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
-      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
-      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
-      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
+      const S A1 = twox * cra<S>(1, K), mB1 = -crb<S>(1, K);
+      const S A2 = twox * cra<S>(2, K), mB2 = -crb<S>(2, K);
+      const S A3 = twox * cra<S>(3, K), mB3 = -crb<S>(3, K);
 #pragma unroll
       for (int f = 0; f < 4; f++) {
-        const double2 a3 = ld2(r0 + o + 4 * f), b3 = ld2(r1 + o + 4 * f);
-        const double2 a1 = ld2(r0 + o + 4 * f + 2), b1 = ld2(r1 + o + 4 * f + 2);
-        const double c3 = HY(a3, b3), c2 = LY(a3, b3), c1 = HY(a1, b1);
+        const auto a3 = ld2<S>(r0 + o + 4 * f), b3 = ld2<S>(r1 + o + 4 * f);
+        const auto a1 = ld2<S>(r0 + o + 4 * f + 2), b1 = ld2<S>(r1 + o + 4 * f + 2);
+        const S c3 = HY(a3, b3), c2 = LY(a3, b3), c1 = HY(a1, b1);
         if (f == 0) {
           if (K >= 1) { st0(A3o0, twox, c3); st0(A2o0, twox, c2); st0(A1o0, twox, c1); stn(A3o1, A1, mB1, c3); }
           else { fA3 = fin0(A3o0, twox, c3); fA2 = fin0(A2o0, twox, c2); fA1 = fin0(A1o0, twox, c1); }
@@ -317,33 +347,33 @@ __device__ __noinline__ void interp_column(const double *__restrict__ r0,
         }
       }
     }
-    W[0] = 2.0 * A3o1.b; W[1] = fA1; W[2] = fA2; W[3] = fA3;
-    W[4] = 48.0 * B3o3.b; W[5] = 8.0 * B1o2.b; W[6] = 8.0 * B2o2.b; W[7] = 8.0 * B3o2.b;
-    W[8] = 8.0 * C3o2.b; W[9] = 2.0 * C1o1.b; W[10] = 2.0 * C2o1.b; W[11] = 2.0 * C3o1.b;
-    W[12] = 2.0 * D3o1.b; W[13] = fD1; W[14] = fD2; W[15] = fD3;
+    W[0] = S(2) * A3o1.b; W[1] = fA1; W[2] = fA2; W[3] = fA3;
+    W[4] = S(48) * B3o3.b; W[5] = S(8) * B1o2.b; W[6] = S(8) * B2o2.b; W[7] = S(8) * B3o2.b;
+    W[8] = S(8) * C3o2.b; W[9] = S(2) * C1o1.b; W[10] = S(2) * C2o1.b; W[11] = S(2) * C3o1.b;
+    W[12] = S(2) * D3o1.b; W[13] = fD1; W[14] = fD2; W[15] = fD3;
   }
   {
-    Rc E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
-    Rc F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
-    Rc G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
-    Rc H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
-    double fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
+    Rc<S> E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
+    Rc<S> F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
+    Rc<S> G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
+    Rc<S> H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
+    S fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
-      const double A1 = twox * cRa[1][K], mB1 = -cRb[1][K];
-      const double A2 = twox * cRa[2][K], mB2 = -cRb[2][K];
-      const double A3 = twox * cRa[3][K], mB3 = -cRb[3][K];
-      const double2 ea = ld2(r0 + o + 16), eb = ld2(r1 + o + 16);
-      const double2 fa = ld2(r0 + o + 18), fb = ld2(r1 + o + 18);
-      const double2 fa1 = ld2(r0 + o + 20), fb1 = ld2(r1 + o + 20);
-      const double2 ga = ld2(r0 + o + 22), gb = ld2(r1 + o + 22);
-      const double2 ga1 = ld2(r0 + o + 24), gb1 = ld2(r1 + o + 24);
-      const double2 ha = ld2(r0 + o + 26), hb = ld2(r1 + o + 26);
-      const double e3 = HY(ea, eb), e2 = LY(ea, eb), ed = w.dd * (eb.y - ea.y);
-      const double f3 = HY(fa, fb), f2 = LY(fa, fb), f1 = HY(fa1, fb1);
-      const double g3 = HY(ga, gb), g2 = LY(ga, gb), g1 = HY(ga1, gb1);
-      const double h3 = HY(ha, hb), h2 = LY(ha, hb), hd = w.dd * (hb.y - ha.y);
+      const S A1 = twox * cra<S>(1, K), mB1 = -crb<S>(1, K);
+      const S A2 = twox * cra<S>(2, K), mB2 = -crb<S>(2, K);
+      const S A3 = twox * cra<S>(3, K), mB3 = -crb<S>(3, K);
+      const auto ea = ld2<S>(r0 + o + 16), eb = ld2<S>(r1 + o + 16);
+      const auto fa = ld2<S>(r0 + o + 18), fb = ld2<S>(r1 + o + 18);
+      const auto fa1 = ld2<S>(r0 + o + 20), fb1 = ld2<S>(r1 + o + 20);
+      const auto ga = ld2<S>(r0 + o + 22), gb = ld2<S>(r1 + o + 22);
+      const auto ga1 = ld2<S>(r0 + o + 24), gb1 = ld2<S>(r1 + o + 24);
+      const auto ha = ld2<S>(r0 + o + 26), hb = ld2<S>(r1 + o + 26);
+      const S e3 = HY(ea, eb), e2 = LY(ea, eb), ed = w.dd * (eb.y - ea.y);
+      const S f3 = HY(fa, fb), f2 = LY(fa, fb), f1 = HY(fa1, fb1);
+      const S g3 = HY(ga, gb), g2 = LY(ga, gb), g1 = HY(ga1, gb1);
+      const S h3 = HY(ha, hb), h2 = LY(ha, hb), hd = w.dd * (hb.y - ha.y);
       if (K >= 1) {
         stn(E3o1, A1, mB1, e3); stn(E2o1, A1, mB1, e2); stn(Edo1, A1, mB1, ed);
         stn(F3o1, A1, mB1, f3); stn(F2o1, A1, mB1, f2); stn(F1o1, A1, mB1, f1);
@@ -358,19 +388,20 @@ __device__ __noinline__ void interp_column(const double *__restrict__ r0,
       }
       if (K >= 3) stn(E3o3, A3, mB3, e3);
     }
-    W[16] = 8.0 * E3o2.b; W[17] = 2.0 * F3o1.b; W[18] = 2.0 * E2o1.b; W[19] = 2.0 * E3o1.b;
-    W[20] = 8.0 * F3o2.b; W[21] = 2.0 * F1o1.b; W[22] = 2.0 * F2o1.b; W[23] = 2.0 * F3o1.b;
-    W[24] = 2.0 * G3o1.b; W[25] = fG1; W[26] = fG2; W[27] = fG3;
-    W[28] = 48.0 * E3o3.b; W[29] = 8.0 * F3o2.b; W[30] = 8.0 * E2o2.b; W[31] = 8.0 * E3o2.b;
-    W[32] = 8.0 * H3o2.b; W[33] = 2.0 * G3o1.b; W[34] = 2.0 * H2o1.b; W[35] = 2.0 * H3o1.b;
+    W[16] = S(8) * E3o2.b; W[17] = S(2) * F3o1.b; W[18] = S(2) * E2o1.b; W[19] = S(2) * E3o1.b;
+    W[20] = S(8) * F3o2.b; W[21] = S(2) * F1o1.b; W[22] = S(2) * F2o1.b; W[23] = S(2) * F3o1.b;
+    W[24] = S(2) * G3o1.b; W[25] = fG1; W[26] = fG2; W[27] = fG3;
+    W[28] = S(48) * E3o3.b; W[29] = S(8) * F3o2.b; W[30] = S(8) * E2o2.b; W[31] = S(8) * E3o2.b;
+    W[32] = S(8) * H3o2.b; W[33] = S(2) * G3o1.b; W[34] = S(2) * H2o1.b; W[35] = S(2) * H3o1.b;
     W[36] = fH2;
-    W[37] = 2.0 * Edo1.b; W[38] = fHd;
+    W[37] = S(2) * Edo1.b; W[38] = fHd;
   }
 }
 
 /* Per-x column tables: thread per (x, iy, K) */
+template <typename S>
 __global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs, size_t nx,
-                                     double *__restrict__ col)
+                                     S *__restrict__ col)
 {
   const size_t per_x = (size_t)T.nstpy * T.NK;
   const size_t tot = nx * per_x;
@@ -379,7 +410,7 @@ __global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs,
     const size_t k = u / per_x;
     const int rem = (int)(u % per_x);
     const int iy = rem / T.NK, K = rem % T.NK;
-    double *out = col + u * kRow;
+    S *out = col + u * kRow;
     const double *xv = xs + 4 * k;
     double xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
     xsq = xsq < 1E-7 ? 1E-7 : xsq;
@@ -387,13 +418,13 @@ __global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs,
     const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
     if (!(X >= xlo && X <= xhi)) {
 #pragma unroll
-      for (int j = 0; j < kRow; j++) out[j] = 0.0;
+      for (int j = 0; j < kRow; j++) out[j] = S(0);
       continue;
     }
     const int flag_hx = (X >= xhi);
     const int ix0 = bsrch(T.XX, X, 0, T.nstpx);
     const int ix1 = flag_hx ? ix0 : ix0 + 1;
-    Wts w;
+    Wts<double> w;
     if (flag_hx) {
       w.xA = 1.0; w.xB = 0.0; w.xC1 = 0.0; w.xC2 = 0.0; w.lAx = 1.0;
     } else {
@@ -410,10 +441,10 @@ __global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs,
     for (int f = 0; f < 8; f++) {
       const int sn = 2 * fam[f][0], sp = 2 * fam[f][1];
       for (int c = 0; c < 2; c++)
-        out[dst[f] + c] = HX(__ldg(n0 + sn + c), __ldg(n1 + sn + c), __ldg(n0 + sp + c), __ldg(n1 + sp + c));
+        out[dst[f] + c] = (S)HX(__ldg(n0 + sn + c), __ldg(n1 + sn + c), __ldg(n0 + sp + c), __ldg(n1 + sp + c));
       if (fam[f][2] >= 0) {
         const int se = 2 * fam[f][2];
-        for (int c = 0; c < 2; c++) out[dst[f] + 2 + c] = LX(__ldg(n0 + se + c), __ldg(n1 + se + c));
+        for (int c = 0; c < 2; c++) out[dst[f] + 2 + c] = (S)LX(__ldg(n0 + se + c), __ldg(n1 + se + c));
       }
     }
   }
@@ -430,13 +461,13 @@ __global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs,
 __device__ double node_cheb(const double *__restrict__ base, int comp, int NK, int order, double x)
 {
   const double twox = 2.0 * x;
-  Rc r = {0, 0};
+  Rc<double> r = {0, 0};
   if (order == 0) {
-    for (int K = NK - 1; K >= 1; --K) st0(r, twox, __ldg(base + K * kRow + comp));
-    return fin0(r, twox, __ldg(base + comp));
+    for (int K = NK - 1; K >= 1; --K) st0<double>(r, twox, __ldg(base + K * kRow + comp));
+    return fin0<double>(r, twox, __ldg(base + comp));
   }
   for (int K = NK - 1; K >= order; --K)
-    stn(r, twox * cRa[order][K], -cRb[order][K], __ldg(base + K * kRow + comp));
+    stn<double>(r, twox * cRa[order][K], -cRb[order][K], __ldg(base + K * kRow + comp));
   return (order == 1 ? 2.0 : order == 2 ? 8.0 : 48.0) * r.b;
 }
 
@@ -846,51 +877,63 @@ __device__ int V_taylor(const DevTables &T, VS &D, double x, double y, double xs
 
 /* --------------------------------------------------- records (phase A) */
 
+/* Destination of a pair's record: float (mixed form) or double */
+struct Sink {
+  float *f;
+  double *d;
+  __device__ __forceinline__ void put(int i, double v) const
+  {
+    if (d) d[i] = v;
+    else f[i] = (float)v;
+  }
+};
+
 /* everything phase B needs about a generic pair, given its S/T/V scalars
    (post swap): the per-index vectors of chnr_dS/dT loops and get_dv
    (chnr_dV.c:277-325) */
-__device__ void fill_generic_record(double *R, const double *xv, const double *yv, const Inv &I,
+__device__ void fill_generic_record(const Sink &R, const double *xv, const double *yv, const Inv &I,
                                     double dg0dx, double dg0dy, double dg0dcb, const TS &T,
                                     const VS &D)
 {
   const double x = I.x, y = I.yorig, cb = I.cborig;
   const double rX = 1.0 / x, rY = 1.0 / y;
   for (int m = 0; m < 4; m++) {
-    R[R_XV + m] = xv[m];
-    R[R_YV + m] = yv[m];
+    R.put(R_XV + m, xv[m]);
+    R.put(R_YV + m, yv[m]);
     const double xh = xv[m] * rX, yh = yv[m] * rY;
-    R[R_XH + m] = xh;
-    R[R_YH + m] = yh;
-    R[R_C2 + m] = (xh - cb * yh) * rY;
-    R[R_C4 + m] = (yh - cb * xh) * rX;
+    R.put(R_XH + m, xh);
+    R.put(R_YH + m, yh);
+    R.put(R_C2 + m, (xh - cb * yh) * rY);
+    R.put(R_C4 + m, (yh - cb * xh) * rX);
   }
-  R[R_X] = x; R[R_YO] = y; R[R_CB] = cb; R[R_XSQ] = I.xsq; R[R_YSQ] = I.ysq; R[R_XDY] = I.xdoty;
-  R[R_RX] = rX; R[R_RY] = rY;
-  R[R_S + 0] = dg0dx; R[R_S + 1] = dg0dy; R[R_S + 2] = dg0dcb;
-  R[R_T + 0] = T.ell1; R[R_T + 1] = T.ell2; R[R_T + 2] = T.ell3;
-  R[R_T + 3] = T.d1x; R[R_T + 4] = T.d1y; R[R_T + 5] = T.d1cb;
-  R[R_T + 6] = T.d2x; R[R_T + 7] = T.d2y; R[R_T + 8] = T.d2cb;
-  R[R_T + 9] = T.d3x; R[R_T + 10] = T.d3y; R[R_T + 11] = T.d3cb;
+  R.put(R_X, x); R.put(R_YO, y); R.put(R_CB, cb); R.put(R_XSQ, I.xsq); R.put(R_YSQ, I.ysq); R.put(R_XDY, I.xdoty);
+  R.put(R_RX, rX); R.put(R_RY, rY);
+  R.put(R_S + 0, dg0dx); R.put(R_S + 1, dg0dy); R.put(R_S + 2, dg0dcb);
+  R.put(R_T + 0, T.ell1); R.put(R_T + 1, T.ell2); R.put(R_T + 2, T.ell3);
+  R.put(R_T + 3, T.d1x); R.put(R_T + 4, T.d1y); R.put(R_T + 5, T.d1cb);
+  R.put(R_T + 6, T.d2x); R.put(R_T + 7, T.d2y); R.put(R_T + 8, T.d2cb);
+  R.put(R_T + 9, T.d3x); R.put(R_T + 10, T.d3y); R.put(R_T + 11, T.d3cb);
   for (int m = 0; m < 4; m++) {
-    R[R_VD + 0 + m] = xv[m] * D.ddg1dxdx + yv[m] * D.ddg2dxdx;
-    R[R_VD + 4 + m] = xv[m] * D.ddg1dxdy + yv[m] * D.ddg2dxdy;
-    R[R_VD + 8 + m] = xv[m] * D.ddg1dxdcb + yv[m] * D.ddg2dxdcb;
-    R[R_VD + 12 + m] = xv[m] * D.ddg1dydcb + yv[m] * D.ddg2dydcb;
-    R[R_VD + 16 + m] = xv[m] * D.ddg1dxdcb + yv[m] * D.ddg2dxdcb;
-    R[R_VD + 20 + m] = xv[m] * D.ddg1dcbdcb + yv[m] * D.ddg2dcbdcb;
-    R[R_VD + 24 + m] = (xv[m] * D.dg1dx + yv[m] * D.dg2dx) * rX;
-    R[R_VD + 28 + m] = (xv[m] * D.dg1dcb + yv[m] * D.dg2dcb) * rX;
+    R.put(R_VD + 0 + m, xv[m] * D.ddg1dxdx + yv[m] * D.ddg2dxdx);
+    R.put(R_VD + 4 + m, xv[m] * D.ddg1dxdy + yv[m] * D.ddg2dxdy);
+    R.put(R_VD + 8 + m, xv[m] * D.ddg1dxdcb + yv[m] * D.ddg2dxdcb);
+    R.put(R_VD + 12 + m, xv[m] * D.ddg1dydcb + yv[m] * D.ddg2dydcb);
+    R.put(R_VD + 16 + m, xv[m] * D.ddg1dxdcb + yv[m] * D.ddg2dxdcb);
+    R.put(R_VD + 20 + m, xv[m] * D.ddg1dcbdcb + yv[m] * D.ddg2dcbdcb);
+    R.put(R_VD + 24 + m, (xv[m] * D.dg1dx + yv[m] * D.dg2dx) * rX);
+    R.put(R_VD + 28 + m, (xv[m] * D.dg1dcb + yv[m] * D.dg2dcb) * rX);
   }
   for (int m = 0; m < 4; m++) {
-    const double xh = R[R_XH + m], yh = R[R_YH + m];
-    R[R_VA + m] = (D.dg1dx + D.dg2dx) * xh + (D.dg1dcb + D.dg2dcb) * R[R_C4 + m];
-    R[R_VB + m] = (D.dg1dx * xh + D.dg1dy * yh + D.dg1dcb * (xh * rY + yh * rX - cb * (xh * rX + yh * rY)));
+    const double xh = xv[m] * rX, yh = yv[m] * rY;
+    const double c4 = (yh - cb * xh) * rX;
+    R.put(R_VA + m, (D.dg1dx + D.dg2dx) * xh + (D.dg1dcb + D.dg2dcb) * c4);
+    R.put(R_VB + m, (D.dg1dx * xh + D.dg1dy * yh + D.dg1dcb * (xh * rY + yh * rX - cb * (xh * rX + yh * rY))));
   }
 }
 
 /* Tabd_xeq0 scalars, src/LIBFILES/Tabd.c:22-84; returns 1 when |y| is above
    the TAYLORX grid (zero kernel) */
-__device__ int fill_x0_record(const DevTables &T, double *R, const double *yv)
+__device__ int fill_x0_record(const DevTables &T, const Sink &R, const double *yv)
 {
   const double ysq = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
   const double y = sqrt(fabs(ysq));
@@ -916,28 +959,28 @@ __device__ int fill_x0_record(const DevTables &T, double *R, const double *yv)
   for (int m = 0; m < 4; m++) {
     const double yh = yv[m] / y;
     const double dg0dy = yh * fy / 2, dg0dx = yh * fx / 2;
-    R[X0_Q + m] = yv[m];
-    R[X0_QH + m] = yh;
-    R[X0_YVE + m] = yv[m] * E;
-    R[X0_YVL3 + m] = yv[m] * ell3a;
-    R[X0_YHD1 + m] = yh * D1;
-    R[X0_YHD2 + m] = yh * D2;
-    R[X0_YHD3 + m] = yh * D3;
-    R[X0_YHG2 + m] = yh * dg2dx;
+    R.put(X0_Q + m, yv[m]);
+    R.put(X0_QH + m, yh);
+    R.put(X0_YVE + m, yv[m] * E);
+    R.put(X0_YVL3 + m, yv[m] * ell3a);
+    R.put(X0_YHD1 + m, yh * D1);
+    R.put(X0_YHD2 + m, yh * D2);
+    R.put(X0_YHD3 + m, yh * D3);
+    R.put(X0_YHG2 + m, yh * dg2dx);
     const double yalf2dx = yh * (dell2adx);
-    R[X0_YA2 + m] = yalf2dx;
-    R[X0_TII + m] = dg0dx - 0.5 * R[X0_YVL3 + m] - ysq_4 * yalf2dx;
-    R[X0_TIII + m] = (dg0dx + dg0dy) - 0.5 * R[X0_YVE + m] - ysq_4 * R[X0_YHD2 + m];
-    R[X0_YD12 + m] = yh * D12;
+    R.put(X0_YA2 + m, yalf2dx);
+    R.put(X0_TII + m, dg0dx - 0.5 * (yv[m] * ell3a) - ysq_4 * yalf2dx);
+    R.put(X0_TIII + m, (dg0dx + dg0dy) - 0.5 * (yv[m] * E) - ysq_4 * (yh * D2));
+    R.put(X0_YD12 + m, yh * D12);
   }
-  R[X0_PHI1] = phi1;
-  R[X0_PHI2] = phi2;
+  R.put(X0_PHI1, phi1);
+  R.put(X0_PHI2, phi2);
   return 0;
 }
 
 /* Tabd_yeq0 scalars, src/LIBFILES/Tabd.c:116-195; returns 1 when |x| is
    beyond the grid (zero kernel) */
-__device__ int fill_y0_record(const DevTables &T, double *R, const double *xv)
+__device__ int fill_y0_record(const DevTables &T, const Sink &R, const double *xv)
 {
   const double xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
   const double x = sqrt(fabs(xsq));
@@ -975,15 +1018,15 @@ __device__ int fill_y0_record(const DevTables &T, double *R, const double *xv)
   for (int m = 0; m < 4; m++) {
     const double xh = xv[m] / x;
     const double dg0dy = xh * fy / 2, dg0dx = xh * fx / 2;
-    R[Y0_X + m] = xv[m];
-    R[Y0_XH + m] = xh;
-    R[Y0_XVE + m] = xv[m] * E;
-    R[Y0_XVL1 + m] = xv[m] * ell1;
-    R[Y0_XHD + m] = xh * (dell1dx);
-    R[Y0_TII + m] = (dg0dx - 0.5 * R[Y0_XVL1 + m]);
-    R[Y0_DG0 + m] = (dg0dx + dg0dy - 0.5 * R[Y0_XVE + m]);
+    R.put(Y0_X + m, xv[m]);
+    R.put(Y0_XH + m, xh);
+    R.put(Y0_XVE + m, xv[m] * E);
+    R.put(Y0_XVL1 + m, xv[m] * ell1);
+    R.put(Y0_XHD + m, xh * (dell1dx));
+    R.put(Y0_TII + m, (dg0dx - 0.5 * (xv[m] * ell1)));
+    R.put(Y0_DG0 + m, (dg0dx + dg0dy - 0.5 * (xv[m] * E)));
   }
-  R[Y0_XSQ4] = xsq_4; R[Y0_D1] = D1; R[Y0_D2] = D2; R[Y0_D3] = D3; R[Y0_D4] = D4;
+  R.put(Y0_XSQ4, xsq_4); R.put(Y0_D1, D1); R.put(Y0_D2, D2); R.put(Y0_D3, D3); R.put(Y0_D4, D4);
   return 0;
 }
 
@@ -994,8 +1037,9 @@ __device__ __forceinline__ bool is_zero4(const double *v)
 
 /* Phase A for one pair: classify (QED_kernel_L0, kernels.c:81-115), fill the
    record, return the kind and status bits. */
-__device__ int phase_a(const DevTables &T, const double *xv, const double *yv, double *R,
-                       int &status, const double *colx = nullptr)
+template <typename S>
+__device__ int phase_a(const DevTables &T, const double *xv, const double *yv, const Sink &R,
+                       int &status, const S *colx = nullptr, const double *col64 = nullptr)
 {
   status = 0;
   /* non-finite input: the reference's grid search would run off the tables;
@@ -1045,7 +1089,7 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, d
     const int flag_hy = (I.y >= __ldg(T.YY + T.nstpy - 1));
     const int ix0 = I.ix, ix1 = flag_hx ? I.ix : I.ix + 1;
     const int iy0 = I.iy, iy1 = flag_hy ? I.iy : I.iy + 1;
-    Wts w;
+    Wts<double> w;
     if (flag_hx) {
       w.xA = 1.0; w.xB = 0.0; w.xC1 = 0.0; w.xC2 = 0.0; w.lAx = 1.0;
     } else {
@@ -1064,15 +1108,33 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, d
     const int NK = T.NK;
     const int Ktop = max(__ldg(T.nfx + ix0), __ldg(T.nfx + ix1)) + 2;
     double W[39];
-    if (colx) {
-      interp_column(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, w,
-                    2.0 * I.cb, W);
+    Wts<S> ws;
+    ws.xA = (S)w.xA; ws.xB = (S)w.xB; ws.xC1 = (S)w.xC1; ws.xC2 = (S)w.xC2; ws.lAx = (S)w.lAx;
+    ws.yA = (S)w.yA; ws.yB = (S)w.yB; ws.yC1 = (S)w.yC1; ws.yC2 = (S)w.yC2; ws.lAy = (S)w.lAy;
+    ws.dd = (S)w.dd;
+    /* the float form keeps FP64 for the Chebyshev sums near cb = +-1, where
+       their derivatives lose digits in float */
+    const bool cb64 = sizeof(S) == 4 && fabs(I.cb) > 0.99;
+    if (cb64 && col64) {
+      Wts<double> wd = w;
+      interp_column<double>(col64 + (size_t)iy0 * NK * kRow, col64 + (size_t)iy1 * NK * kRow, Ktop,
+                            wd, 2.0 * I.cb, W);
+    } else if (cb64) {
+      const double *node = T.node;
+      interp_generic<double>(node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow,
+                             node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow,
+                             node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow,
+                             node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, w, 2.0 * I.cb, W);
+    } else if (colx) {
+      interp_column<S>(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, ws,
+                       (S)(2.0 * I.cb), W);
     } else {
-      const double *b00 = T.node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow;
-      const double *b01 = T.node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow;
-      const double *b10 = T.node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow;
-      const double *b11 = T.node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow;
-      interp_generic(T, b00, b01, b10, b11, Ktop, w, 2.0 * I.cb, W);
+      const S *node = node_table<S>(T);
+      const S *b00 = node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow;
+      const S *b01 = node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow;
+      const S *b10 = node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow;
+      const S *b11 = node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow;
+      interp_generic<S>(b00, b01, b10, b11, Ktop, ws, (S)(2.0 * I.cb), W);
     }
     dg0dcb = W[0]; dg0dx = W[1]; dg0dy = W[2];
     T_generic(I, W, Ts);
@@ -1092,21 +1154,23 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, d
 
 /* 200 STV components of one generic pair into stv[] (lane-parallel):
    chnr_dS.c:85-93, chnr_dT.c:353-385, get_dv chnr_dV.c:326-357 */
-__device__ __forceinline__ void stv_generic(const double *R, double *stv, int lane)
+template <typename S>
+__device__ __forceinline__ void stv_generic(const S *R, S *stv, int lane)
 {
+  const S z = S(0);
 #pragma unroll
   for (int r = 0; r < 2; r++) {
     const int idx = r * 32 + lane;
     const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
     const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
-    const double *xv = R + R_XV, *yv = R + R_YV;
-    const double c1 = R[R_YH + b], c3 = R[R_XH + b], c2 = R[R_C2 + b], c4 = R[R_C4 + b];
-    const double t1 = (d_ab ? yv[d] : 0.0) + (d_bd ? yv[a] : 0.0) - (d_ad ? 0.5 * yv[b] : 0.0);
-    const double t2 = (d_ab ? xv[d] : 0.0) + (d_bd ? xv[a] : 0.0) - (d_ad ? 0.5 * xv[b] : 0.0);
-    const double t3 = xv[a] * xv[d] - (d_ad ? R[R_XSQ] / 4 : 0.0);
-    const double t4 = yv[a] * yv[d] - (d_ad ? R[R_YSQ] / 4 : 0.0);
-    const double t5 = xv[a] * yv[d] + yv[a] * xv[d] - (d_ad ? 0.5 * R[R_XDY] : 0.0);
-    const double *T = R + R_T;
+    const S *xv = R + R_XV, *yv = R + R_YV;
+    const S c1 = R[R_YH + b], c3 = R[R_XH + b], c2 = R[R_C2 + b], c4 = R[R_C4 + b];
+    const S t1 = (d_ab ? yv[d] : z) + (d_bd ? yv[a] : z) - (d_ad ? S(0.5) * yv[b] : z);
+    const S t2 = (d_ab ? xv[d] : z) + (d_bd ? xv[a] : z) - (d_ad ? S(0.5) * xv[b] : z);
+    const S t3 = xv[a] * xv[d] - (d_ad ? R[R_XSQ] * S(0.25) : z);
+    const S t4 = yv[a] * yv[d] - (d_ad ? R[R_YSQ] * S(0.25) : z);
+    const S t5 = xv[a] * yv[d] + yv[a] * xv[d] - (d_ad ? S(0.5) * R[R_XDY] : z);
+    const S *T = R + R_T;
     stv[72 + idx] = t1 * T[1] + t2 * T[2] + t3 * (c1 * T[4] + c2 * T[5]) +
                     t4 * (c1 * T[7] + c2 * T[8]) + t5 * (c1 * T[10] + c2 * T[11]);
     stv[8 + idx] = t2 * T[0] + t1 * T[2] + t3 * (c3 * T[3] + c4 * T[5]) +
@@ -1117,16 +1181,16 @@ __device__ __forceinline__ void stv_generic(const double *R, double *stv, int la
     const int idx = r * 32 + lane;
     const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
     const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
-    const double xa = R[R_XH + a], xb = R[R_XH + b], ya = R[R_YH + a], yb = R[R_YH + b];
-    const double cb = R[R_CB];
-    const double c4a = R[R_C4 + a];
-    const double c2c4 = R[R_C2 + b] + R[R_C4 + b];
-    const double xaxb = xa * xb, yayb = ya * yb, xayb = xa * yb, yaxb = ya * xb;
-    const double dab = d_ab ? 1.0 : 0.0;
-    const double c1 = ((cb * (3.0 * xaxb - dab) - xayb - yaxb) * R[R_RX] +
-                       (dab + xayb * cb - xaxb - yayb) * R[R_RY]);
-    const double *Dv = R + R_VD;
-    double f = d_bd ? R[R_VA + a] : 0.0;
+    const S xa = R[R_XH + a], xb = R[R_XH + b], ya = R[R_YH + a], yb = R[R_YH + b];
+    const S cb = R[R_CB];
+    const S c4a = R[R_C4 + a];
+    const S c2c4 = R[R_C2 + b] + R[R_C4 + b];
+    const S xaxb = xa * xb, yayb = ya * yb, xayb = xa * yb, yaxb = ya * xb;
+    const S dab = d_ab ? S(1) : z;
+    const S c1 = ((cb * (S(3) * xaxb - dab) - xayb - yaxb) * R[R_RX] +
+                  (dab + xayb * cb - xaxb - yayb) * R[R_RY]);
+    const S *Dv = R + R_VD;
+    S f = d_bd ? R[R_VA + a] : z;
     if (d_ad) f += R[R_VB + b];
     f += Dv[0 + d] * xaxb + Dv[4 + d] * xayb;
     f += (Dv[8 + d] * xb + Dv[12 + d] * yb) * c4a;
@@ -1142,23 +1206,25 @@ __device__ __forceinline__ void stv_generic(const double *R, double *stv, int la
 }
 
 /* x = 0: tI -> V, tII -> Tx, tIII -> Ty (Tabd.c:87-111) */
-__device__ __forceinline__ void stv_x0(const double *R, double *stv, int lane)
+template <typename S>
+__device__ __forceinline__ void stv_x0(const S *R, S *stv, int lane)
 {
+  const S z = S(0);
 #pragma unroll
   for (int r = 0; r < 2; r++) {
     const int idx = r * 32 + lane;
     const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
     const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
-    const double *yv = R + X0_Q, *yh = R + X0_QH;
-    double tIII = yv[a] * yv[d] * R[X0_YHD2 + b];
+    const S *yv = R + X0_Q, *yh = R + X0_QH;
+    S tIII = yv[a] * yv[d] * R[X0_YHD2 + b];
     if (d_ab) tIII += R[X0_YVE + d];
     if (d_bd) tIII += R[X0_YVE + a];
     if (d_ad) tIII += R[X0_TIII + b];
-    double tII = yv[b] * yv[d] * R[X0_YA2 + a];
+    S tII = yv[b] * yv[d] * R[X0_YA2 + a];
     if (d_bd) tII += R[X0_TII + a];
-    tII += ((d_ab ? R[X0_YVL3 + d] : 0.0) + (d_ad ? R[X0_YVL3 + b] : 0.0));
-    const double tIsum = 2 * ((d_ab ? R[X0_PHI1] : 0.0) + yh[a] * yh[b] * R[X0_PHI2]);
-    double tI = d_bd ? R[X0_YD12 + a] : 0.0;
+    tII += ((d_ab ? R[X0_YVL3 + d] : z) + (d_ad ? R[X0_YVL3 + b] : z));
+    const S tIsum = S(2) * ((d_ab ? R[X0_PHI1] : z) + yh[a] * yh[b] * R[X0_PHI2]);
+    S tI = d_bd ? R[X0_YD12 + a] : z;
     if (d_ab) tI += R[X0_YHG2 + d];
     tI += R[X0_YHD3 + b] * yh[a] * yh[d];
     if (d_ad) tI += R[X0_YHD1 + b];
@@ -1170,30 +1236,32 @@ __device__ __forceinline__ void stv_x0(const double *R, double *stv, int lane)
 }
 
 /* y = 0 (and x = y): Tabd.c:196-217 */
-__device__ __forceinline__ void stv_y0(const double *R, double *stv, int lane)
+template <typename S>
+__device__ __forceinline__ void stv_y0(const S *R, S *stv, int lane)
 {
+  const S z = S(0);
 #pragma unroll
   for (int r = 0; r < 2; r++) {
     const int idx = r * 32 + lane;
     const int a = idx >> 4, b = (idx >> 2) & 3, d = idx & 3;
     const bool d_ab = (a == b), d_bd = (b == d), d_ad = (a == d);
-    const double *xv = R + Y0_X, *xh = R + Y0_XH;
-    const double xsq_4 = R[Y0_XSQ4];
-    const double xad = (xv[a] * xv[d] - (d_ad ? xsq_4 : 0.0));
-    double tIII = xad * xh[b] * R[Y0_D1];
+    const S *xv = R + Y0_X, *xh = R + Y0_XH;
+    const S xsq_4 = R[Y0_XSQ4];
+    const S xad = (xv[a] * xv[d] - (d_ad ? xsq_4 : z));
+    S tIII = xad * xh[b] * R[Y0_D1];
     if (d_ab) tIII += R[Y0_XVE + d];
     if (d_bd) tIII += R[Y0_XVE + a];
     if (d_ad) tIII += R[Y0_DG0 + b];
-    double tII = (xv[b] * xv[d] - (d_bd ? xsq_4 : 0.0)) * R[Y0_XHD + a];
+    S tII = (xv[b] * xv[d] - (d_bd ? xsq_4 : z)) * R[Y0_XHD + a];
     if (d_ab) tII += R[Y0_XVL1 + d];
     if (d_ad) tII += R[Y0_XVL1 + b];
     if (d_bd) tII += R[Y0_TII + a];
-    double s = 0.0;
-    if (d_ad) s += xh[b];
-    if (d_bd) s += xh[a];
-    if (d_ab) s += xh[d];
-    const double tI = (s - xh[a] * xh[b] * xh[d]) * R[Y0_D4] +
-                      xh[a] * (xh[b] * xv[d] * R[Y0_D2] - (d_bd ? R[Y0_D3] : 0.0));
+    S sm = z;
+    if (d_ad) sm += xh[b];
+    if (d_bd) sm += xh[a];
+    if (d_ab) sm += xh[d];
+    const S tI = (sm - xh[a] * xh[b] * xh[d]) * R[Y0_D4] +
+                 xh[a] * (xh[b] * xv[d] * R[Y0_D2] - (d_bd ? R[Y0_D3] : z));
     stv[136 + idx] = tI;
     stv[8 + idx] = tII;
     stv[72 + idx] = tIII;
@@ -1202,21 +1270,36 @@ __device__ __forceinline__ void stv_y0(const double *R, double *stv, int lane)
 
 /* the STV -> 384 map for the current pair, rows dealt to lanes; result into
    tbuf (natural row order) */
+template <typename S>
 __device__ __forceinline__ void apply_map_warp(const uint16_t *ent, const uint16_t *rows,
-                                               const MapSched &S, const double *coef,
-                                               const double *stv, double *tbuf, int lane)
+                                               const MapSched &M, const S *coef, const S *stv,
+                                               S *tbuf, int lane)
 {
 #pragma unroll 1
   for (int r = 0; r < kMapRounds; r++) {
-    const uint16_t *e = ent + S.off[r] + lane;
-    double acc = 0.0;
-    const int len = S.len[r];
+    const uint16_t *e = ent + M.off[r] + lane;
+    const int len = M.len[r];
+    if (sizeof(S) == 8) {
+      S acc = S(0);
 #pragma unroll 4
-    for (int s = 0; s < len; s++) {
-      const uint16_t v = e[s * 32];
-      acc = fma(coef[v >> 8], stv[v & 0xff], acc);
+      for (int q = 0; q < len; q++) {
+        const uint16_t v = e[q * 32];
+        acc = fma(coef[v >> 8], stv[v & 0xff], acc);
+      }
+      tbuf[rows[r * 32 + lane]] = acc;
+    } else {
+      /* float: the products by +-1/2, +-1, +-2 are exact; Kahan-compensated sum */
+      S acc = S(0), cmp = S(0);
+#pragma unroll 4
+      for (int q = 0; q < len; q++) {
+        const uint16_t v = e[q * 32];
+        const S yv = coef[v >> 8] * stv[v & 0xff] - cmp;
+        const S t = acc + yv;
+        cmp = (t - acc) - yv;
+        acc = t;
+      }
+      tbuf[rows[r * 32 + lane]] = acc;
     }
-    tbuf[rows[r * 32 + lane]] = acc;
   }
 }
 
@@ -1228,110 +1311,201 @@ __device__ __forceinline__ int mulam(int i)
 
 /* ------------------------------------------------------------ kernels */
 
-struct WarpSmem {
-  double *rec;   /* [32][REC] */
-  double *stv;   /* [200] components, [200] = 0 (padding target of the map) */
-  double *tbuf;  /* [384] */
-  int *kind;     /* [32] */
-};
+/* Per-warp shared memory.  Records of the warp's 32 pairs are stored in the
+   record type S of the fast assembly path; the mixed form (S = float) keeps
+   up to kSlots64 FP64 records for pairs it assembles in FP64.  The STV and
+   384-component buffers are sized for doubles and reused as floats. */
+constexpr int kSlots64 = 4;
+template <typename S> struct NSlots { static constexpr int v = 0; };
+template <> struct NSlots<float> { static constexpr int v = kSlots64; };
 
-__host__ __device__ constexpr size_t warp_smem_doubles() { return 32 * REC + 202 + 384; }
-
-size_t smem_bytes_l0(int wpb)
+template <typename S> __host__ __device__ constexpr size_t warp_smem_bytes()
 {
-  return (size_t)wpb * (warp_smem_doubles() * sizeof(double) + 32 * sizeof(int)) + 8 * sizeof(double) +
-         (size_t)(2 * 3072 + 2 * 384) * sizeof(uint16_t);
+  return 32 * REC * sizeof(S) + NSlots<S>::v * REC * sizeof(double) + (202 + 384) * sizeof(double) +
+         32 * sizeof(int);
 }
 
-/* block prologue: coefficient LUT and the two map schedules into shared memory */
-__device__ __forceinline__ void load_maps(const DevMaps &M, double *coef, uint16_t *eg,
-                                          uint16_t *ez, uint16_t *rg, uint16_t *rz)
+constexpr size_t kSchedBytes = (size_t)(2 * 3072 + 2 * 384) * sizeof(uint16_t);
+
+template <typename S> static size_t smem_bytes(int wpb)
 {
-  if (threadIdx.x < 8) {
-    const double c[8] = {-2.0, -1.0, -0.5, 0.5, 1.0, 2.0, 0.0, 0.0};
-    coef[threadIdx.x] = c[threadIdx.x];
-  }
-  for (int i = threadIdx.x; i < M.gen.total; i += blockDim.x) eg[i] = M.ent_gen[i];
-  for (int i = threadIdx.x; i < M.zero.total; i += blockDim.x) ez[i] = M.ent_zero[i];
-  for (int i = threadIdx.x; i < 384; i += blockDim.x) { rg[i] = M.row_gen[i]; rz[i] = M.row_zero[i]; }
-  __syncthreads();
+  return (size_t)wpb * warp_smem_bytes<S>() + 8 * sizeof(double) + 8 * sizeof(float) + kSchedBytes;
 }
 
-struct SmemLayout {
-  double *coef;
-  uint16_t *eg, *ez, *rg, *rz;
-  WarpSmem w;
+size_t smem_bytes_l0(int wpb) { return smem_bytes<double>(wpb); }
+
+template <typename S> struct WarpSmem {
+  S *rec;          /* [32][REC] */
+  double *rec64;   /* [kSlots64][REC] (mixed form) */
+  double *stvd;    /* [202] as doubles; [200] = 0 is the map's padding target */
+  double *tbufd;   /* [384] as doubles */
+  int *kind;       /* [32]: kind | fp64-assembly flag << 8 | slot << 9 */
 };
 
-__device__ __forceinline__ SmemLayout carve(int wpb, const DevMaps &M)
+template <typename S> struct SmemLayout {
+  double *coefd;
+  float *coeff;
+  uint16_t *eg, *ez, *rg, *rz;   /* map schedules */
+  WarpSmem<S> w;
+};
+
+template <typename S>
+__device__ __forceinline__ SmemLayout<S> carve(int wpb)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemLayout L;
+  SmemLayout<S> L;
   const int warp = threadIdx.x >> 5;
-  double *wbase = reinterpret_cast<double *>(smem_raw) + (size_t)warp * warp_smem_doubles();
-  L.w.rec = wbase;
-  L.w.stv = wbase + 32 * REC;
-  L.w.tbuf = L.w.stv + 202;
-  double *after = reinterpret_cast<double *>(smem_raw) + (size_t)wpb * warp_smem_doubles();
-  L.coef = after;
-  int *kinds = reinterpret_cast<int *>(after + 8);
-  L.w.kind = kinds + warp * 32;
-  uint16_t *u = reinterpret_cast<uint16_t *>(kinds + wpb * 32);
-  L.eg = u;
-  L.ez = u + 3072;
+  unsigned char *wb = smem_raw + (size_t)warp * warp_smem_bytes<S>();
+  L.w.stvd = reinterpret_cast<double *>(wb);
+  L.w.tbufd = L.w.stvd + 202;
+  L.w.rec64 = L.w.tbufd + 384;
+  L.w.rec = reinterpret_cast<S *>(L.w.rec64 + NSlots<S>::v * REC);
+  L.w.kind = reinterpret_cast<int *>(L.w.rec + 32 * REC);
+  unsigned char *after = smem_raw + (size_t)wpb * warp_smem_bytes<S>();
+  L.coefd = reinterpret_cast<double *>(after);
+  L.coeff = reinterpret_cast<float *>(L.coefd + 8);
+  L.eg = reinterpret_cast<uint16_t *>(L.coeff + 8);
+  L.ez = L.eg + 3072;
   L.rg = L.ez + 3072;
   L.rz = L.rg + 384;
   return L;
 }
 
-/* assemble the 384 components of the warp's pair q into tbuf; returns false
-   for a zero kernel */
-__device__ __forceinline__ bool assemble_pair(const SmemLayout &L, const DevMaps &M, int q,
-                                              int lane, bool &perm)
+template <typename S>
+__device__ __forceinline__ void block_prologue(const DevMaps &M, SmemLayout<S> &L)
 {
-  const int kind = L.w.kind[q];
+  if (threadIdx.x < 8) {
+    const float c[8] = {-2.0f, -1.0f, -0.5f, 0.5f, 1.0f, 2.0f, 0.0f, 0.0f};
+    L.coefd[threadIdx.x] = (double)c[threadIdx.x];
+    L.coeff[threadIdx.x] = c[threadIdx.x];
+  }
+  for (int i = threadIdx.x; i < M.gen.total; i += blockDim.x) L.eg[i] = M.ent_gen[i];
+  for (int i = threadIdx.x; i < M.zero.total; i += blockDim.x) L.ez[i] = M.ent_zero[i];
+  for (int i = threadIdx.x; i < 384; i += blockDim.x) { L.rg[i] = M.row_gen[i]; L.rz[i] = M.row_zero[i]; }
+  __syncthreads();
+}
+
+/* assemble the 384 components of one pair into tbuf (type A) */
+template <typename A, typename S>
+__device__ __forceinline__ void assemble(const SmemLayout<S> &L, const DevMaps &M, int kind,
+                                         const A *R, A *stv, A *tbuf, const A *coef, int lane)
+{
+  if (lane == 0) { stv[200] = A(0); stv[201] = A(0); }
+  if (kind == K_GEN) stv_generic<A>(R, stv, lane);
+  else if (kind == K_X0) stv_x0<A>(R, stv, lane);
+  else stv_y0<A>(R, stv, lane);
+  __syncwarp();
+  if (kind == K_GEN) apply_map_warp<A>(L.eg, L.rg, M.gen, coef, stv, tbuf, lane);
+  else apply_map_warp<A>(L.ez, L.rz, M.zero, coef, stv, tbuf, lane);
+  __syncwarp();
+}
+
+/* The x = 0 / y = 0 / x = y forms are assembled in FP64 by the mixed form:
+   there L1..L3 vanish identically (kernels.c:117-177) and must come out
+   as exact differences of the FP64 per-site and per-x terms. */
+__device__ __forceinline__ bool fp64_assembly(const double *xv, const double *yv, int variant)
+{
+  const double xx = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
+  const double yy = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
+  const double d0 = xv[0] - yv[0], d1 = xv[1] - yv[1], d2 = xv[2] - yv[2], d3 = xv[3] - yv[3];
+  const double dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
+  (void)variant;
+  return xx < 1E-28 || yy < 1E-28 || dd < 1E-28;
+}
+
+/* Phase A for the warp's 32 pairs: records into shared memory, the mixed
+   form routing up to kSlots64 lanes to FP64 records */
+template <typename SI, typename S>
+__device__ __forceinline__ void warp_phase_a(const DevTables &T, SmemLayout<S> &L, bool active,
+                                             const double *xv, const double *yv, const SI *colx,
+                                             const double *col64, int variant, int lane,
+                                             int &status)
+{
+  int kind = K_NONE, tag = 0;
+  status = 0;
+  bool fb = false;
+  if (NSlots<S>::v > 0) fb = active && fp64_assembly(xv, yv, variant);
+  const unsigned ball = __ballot_sync(0xffffffffu, fb);
+  const int slot = __popc(ball & ((1u << lane) - 1u));
+  if (fb && slot >= NSlots<S>::v) fb = false;
+  if (active) {
+    Sink sk;
+    if (NSlots<S>::v == 0) {
+      sk.f = nullptr;
+      sk.d = reinterpret_cast<double *>(L.w.rec) + lane * REC;
+    } else if (fb) {
+      sk.f = nullptr;
+      sk.d = L.w.rec64 + slot * REC;
+      tag = (1 << 8) | (slot << 9);
+    } else {
+      sk.f = reinterpret_cast<float *>(L.w.rec) + lane * REC;
+      sk.d = nullptr;
+    }
+    kind = phase_a<SI>(T, xv, yv, sk, status, colx, col64);
+  }
+  L.w.kind[lane] = kind | tag;
+  __syncwarp();
+}
+
+/* pair q of the warp: assemble in its precision; returns false for a zero
+   kernel.  On return tbuf64 says which buffer holds the components. */
+template <typename S>
+__device__ __forceinline__ bool assemble_pair(const SmemLayout<S> &L, const DevMaps &M, int q,
+                                              int lane, bool &perm, bool &tbuf64)
+{
+  const int code = L.w.kind[q];
+  const int kind = code & 0xff;
   perm = (kind == K_Y0PERM);
+  tbuf64 = (NSlots<S>::v == 0) || (code & (1 << 8));
   if (kind == K_NONE) return false;
-  const double *R = L.w.rec + q * REC;
-  if (kind == K_GEN) stv_generic(R, L.w.stv, lane);
-  else if (kind == K_X0) stv_x0(R, L.w.stv, lane);
-  else stv_y0(R, L.w.stv, lane);
-  __syncwarp();
-  if (kind == K_GEN) apply_map_warp(L.eg, L.rg, M.gen, L.coef, L.w.stv, L.w.tbuf, lane);
-  else apply_map_warp(L.ez, L.rz, M.zero, L.coef, L.w.stv, L.w.tbuf, lane);
-  __syncwarp();
+  if (tbuf64) {
+    const double *R = (NSlots<S>::v == 0) ? reinterpret_cast<const double *>(L.w.rec) + q * REC
+                                          : L.w.rec64 + (code >> 9) * REC;
+    assemble<double>(L, M, kind, R, L.w.stvd, L.w.tbufd, L.coefd, lane);
+  } else {
+    const float *R = reinterpret_cast<const float *>(L.w.rec) + q * REC;
+    assemble<float>(L, M, kind, R, reinterpret_cast<float *>(L.w.stvd),
+                    reinterpret_cast<float *>(L.w.tbufd), L.coeff, lane);
+  }
   return true;
 }
 
-/* Batched L0: out[i][384] */
-__global__ void __launch_bounds__(128) l0_fp64_kernel(DevTables T, DevMaps M, L0Args A, int wpb)
+template <typename S>
+__device__ __forceinline__ double kcomp(const SmemLayout<S> &L, bool t64, bool perm, int i)
 {
-  SmemLayout L = carve(wpb, M);
-  if ((threadIdx.x & 31) == 0) { L.w.stv[200] = 0.0; L.w.stv[201] = 0.0; }
-  load_maps(M, L.coef, L.eg, L.ez, L.rg, L.rz);
+  const int j = perm ? mulam(i) : i;
+  const double v = t64 ? L.w.tbufd[j] : (double)reinterpret_cast<const float *>(L.w.tbufd)[j];
+  return perm ? -v : v;
+}
+
+/* Batched L0: out[i][384] */
+template <typename SI, typename S>
+__global__ void __launch_bounds__(128) l0_kernel(DevTables T, DevMaps M, L0Args A, int wpb)
+{
+  SmemLayout<S> L = carve<S>(wpb);
+  block_prologue<S>(M, L);
   const int lane = threadIdx.x & 31;
   const size_t tile = (size_t)wpb * 32;
   for (size_t base = (size_t)blockIdx.x * tile; base < A.n; base += (size_t)gridDim.x * tile) {
     const size_t wbase = base + (threadIdx.x & ~31);
     const size_t p = wbase + lane;
-    int kind = K_NONE, status = 0;
-    if (p < A.n) {
-      double xv[4], yv[4];
+    const bool active = p < A.n;
+    double xv[4] = {0, 0, 0, 0}, yv[4] = {0, 0, 0, 0};
+    if (active)
       for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * p + m]; yv[m] = A.y[4 * p + m]; }
-      kind = phase_a(T, xv, yv, L.w.rec + lane * REC, status);
-      if (A.status) A.status[p] = (uint8_t)status;
-    }
-    L.w.kind[lane] = kind;
-    __syncwarp();
+    int status;
+    warp_phase_a<SI, S>(T, L, active, xv, yv, (const SI *)nullptr, (const double *)nullptr,
+                        A.variant, lane, status);
+    if (active && A.status) A.status[p] = (uint8_t)status;
     const int nq = (int)min((size_t)32, A.n > wbase ? A.n - wbase : (size_t)0);
     for (int q = 0; q < nq; q++) {
-      bool perm;
-      const bool live = assemble_pair(L, M, q, lane, perm);
+      bool perm, t64;
+      const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
       double *o = A.out + (wbase + q) * 384;
 #pragma unroll
       for (int r = 0; r < 12; r++) {
         const int i = r * 32 + lane;
-        o[i] = live ? (perm ? -L.w.tbuf[mulam(i)] : L.w.tbuf[i]) : 0.0;
+        o[i] = live ? kcomp<S>(L, t64, perm, i) : 0.0;
       }
       __syncwarp();
     }
@@ -1346,51 +1520,95 @@ __device__ __forceinline__ void kadd(double &s, double &c, double v)
   s = t;
 }
 
+/* float value of an FP64 input by integer bit manipulation, rounded to
+   nearest (ties away from zero; normal range; zero and underflow give zero),
+   so the mixed form does not spend FP64-pipe conversions on Pi */
+__device__ __forceinline__ float d2f_round(double v)
+{
+  const int hi = __double2hiint(v);
+  const unsigned lo = (unsigned)__double2loint(v);
+  const int e = ((hi >> 20) & 0x7ff) - 1023 + 127;
+  const unsigned sign = (unsigned)hi & 0x80000000u;
+  const unsigned mag = (((unsigned)e << 23) | (((unsigned)hi & 0xfffffu) << 3) | (lo >> 29)) +
+                       ((lo >> 28) & 1u);
+  const unsigned bits = e <= 0 ? sign : (e >= 255 ? (sign | 0x7f800000u) : (sign | mag));
+  return __uint_as_float(bits);
+}
+
+/* sum_i K_i Pi_i of one pair, lane-partial: FP64 when the pair was assembled
+   in FP64, else float products with the float per-site / per-x terms */
+template <typename S>
+__device__ __forceinline__ double contract(const SmemLayout<S> &L, bool live, bool perm, bool t64,
+                                           const double *pi, const double *ky, const double *bx,
+                                           const float *ky32, const float *bx32, int lane)
+{
+  if (t64 || !live) {
+    double acc = 0.0;
+#pragma unroll
+    for (int r = 0; r < 12; r++) {
+      const int i = r * 32 + lane;
+      double kv = live ? kcomp<S>(L, true, perm, i) : 0.0;
+      if (ky) kv += __ldg(ky + i);
+      if (bx) kv += __ldg(bx + i);
+      acc = fma(kv, __ldg(pi + i), acc);
+    }
+    return acc;
+  }
+  const float *tb = reinterpret_cast<const float *>(L.w.tbufd);
+  float acc = 0.0f;
+#pragma unroll
+  for (int r = 0; r < 12; r++) {
+    const int i = r * 32 + lane;
+    float kv = perm ? -tb[mulam(i)] : tb[i];
+    if (ky32) kv += __ldg(ky32 + i);
+    if (bx32) kv += __ldg(bx32 + i);
+    acc = fmaf(kv, d2f_round(__ldg(pi + i)), acc);
+  }
+  return (double)acc;
+}
+
+template <typename S> __device__ __forceinline__ const S *column_of(const LatticeArgs &A);
+template <> __device__ __forceinline__ const double *column_of<double>(const LatticeArgs &A) { return A.col; }
+template <> __device__ __forceinline__ const float *column_of<float>(const LatticeArgs &A) { return A.col32; }
+
 /* Fused lattice integrand: block (tile, k) sums pairs (x_k, y_n), n in the
    tile; writes partial[k][tile] = (sum, compensation). */
-__global__ void __launch_bounds__(128) lattice_fp64_kernel(DevTables T, DevMaps M, LatticeArgs A,
-                                                           int wpb)
+template <typename SI, typename S>
+__global__ void __launch_bounds__(128) lattice_kernel(DevTables T, DevMaps M, LatticeArgs A, int wpb)
 {
-  SmemLayout L = carve(wpb, M);
-  if ((threadIdx.x & 31) == 0) { L.w.stv[200] = 0.0; L.w.stv[201] = 0.0; }
-  load_maps(M, L.coef, L.eg, L.ez, L.rg, L.rz);
+  SmemLayout<S> L = carve<S>(wpb);
+  block_prologue<S>(M, L);
   __shared__ double red_s[8], red_c[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const size_t tile = (size_t)wpb * 32;
   const size_t nunits = A.nx * (size_t)A.tiles;
+  const SI *col = column_of<SI>(A);
+  const bool f32 = NSlots<S>::v > 0;
   for (size_t u = blockIdx.x; u < nunits; u += gridDim.x) {
     const size_t k = u / A.tiles, t = u % A.tiles;
     const size_t wbase = t * tile + (size_t)warp * 32;
     const size_t n = wbase + lane;
-    double xv[4];
+    double xv[4], yv[4] = {0, 0, 0, 0};
     for (int m = 0; m < 4; m++) xv[m] = A.x[4 * k + m];
-    int kind = K_NONE, status = 0;
-    if (n < A.ny) {
-      double yv[4];
+    const bool active = n < A.ny;
+    if (active)
       for (int m = 0; m < 4; m++) yv[m] = A.y[4 * n + m];
-      const double *colx = A.col ? A.col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
-      kind = phase_a(T, xv, yv, L.w.rec + lane * REC, status, colx);
-    }
-    L.w.kind[lane] = kind;
-    __syncwarp();
+    const SI *colx = col ? col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
+    const double *c64 = A.col ? A.col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
+    int status;
+    warp_phase_a<SI, S>(T, L, active, xv, yv, colx, c64, A.variant, lane, status);
     double s = 0.0, c = 0.0;
     const int nq = (int)min((size_t)32, A.ny > wbase ? A.ny - wbase : (size_t)0);
     for (int q = 0; q < nq; q++) {
-      bool perm;
-      const bool live = assemble_pair(L, M, q, lane, perm);
+      bool perm, t64;
+      const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
       const size_t nn = wbase + q;
       const double *pi = A.pi + (k * A.ny + nn) * 384;
       const double *ky = A.Ky ? A.Ky + nn * 384 : nullptr;
       const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
-      double acc = 0.0;
-#pragma unroll
-      for (int r = 0; r < 12; r++) {
-        const int i = r * 32 + lane;
-        double kv = live ? (perm ? -L.w.tbuf[mulam(i)] : L.w.tbuf[i]) : 0.0;
-        if (ky) kv += __ldg(ky + i);
-        if (bx) kv += __ldg(bx + i);
-        acc = fma(kv, __ldg(pi + i), acc);
-      }
+      const float *ky32 = (f32 && A.Ky32) ? A.Ky32 + nn * 384 : nullptr;
+      const float *bx32 = (f32 && A.Bx32) ? A.Bx32 + k * 384 : nullptr;
+      double acc = contract<S>(L, live, perm, t64, pi, ky, bx, ky32, bx32, lane);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
       kadd(s, c, acc);
@@ -1478,23 +1696,69 @@ static int num_sms()
   return n;
 }
 
+/* persistent grid: resident blocks per SM from the occupancy calculator,
+   capped at 3 for the FP64 kernels (measured: a fourth 2-warp block per SM
+   slows them, the FP64 pipe is already saturated and the extra shared memory
+   comes out of L1, which holds the x columns) and 4 for the float ones */
+static size_t grid_blocks(const void *fn, int wpb, size_t smem, size_t scalar_bytes)
+{
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int cap = scalar_bytes == 8 ? 3 : 4;
+  return (size_t)num_sms() * (size_t)min(per_sm, cap);
+}
+
 static cudaError_t prep_kernel_smem(const void *fn, size_t bytes)
 {
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a,
-                           const LaunchCfg &cfg, cudaStream_t s)
+template <typename SI, typename S>
+static cudaError_t launch_l0_t(const DevTables &T, const DevMaps &M, const L0Args &a,
+                               const LaunchCfg &cfg, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
   const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
-  const size_t smem = smem_bytes_l0(wpb);
-  cudaError_t e = prep_kernel_smem((const void *)l0_fp64_kernel, smem);
+  const size_t smem = smem_bytes<S>(wpb);
+  cudaError_t e = prep_kernel_smem((const void *)l0_kernel<SI, S>, smem);
   if (e != cudaSuccess) return e;
   const size_t tiles = (a.n + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32);
-  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : (size_t)num_sms() * 2;
+  const size_t blocks0 = grid_blocks((const void *)l0_kernel<SI, S>, wpb, smem, sizeof(S));
+  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : blocks0;
   if (blocks > tiles) blocks = tiles;
-  l0_fp64_kernel<<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
+  l0_kernel<SI, S><<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a,
+                           const LaunchCfg &cfg, cudaStream_t s)
+{
+  return launch_l0_t<double, double>(T, M, a, cfg, s);
+}
+
+cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &a,
+                            const LaunchCfg &cfg, cudaStream_t s)
+{
+  return launch_l0_t<float, float>(T, M, a, cfg, s);
+}
+
+template <typename SI, typename S>
+static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                    const LaunchCfg &cfg, cudaStream_t s)
+{
+  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
+  const size_t smem = smem_bytes<S>(wpb);
+  cudaError_t e = prep_kernel_smem((const void *)lattice_kernel<SI, S>, smem);
+  if (e != cudaSuccess) return e;
+  const size_t units = a.nx * (size_t)a.tiles;
+  if (units == 0) return cudaSuccess;
+  const size_t blocks0 = grid_blocks((const void *)lattice_kernel<SI, S>, wpb, smem, sizeof(S));
+  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : blocks0;
+  if (blocks > units) blocks = units;
+  lattice_kernel<SI, S><<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
   g_launches++;
   return cudaGetLastError();
 }
@@ -1502,15 +1766,26 @@ cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a
 cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                 const LaunchCfg &cfg, cudaStream_t s)
 {
-  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
-  const size_t smem = smem_bytes_l0(wpb);
-  cudaError_t e = prep_kernel_smem((const void *)lattice_fp64_kernel, smem);
-  if (e != cudaSuccess) return e;
-  const size_t units = a.nx * (size_t)a.tiles;
-  if (units == 0) return cudaSuccess;
-  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : (size_t)num_sms() * 3;
-  if (blocks > units) blocks = units;
-  lattice_fp64_kernel<<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
+  return launch_lattice_t<double, double>(T, M, a, cfg, s);
+}
+
+cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                 const LaunchCfg &cfg, cudaStream_t s, int split)
+{
+  /* split 0: float interpolation, float assembly except the FP64-routed
+     pairs; 2: FP64 interpolation, same assembly (diagnostic) */
+  if (split == 2) return launch_lattice_t<double, float>(T, M, a, cfg, s);
+  return launch_lattice_t<float, float>(T, M, a, cfg, s);
+}
+
+template <typename S>
+static cudaError_t launch_build_columns_t(const DevTables &T, const double *xs, size_t nx, S *col,
+                                          cudaStream_t s)
+{
+  const size_t tot = nx * (size_t)T.nstpy * T.NK;
+  if (tot == 0) return cudaSuccess;
+  const size_t b = min((tot + 127) / 128, (size_t)num_sms() * 16);
+  build_columns_kernel<S><<<(unsigned)b, 128, 0, s>>>(T, xs, nx, col);
   g_launches++;
   return cudaGetLastError();
 }
@@ -1518,10 +1793,26 @@ cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const Latt
 cudaError_t launch_build_columns(const DevTables &T, const double *xs, size_t nx, double *col,
                                  cudaStream_t s)
 {
-  const size_t tot = nx * (size_t)T.nstpy * T.NK;
-  if (tot == 0) return cudaSuccess;
-  const size_t b = min((tot + 127) / 128, (size_t)num_sms() * 16);
-  build_columns_kernel<<<(unsigned)b, 128, 0, s>>>(T, xs, nx, col);
+  return launch_build_columns_t<double>(T, xs, nx, col, s);
+}
+
+cudaError_t launch_build_columns32(const DevTables &T, const double *xs, size_t nx, float *col,
+                                   cudaStream_t s)
+{
+  return launch_build_columns_t<float>(T, xs, nx, col, s);
+}
+
+__global__ void to_float_kernel(const double *in, float *out, size_t n)
+{
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+cudaError_t launch_to_float(const double *in, float *out, size_t n, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  const size_t b = min((n + 255) / 256, (size_t)num_sms() * 8);
+  to_float_kernel<<<(unsigned)b, 256, 0, s>>>(in, out, n);
   g_launches++;
   return cudaGetLastError();
 }

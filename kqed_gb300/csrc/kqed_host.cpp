@@ -144,6 +144,7 @@ struct Ctx {
   DevTables T{};
   DevMaps M{};
   LaunchCfg cfg{2, 0};
+  int mixed_split = 0;
   std::vector<void *> allocs;
 };
 
@@ -153,7 +154,7 @@ struct ThreadStage {
   cudaStream_t stream = nullptr, copy_stream = nullptr;
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double *h_pin = nullptr;   /* 8 + 384 doubles */
-  Scratch d_io, d_tmp, d_aux, d_aux2, d_col;
+  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32;
   ~ThreadStage() { reset(); }
   void reset()
   {
@@ -166,7 +167,7 @@ struct ThreadStage {
     }
     copy_stream = nullptr;
     if (h_pin) cudaFreeHost(h_pin);
-    d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release(); d_col.release();
+    d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release(); d_col.release(); d_col32.release();
     stream = nullptr;
     h_pin = nullptr;
     owner = nullptr;
@@ -411,8 +412,14 @@ static int setup_device(struct Grid_coeffs *G, Ctx *c)
   T.TX = (const double *)dev_upload(c, tx.data(), sizeof(double) * tx.size());
   T.TY = (const double *)dev_upload(c, ty.data(), sizeof(double) * ty.size());
   T.node = (const double *)dev_upload(c, node.data(), sizeof(double) * node.size());
+  {
+    std::vector<float> node32(node.size());
+    for (size_t i = 0; i < node.size(); i++) node32[i] = (float)node[i];
+    T.node32 = (const float *)dev_upload(c, node32.data(), sizeof(float) * node32.size());
+  }
   T.nfx = (const int *)dev_upload(c, G->nfx, sizeof(int) * G->nstpx);
-  if (!T.XX || !T.YY || !T.TX || !T.TY || !T.node || !T.nfx) return fail("device table upload failed");
+  if (!T.XX || !T.YY || !T.TX || !T.TY || !T.node || !T.node32 || !T.nfx)
+    return fail("device table upload failed");
   T.nstpx = G->nstpx; T.nstpy = G->nstpy; T.ny_tay = G->NY_tay; T.nx_tay = G->NX_tay; T.NK = NK;
   T.ystp = G->ystp;
   /* map schedules */
@@ -429,6 +436,8 @@ static int setup_device(struct Grid_coeffs *G, Ctx *c)
   const char *blk = getenv("KQED_BLOCKS");
   if (wpb) c->cfg.warps_per_block = std::max(1, std::min(4, atoi(wpb)));
   if (blk) c->cfg.blocks = std::max(0, atoi(blk));
+  const char *sp = getenv("KQED_MIXED_SPLIT");
+  if (sp) c->mixed_split = std::max(0, std::min(2, atoi(sp)));
   return 0;
 }
 
@@ -519,18 +528,22 @@ extern "C" int initialize_QED_kernel_temps(struct QED_kernel_temps *t) { return 
 static int check_variant_precision(int variant, int precision)
 {
   if (variant < 0 || variant > 3) return fail("variant %d not in 0..3", variant);
-  if (precision != KQED_FP64) return fail("precision mode %d is not available in this build", precision);
+  if (precision != KQED_FP64 && precision != KQED_FP32_MIXED)
+    return fail("precision mode %d is not available in this build", precision);
   return 0;
 }
 
 /* L0 over n pairs on the device */
+static thread_local int tl_precision = KQED_FP64;
+
 static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *dout,
-                  uint8_t *dstatus, cudaStream_t s, bool timed = true)
+                  uint8_t *dstatus, cudaStream_t s, bool timed = true, int variant = 0)
 {
-  L0Args a{dx, dy, n, dout, dstatus};
+  L0Args a{dx, dy, n, dout, dstatus, variant};
   TimedLaunch tl{nullptr, nullptr};
   if (timed) prof_begin(s, tl);
-  CUDA_OK(launch_l0_fp64(c->T, c->M, a, c->cfg, s));
+  if (tl_precision == KQED_FP32_MIXED && timed) CUDA_OK(launch_l0_mixed(c->T, c->M, a, c->cfg, s));
+  else CUDA_OK(launch_l0_fp64(c->T, c->M, a, c->cfg, s));
   prof_end(s, tl);
   return 0;
 }
@@ -539,7 +552,7 @@ static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *
 static int run_variant(Ctx *c, int variant, const double *dx, const double *dy, size_t n,
                        double *dout, uint8_t *dstatus, cudaStream_t s, ThreadStage &st)
 {
-  if (run_l0(c, dx, dy, n, dout, dstatus, s)) return 1;
+  if (run_l0(c, dx, dy, n, dout, dstatus, s, true, variant)) return 1;
   if (variant == 0) return 0;
   double *tmp = st.d_tmp.get(n * 384);
   double *zero = st.d_aux.get(n * 4);
@@ -588,7 +601,10 @@ extern "C" int kqed_kernel_batch_dev(const struct QED_kernel_temps *t, int varia
   if (!c) return fail("tables not initialised");
   if (check_variant_precision(variant, precision)) return 1;
   if (n && (!d_x || !d_y || !d_kerv)) return fail("null buffer");
-  return run_variant(c, variant, d_x, d_y, n, d_kerv, d_status, (cudaStream_t)stream, stage_for(c));
+  tl_precision = precision;
+  const int rc = run_variant(c, variant, d_x, d_y, n, d_kerv, d_status, (cudaStream_t)stream, stage_for(c));
+  tl_precision = KQED_FP64;
+  return rc;
 }
 
 extern "C" int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, size_t n,
@@ -608,7 +624,10 @@ extern "C" int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, 
   uint8_t *dst = status ? reinterpret_cast<uint8_t *>(io + n * (8 + 384)) : nullptr;
   CUDA_OK(cudaMemcpyAsync(dx, x, n * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
   CUDA_OK(cudaMemcpyAsync(dy, y, n * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
-  if (run_variant(c, variant, dx, dy, n, dk, dst, st.stream, st)) return 1;
+  tl_precision = precision;
+  const int rc = run_variant(c, variant, dx, dy, n, dk, dst, st.stream, st);
+  tl_precision = KQED_FP64;
+  if (rc) return 1;
   CUDA_OK(cudaMemcpyAsync(kerv, dk, n * 384 * sizeof(double), cudaMemcpyDeviceToHost, st.stream));
   if (status) CUDA_OK(cudaMemcpyAsync(status, dst, n, cudaMemcpyDeviceToHost, st.stream));
   CUDA_OK(cudaStreamSynchronize(st.stream));
@@ -723,21 +742,49 @@ struct LatticeRun {
   const double *d_x, *d_y;
   size_t nx, ny;
   double *Ky, *Bx, *partial, *col;
-  int tiles;
+  float *Ky32, *Bx32, *col32;
+  int tiles, precision, variant;
 };
 
 static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, size_t ny,
-                           const double *d_y, cudaStream_t s, ThreadStage &st, LatticeRun &R)
+                           const double *d_y, cudaStream_t s, ThreadStage &st, LatticeRun &R,
+                           int precision)
 {
-  R.c = c; R.d_x = d_x; R.d_y = d_y; R.nx = nx; R.ny = ny;
+  R.c = c; R.d_x = d_x; R.d_y = d_y; R.nx = nx; R.ny = ny; R.precision = precision;
+  R.variant = variant;
+  R.Ky32 = R.Bx32 = R.col32 = nullptr;
+  R.col = nullptr;
   if (lattice_terms(c, variant, d_x, nx, d_y, ny, &R.Ky, &R.Bx, s, st)) return 1;
   const int wpb = c->cfg.warps_per_block;
   R.tiles = (int)((ny + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32));
   R.partial = st.d_tmp.get(nx * (size_t)std::max(R.tiles, 1) * 2);
   if (!R.partial) return fail("out of device memory for partial sums");
-  R.col = st.d_col.get(nx * (size_t)c->T.nstpy * c->T.NK * kRow);
+  const size_t ncol = nx * (size_t)c->T.nstpy * c->T.NK * kRow;
+  const bool mixed = precision == KQED_FP32_MIXED;
+  const int split = mixed ? c->mixed_split : -1;
+  /* FP64 columns always (the FP64 form, and the float form's pairs near
+     cb = +-1); float columns for the float interpolation of the mixed form */
+  R.col = st.d_col.get(ncol);
   if (!R.col) return fail("out of device memory for x-column tables");
   CUDA_OK(launch_build_columns(c->T, d_x, nx, R.col, s));
+  if (mixed) {
+    const bool col32 = split != 2;
+    const size_t n32 = (col32 ? ncol : 0) + (R.Ky ? (ny + nx) * 384 : 0);
+    float *b32 = reinterpret_cast<float *>(st.d_col32.get(n32 / 2 + 2));
+    if (!b32) return fail("out of device memory for float tables");
+    if (col32) {
+      R.col32 = b32;
+      b32 += ncol;
+      CUDA_OK(launch_build_columns32(c->T, d_x, nx, R.col32, s));
+    }
+    if (R.Ky) {
+      /* the FP64-evaluated per-site / per-x terms, as float */
+      R.Ky32 = b32;
+      R.Bx32 = R.Ky32 + ny * 384;
+      CUDA_OK(launch_to_float(R.Ky, R.Ky32, ny * 384, s));
+      CUDA_OK(launch_to_float(R.Bx, R.Bx32, nx * 384, s));
+    }
+  }
   return 0;
 }
 
@@ -746,11 +793,17 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
                           cudaStream_t s)
 {
   const size_t per_x = (size_t)R.c->T.nstpy * R.c->T.NK * kRow;
-  LatticeArgs a{R.d_x + 4 * x0, R.d_y, nxc, R.ny, d_pi, R.Ky, R.Bx ? R.Bx + 384 * x0 : nullptr,
-                R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1), R.tiles, R.col + per_x * x0};
+  const bool mixed = R.precision == KQED_FP32_MIXED;
+  LatticeArgs a{R.d_x + 4 * x0, R.d_y, nxc, R.ny, d_pi,
+                R.Ky, R.Bx ? R.Bx + 384 * x0 : nullptr,
+                R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1), R.tiles,
+                R.col ? R.col + per_x * x0 : nullptr,
+                R.Ky32, R.Bx32 ? R.Bx32 + 384 * x0 : nullptr,
+                R.col32 ? R.col32 + per_x * x0 : nullptr, R.variant};
   TimedLaunch tl;
   prof_begin(s, tl);
-  CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, R.c->cfg, s));
+  if (mixed) CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s, R.c->mixed_split));
+  else CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, R.c->cfg, s));
   prof_end(s, tl);
   return 0;
 }
@@ -767,7 +820,7 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
   cudaStream_t s = (cudaStream_t)stream;
   ThreadStage &st = stage_for(c);
   LatticeRun R;
-  if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R)) return 1;
+  if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R, precision)) return 1;
   if (lattice_launch(R, 0, nx, d_pi, s)) return 1;
   CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, d_sums, s));
   return 0;
@@ -799,7 +852,7 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
   CUDA_OK(cudaMemcpyAsync(dx, x, nx * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
   CUDA_OK(cudaMemcpyAsync(dy, y, ny * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
   LatticeRun R;
-  if (lattice_prepare(c, variant, nx, dx, ny, dy, s, st, R)) return 1;
+  if (lattice_prepare(c, variant, nx, dx, ny, dy, s, st, R, precision)) return 1;
   if (!st.ev_copied[0]) {
     for (int i = 0; i < 2; i++) {
       CUDA_OK(cudaEventCreateWithFlags(&st.ev_copied[i], cudaEventDisableTiming));

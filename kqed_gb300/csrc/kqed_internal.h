@@ -49,6 +49,7 @@ struct DevTables {
   const double *TX;      /* [23][ny_tay] TAYLORX */
   const double *TY;      /* [14][nx_tay] TAYLORY */
   const double *node;
+  const float *node32;   /* the same table rounded to float (mixed-precision form) */
   const int *nfx;
   int nstpx, nstpy, ny_tay, nx_tay, NK;
   double ystp;
@@ -82,6 +83,7 @@ struct L0Args {
   size_t n;
   double *out;          /* [n][384] or NULL */
   uint8_t *status;      /* [n] or NULL */
+  int variant;          /* L0..L3 the terms belong to (mixed form: FP64 zone) */
 };
 
 struct LatticeArgs {
@@ -94,6 +96,8 @@ struct LatticeArgs {
   double *partial;      /* [nx][tiles][2]  (sum, compensation) */
   int tiles;            /* y tiles per x */
   const double *col;    /* per-x column tables [nx][nstpy][NK][kRow] or NULL */
+  const float *Ky32, *Bx32, *col32;   /* the same in float, for the mixed form */
+  int variant;
 };
 
 int upload_map_constants();
@@ -103,6 +107,13 @@ cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const Latt
                                 const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_build_columns(const DevTables &T, const double *xs, size_t nx, double *col,
                                  cudaStream_t s);
+cudaError_t launch_build_columns32(const DevTables &T, const double *xs, size_t nx, float *col,
+                                   cudaStream_t s);
+cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &a,
+                            const LaunchCfg &cfg, cudaStream_t s);
+cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                 const LaunchCfg &cfg, cudaStream_t s, int split = 0);
+cudaError_t launch_to_float(const double *in, float *out, size_t n, cudaStream_t s);
 cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,
                                    cudaStream_t s);
 cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStream_t s);

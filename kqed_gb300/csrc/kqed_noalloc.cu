@@ -76,7 +76,7 @@ int scratch_on_current_device(double **out)
 int l0(const kqed::DevTables &T, const kqed::DevMaps &M, const kqed::LaunchCfg &cfg,
        const double *dx, const double *dy, size_t n, double *out, cudaStream_t s)
 {
-  kqed::L0Args a{dx, dy, n, out, nullptr};
+  kqed::L0Args a{dx, dy, n, out, nullptr, 0};
   return kqed::launch_l0_fp64(T, M, a, cfg, s) != cudaSuccess;
 }
 
@@ -141,7 +141,8 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
     }
     if (bad) return kqed::set_error("kqed_lattice_sum_noalloc: kernel-term launch failed");
   }
-  kqed::LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, (int)tiles, nullptr};
+  kqed::LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, (int)tiles, nullptr,
+                      nullptr, nullptr, nullptr, variant};
   if (kqed::launch_lattice_fp64(T, M, a, cfg, s) != cudaSuccess ||
       kqed::launch_reduce_partials(partial, nx, (int)tiles, d_sums, s) != cudaSuccess)
     return kqed::set_error("kqed_lattice_sum_noalloc: lattice kernel launch failed");

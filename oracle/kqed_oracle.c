@@ -1194,6 +1194,24 @@ int oracle_contract(int variant, long n, const double *x, const double *y, const
   return 0;
 }
 
+/* the 200 STV components of generic pairs (zero vector for other branches) */
+int oracle_stv(long n, const double *x, const double *y, double *out)
+{
+  if (!G_ready) return 1;
+  for (long i = 0; i < n; i++) {
+    double *o = out + 200 * i;
+    memset(o, 0, 200 * sizeof(double));
+    inv_t I;
+    const double *xv = x + 4 * i, *yv = y + 4 * i;
+    if (is_zero(xv) || is_zero(yv)) continue;
+    invariants(xv, yv, &I);
+    if (build_S(xv, yv, &I, o + 0, o + 4) || build_T(xv, yv, &I, o + 8, o + 72) ||
+        build_V(xv, yv, &I, o + 136))
+      memset(o, 0, 200 * sizeof(double));
+  }
+  return 0;
+}
+
 int oracle_branch(long n, const double *x, const double *y, int *code)
 {
   if (!G_ready) return 1;

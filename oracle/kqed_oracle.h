@@ -33,6 +33,9 @@ int oracle_kernel(int variant, long n, const double *x, const double *y, double 
 int oracle_contract(int variant, long n, const double *x, const double *y, const double *pi,
                     double *dots, int nthreads);
 
+/* out[n][200]: the STV building blocks (Sx, Sy, Tx, Ty, V) of generic pairs */
+int oracle_stv(long n, const double *x, const double *y, double *out);
+
 /* Branch taken by L0(x,y): 0 zero (x=y=0), 1 x=0, 2 y=0, 3 x=y, 4 generic,
    5 generic with |x| below the grid (Taylor in x); +8 if the x<->(x-y) swap is
    active; 16 if the kernel is zero because an argument is outside the grid. */
