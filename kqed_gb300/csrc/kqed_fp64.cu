@@ -75,7 +75,8 @@ enum { alpha0dx_0p = 0, alpha0_1p, alpha3_0p, beta2_1p, alpha3_1p, alpha1_0p, be
 
 /* ------------------------------------------------------------ records */
 
-enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4 };
+/* K_SKIP: the pair is not handled in this round of its warp (mixed form) */
+enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4, K_SKIP = 5 };
 
 /* generic record (doubles) */
 enum {
@@ -1112,9 +1113,10 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
     ws.xA = (S)w.xA; ws.xB = (S)w.xB; ws.xC1 = (S)w.xC1; ws.xC2 = (S)w.xC2; ws.lAx = (S)w.lAx;
     ws.yA = (S)w.yA; ws.yB = (S)w.yB; ws.yC1 = (S)w.yC1; ws.yC2 = (S)w.yC2; ws.lAy = (S)w.lAy;
     ws.dd = (S)w.dd;
-    /* the float form keeps FP64 for the Chebyshev sums near cb = +-1, where
-       their derivatives lose digits in float */
-    const bool cb64 = sizeof(S) == 4 && fabs(I.cb) > 0.99;
+    /* the float form keeps FP64 for the Chebyshev sums of the pairs it
+       assembles in FP64 and near cb = +-1, where their derivatives lose
+       digits in float */
+    const bool cb64 = sizeof(S) == 4 && (R.d != nullptr || fabs(I.cb) > 0.99);
     if (cb64 && col64) {
       Wts<double> wd = w;
       interp_column<double>(col64 + (size_t)iy0 * NK * kRow, col64 + (size_t)iy1 * NK * kRow, Ktop,
@@ -1400,34 +1402,45 @@ __device__ __forceinline__ void assemble(const SmemLayout<S> &L, const DevMaps &
   __syncwarp();
 }
 
-/* The x = 0 / y = 0 / x = y forms are assembled in FP64 by the mixed form:
-   there L1..L3 vanish identically (kernels.c:117-177) and must come out
-   as exact differences of the FP64 per-site and per-x terms. */
-__device__ __forceinline__ bool fp64_assembly(const double *xv, const double *yv, int variant)
+/* Pairs the mixed form assembles in FP64:
+   - the x = 0 / y = 0 / x = y forms: there L1..L3 vanish identically
+     (kernels.c:117-177) and must come out as exact differences of the FP64
+     per-site and per-x terms;
+   - |x - y| < max(|x|, |y|) / 4: these take the x <-> (x-y) swap, whose
+     chain rule (1/|x-y| factors) makes the STV terms large and cancelling,
+     so float assembly would lose about log2(max(|x|,|y|)/|x-y|) bits on the
+     pairs that weigh most in a lattice sum. */
+__device__ __forceinline__ bool fp64_assembly(const double *xv, const double *yv)
 {
   const double xx = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
   const double yy = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
   const double d0 = xv[0] - yv[0], d1 = xv[1] - yv[1], d2 = xv[2] - yv[2], d3 = xv[3] - yv[3];
   const double dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
-  (void)variant;
-  return xx < 1E-28 || yy < 1E-28 || dd < 1E-28;
+  return xx < 1E-28 || yy < 1E-28 || dd < 1E-28 || 16.0 * dd < fmax(xx, yy);
 }
 
-/* Phase A for the warp's 32 pairs: records into shared memory, the mixed
-   form routing up to kSlots64 lanes to FP64 records */
+/* Phase A for the pending pairs of the warp: records into shared memory.
+   The mixed form routes pairs to its kSlots64 FP64 record slots; routed
+   pairs beyond the free slots are deferred to a later round of the warp
+   (return value true for this lane) and are K_SKIP in this one. */
 template <typename SI, typename S>
-__device__ __forceinline__ void warp_phase_a(const DevTables &T, SmemLayout<S> &L, bool active,
+__device__ __forceinline__ bool warp_phase_a(const DevTables &T, SmemLayout<S> &L, bool active,
                                              const double *xv, const double *yv, const SI *colx,
-                                             const double *col64, int variant, int lane,
-                                             int &status)
+                                             const double *col64, int lane, int &status)
 {
-  int kind = K_NONE, tag = 0;
+  /* lanes with no pending pair are K_SKIP, so a later round does not count
+     the per-site / per-x terms of the pairs finished before it again */
+  int kind = active ? K_NONE : K_SKIP, tag = 0;
   status = 0;
   bool fb = false;
-  if (NSlots<S>::v > 0) fb = active && fp64_assembly(xv, yv, variant);
+  if (NSlots<S>::v > 0) fb = active && fp64_assembly(xv, yv);
   const unsigned ball = __ballot_sync(0xffffffffu, fb);
   const int slot = __popc(ball & ((1u << lane) - 1u));
-  if (fb && slot >= NSlots<S>::v) fb = false;
+  const bool deferred = fb && slot >= NSlots<S>::v;
+  if (deferred) {
+    active = false;
+    kind = K_SKIP;
+  }
   if (active) {
     Sink sk;
     if (NSlots<S>::v == 0) {
@@ -1445,6 +1458,7 @@ __device__ __forceinline__ void warp_phase_a(const DevTables &T, SmemLayout<S> &
   }
   L.w.kind[lane] = kind | tag;
   __syncwarp();
+  return deferred;
 }
 
 /* pair q of the warp: assemble in its precision; returns false for a zero
@@ -1493,21 +1507,28 @@ __global__ void __launch_bounds__(128) l0_kernel(DevTables T, DevMaps M, L0Args 
     double xv[4] = {0, 0, 0, 0}, yv[4] = {0, 0, 0, 0};
     if (active)
       for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * p + m]; yv[m] = A.y[4 * p + m]; }
-    int status;
-    warp_phase_a<SI, S>(T, L, active, xv, yv, (const SI *)nullptr, (const double *)nullptr,
-                        A.variant, lane, status);
-    if (active && A.status) A.status[p] = (uint8_t)status;
     const int nq = (int)min((size_t)32, A.n > wbase ? A.n - wbase : (size_t)0);
-    for (int q = 0; q < nq; q++) {
-      bool perm, t64;
-      const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
-      double *o = A.out + (wbase + q) * 384;
+    bool pending = active;
+    for (;;) {
+      int status;
+      const bool deferred =
+          warp_phase_a<SI, S>(T, L, pending, xv, yv, (const SI *)nullptr, (const double *)nullptr,
+                              lane, status);
+      if (pending && !deferred && A.status) A.status[p] = (uint8_t)status;
+      for (int q = 0; q < nq; q++) {
+        if (L.w.kind[q] == K_SKIP) continue;
+        bool perm, t64;
+        const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
+        double *o = A.out + (wbase + q) * 384;
 #pragma unroll
-      for (int r = 0; r < 12; r++) {
-        const int i = r * 32 + lane;
-        o[i] = live ? kcomp<S>(L, t64, perm, i) : 0.0;
+        for (int r = 0; r < 12; r++) {
+          const int i = r * 32 + lane;
+          o[i] = live ? kcomp<S>(L, t64, perm, i) : 0.0;
+        }
+        __syncwarp();
       }
-      __syncwarp();
+      if (NSlots<S>::v == 0 || !__any_sync(0xffffffffu, deferred)) break;
+      pending = deferred;
     }
   }
 }
@@ -1595,24 +1616,31 @@ __global__ void __launch_bounds__(128) lattice_kernel(DevTables T, DevMaps M, La
       for (int m = 0; m < 4; m++) yv[m] = A.y[4 * n + m];
     const SI *colx = col ? col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
     const double *c64 = A.col ? A.col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
-    int status;
-    warp_phase_a<SI, S>(T, L, active, xv, yv, colx, c64, A.variant, lane, status);
     double s = 0.0, c = 0.0;
     const int nq = (int)min((size_t)32, A.ny > wbase ? A.ny - wbase : (size_t)0);
-    for (int q = 0; q < nq; q++) {
-      bool perm, t64;
-      const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
-      const size_t nn = wbase + q;
-      const double *pi = A.pi + (k * A.ny + nn) * 384;
-      const double *ky = A.Ky ? A.Ky + nn * 384 : nullptr;
-      const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
-      const float *ky32 = (f32 && A.Ky32) ? A.Ky32 + nn * 384 : nullptr;
-      const float *bx32 = (f32 && A.Bx32) ? A.Bx32 + k * 384 : nullptr;
-      double acc = contract<S>(L, live, perm, t64, pi, ky, bx, ky32, bx32, lane);
+    bool pending = active;
+    for (;;) {
+      int status;
+      const bool deferred =
+          warp_phase_a<SI, S>(T, L, pending, xv, yv, colx, c64, lane, status);
+      for (int q = 0; q < nq; q++) {
+        if (L.w.kind[q] == K_SKIP) continue;
+        bool perm, t64;
+        const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
+        const size_t nn = wbase + q;
+        const double *pi = A.pi + (k * A.ny + nn) * 384;
+        const double *ky = A.Ky ? A.Ky + nn * 384 : nullptr;
+        const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
+        const float *ky32 = (f32 && A.Ky32) ? A.Ky32 + nn * 384 : nullptr;
+        const float *bx32 = (f32 && A.Bx32) ? A.Bx32 + k * 384 : nullptr;
+        double acc = contract<S>(L, live, perm, t64, pi, ky, bx, ky32, bx32, lane);
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-      kadd(s, c, acc);
-      __syncwarp();
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        kadd(s, c, acc);
+        __syncwarp();
+      }
+      if (NSlots<S>::v == 0 || !__any_sync(0xffffffffu, deferred)) break;
+      pending = deferred;
     }
     if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
     __syncthreads();
