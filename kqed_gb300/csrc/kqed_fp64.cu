@@ -33,6 +33,8 @@
 
 #include <stdio.h>
 
+#include <algorithm>
+
 namespace kqed {
 
 std::atomic<uint64_t> g_launches{0};
@@ -75,8 +77,7 @@ enum { alpha0dx_0p = 0, alpha0_1p, alpha3_0p, beta2_1p, alpha3_1p, alpha1_0p, be
 
 /* ------------------------------------------------------------ records */
 
-/* K_SKIP: the pair is not handled in this round of its warp (mixed form) */
-enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4, K_SKIP = 5 };
+enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4 };
 
 /* generic record (doubles) */
 enum {
@@ -1040,7 +1041,7 @@ __device__ __forceinline__ bool is_zero4(const double *v)
    record, return the kind and status bits. */
 template <typename S>
 __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, const Sink &R,
-                       int &status, const S *colx = nullptr, const double *col64 = nullptr)
+                       int &status, const S *colx, const double *col64, bool f64pair)
 {
   status = 0;
   /* non-finite input: the reference's grid search would run off the tables;
@@ -1116,7 +1117,7 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
     /* the float form keeps FP64 for the Chebyshev sums of the pairs it
        assembles in FP64 and near cb = +-1, where their derivatives lose
        digits in float */
-    const bool cb64 = sizeof(S) == 4 && (R.d != nullptr || fabs(I.cb) > 0.99);
+    const bool cb64 = sizeof(S) == 4 && (f64pair || fabs(I.cb) > 0.99);
     if (cb64 && col64) {
       Wts<double> wd = w;
       interp_column<double>(col64 + (size_t)iy0 * NK * kRow, col64 + (size_t)iy1 * NK * kRow, Ktop,
@@ -1313,94 +1314,21 @@ __device__ __forceinline__ int mulam(int i)
 
 /* ------------------------------------------------------------ kernels */
 
-/* Per-warp shared memory.  Records of the warp's 32 pairs are stored in the
-   record type S of the fast assembly path; the mixed form (S = float) keeps
-   up to kSlots64 FP64 records for pairs it assembles in FP64.  The STV and
-   384-component buffers are sized for doubles and reused as floats. */
-constexpr int kSlots64 = 4;
-template <typename S> struct NSlots { static constexpr int v = 0; };
-template <> struct NSlots<float> { static constexpr int v = kSlots64; };
+/* Every batch of pairs runs as two kernels:
+     record kernels (thread per pair): classification, invariants,
+       interpolation, chnr and the swap chain rule -> one FP64 record of REC
+       values per pair in global memory, plus a code byte
+       (kind | FP64-assembly flag << 3 | status << 4);
+     assembly kernels (warp per pair): the STV components, the sparse
+       384 x 200 map and the stored kernel or its contraction with Pi.
+   The record work is long FP64 dependency chains and needs the whole register
+   file (255 per thread, 8 warps per SM); the assembly needs few registers,
+   and with many warps per SM its shared-memory and load latencies hide.  The
+   records cost 712 bytes of HBM traffic each way per pair, against 3 KB of Pi.
 
-template <typename S> __host__ __device__ constexpr size_t warp_smem_bytes()
-{
-  return 32 * REC * sizeof(S) + NSlots<S>::v * REC * sizeof(double) + (202 + 384) * sizeof(double) +
-         32 * sizeof(int);
-}
-
-constexpr size_t kSchedBytes = (size_t)(2 * 3072 + 2 * 384) * sizeof(uint16_t);
-
-template <typename S> static size_t smem_bytes(int wpb)
-{
-  return (size_t)wpb * warp_smem_bytes<S>() + 8 * sizeof(double) + 8 * sizeof(float) + kSchedBytes;
-}
-
-size_t smem_bytes_l0(int wpb) { return smem_bytes<double>(wpb); }
-
-template <typename S> struct WarpSmem {
-  S *rec;          /* [32][REC] */
-  double *rec64;   /* [kSlots64][REC] (mixed form) */
-  double *stvd;    /* [202] as doubles; [200] = 0 is the map's padding target */
-  double *tbufd;   /* [384] as doubles */
-  int *kind;       /* [32]: kind | fp64-assembly flag << 8 | slot << 9 */
-};
-
-template <typename S> struct SmemLayout {
-  double *coefd;
-  float *coeff;
-  uint16_t *eg, *ez, *rg, *rz;   /* map schedules */
-  WarpSmem<S> w;
-};
-
-template <typename S>
-__device__ __forceinline__ SmemLayout<S> carve(int wpb)
-{
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemLayout<S> L;
-  const int warp = threadIdx.x >> 5;
-  unsigned char *wb = smem_raw + (size_t)warp * warp_smem_bytes<S>();
-  L.w.stvd = reinterpret_cast<double *>(wb);
-  L.w.tbufd = L.w.stvd + 202;
-  L.w.rec64 = L.w.tbufd + 384;
-  L.w.rec = reinterpret_cast<S *>(L.w.rec64 + NSlots<S>::v * REC);
-  L.w.kind = reinterpret_cast<int *>(L.w.rec + 32 * REC);
-  unsigned char *after = smem_raw + (size_t)wpb * warp_smem_bytes<S>();
-  L.coefd = reinterpret_cast<double *>(after);
-  L.coeff = reinterpret_cast<float *>(L.coefd + 8);
-  L.eg = reinterpret_cast<uint16_t *>(L.coeff + 8);
-  L.ez = L.eg + 3072;
-  L.rg = L.ez + 3072;
-  L.rz = L.rg + 384;
-  return L;
-}
-
-template <typename S>
-__device__ __forceinline__ void block_prologue(const DevMaps &M, SmemLayout<S> &L)
-{
-  if (threadIdx.x < 8) {
-    const float c[8] = {-2.0f, -1.0f, -0.5f, 0.5f, 1.0f, 2.0f, 0.0f, 0.0f};
-    L.coefd[threadIdx.x] = (double)c[threadIdx.x];
-    L.coeff[threadIdx.x] = c[threadIdx.x];
-  }
-  for (int i = threadIdx.x; i < M.gen.total; i += blockDim.x) L.eg[i] = M.ent_gen[i];
-  for (int i = threadIdx.x; i < M.zero.total; i += blockDim.x) L.ez[i] = M.ent_zero[i];
-  for (int i = threadIdx.x; i < 384; i += blockDim.x) { L.rg[i] = M.row_gen[i]; L.rz[i] = M.row_zero[i]; }
-  __syncthreads();
-}
-
-/* assemble the 384 components of one pair into tbuf (type A) */
-template <typename A, typename S>
-__device__ __forceinline__ void assemble(const SmemLayout<S> &L, const DevMaps &M, int kind,
-                                         const A *R, A *stv, A *tbuf, const A *coef, int lane)
-{
-  if (lane == 0) { stv[200] = A(0); stv[201] = A(0); }
-  if (kind == K_GEN) stv_generic<A>(R, stv, lane);
-  else if (kind == K_X0) stv_x0<A>(R, stv, lane);
-  else stv_y0<A>(R, stv, lane);
-  __syncwarp();
-  if (kind == K_GEN) apply_map_warp<A>(L.eg, L.rg, M.gen, coef, stv, tbuf, lane);
-  else apply_map_warp<A>(L.ez, L.rz, M.zero, coef, stv, tbuf, lane);
-  __syncwarp();
-}
+   Pairs the mixed form assembles in FP64 (see fp64_assembly) are flagged by
+   the record kernel; the assembly kernel picks the precision per pair. */
+static_assert(REC == kRec, "record size");
 
 /* Pairs the mixed form assembles in FP64:
    - the x = 0 / y = 0 / x = y forms: there L1..L3 vanish identically
@@ -1419,118 +1347,127 @@ __device__ __forceinline__ bool fp64_assembly(const double *xv, const double *yv
   return xx < 1E-28 || yy < 1E-28 || dd < 1E-28 || 16.0 * dd < fmax(xx, yy);
 }
 
-/* Phase A for the pending pairs of the warp: records into shared memory.
-   The mixed form routes pairs to its kSlots64 FP64 record slots; routed
-   pairs beyond the free slots are deferred to a later round of the warp
-   (return value true for this lane) and are K_SKIP in this one. */
-template <typename SI, typename S>
-__device__ __forceinline__ bool warp_phase_a(const DevTables &T, SmemLayout<S> &L, bool active,
-                                             const double *xv, const double *yv, const SI *colx,
-                                             const double *col64, int lane, int &status)
+__device__ __forceinline__ uint8_t pair_code(int kind, bool f64, int status)
 {
-  /* lanes with no pending pair are K_SKIP, so a later round does not count
-     the per-site / per-x terms of the pairs finished before it again */
-  int kind = active ? K_NONE : K_SKIP, tag = 0;
-  status = 0;
-  bool fb = false;
-  if (NSlots<S>::v > 0) fb = active && fp64_assembly(xv, yv);
-  const unsigned ball = __ballot_sync(0xffffffffu, fb);
-  const int slot = __popc(ball & ((1u << lane) - 1u));
-  const bool deferred = fb && slot >= NSlots<S>::v;
-  if (deferred) {
-    active = false;
-    kind = K_SKIP;
-  }
-  if (active) {
+  return (uint8_t)(kind | (f64 ? 8 : 0) | (status << 4));
+}
+
+/* records of pairs p0 + r, r < np, of a batch (x[p], y[p]) */
+template <typename SI>
+__global__ void __launch_bounds__(64) l0_rec_kernel(DevTables T, L0Args A, size_t p0, size_t np,
+                                                    int mixed)
+{
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < np;
+       r += (size_t)gridDim.x * blockDim.x) {
+    const size_t p = p0 + r;
+    double xv[4], yv[4];
+    for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * p + m]; yv[m] = A.y[4 * p + m]; }
+    const bool f64 = mixed && fp64_assembly(xv, yv);
     Sink sk;
-    if (NSlots<S>::v == 0) {
-      sk.f = nullptr;
-      sk.d = reinterpret_cast<double *>(L.w.rec) + lane * REC;
-    } else if (fb) {
-      sk.f = nullptr;
-      sk.d = L.w.rec64 + slot * REC;
-      tag = (1 << 8) | (slot << 9);
-    } else {
-      sk.f = reinterpret_cast<float *>(L.w.rec) + lane * REC;
-      sk.d = nullptr;
-    }
-    kind = phase_a<SI>(T, xv, yv, sk, status, colx, col64);
+    sk.f = nullptr;
+    sk.d = A.rec + r * REC;
+    int status;
+    const int kind = phase_a<SI>(T, xv, yv, sk, status, (const SI *)nullptr, nullptr, f64);
+    A.code[r] = pair_code(kind, f64, status);
   }
-  L.w.kind[lane] = kind | tag;
+}
+
+template <typename S> __device__ __forceinline__ const S *column_of(const LatticeArgs &A);
+template <> __device__ __forceinline__ const double *column_of<double>(const LatticeArgs &A) { return A.col; }
+template <> __device__ __forceinline__ const float *column_of<float>(const LatticeArgs &A) { return A.col32; }
+
+/* records of the pairs of lattice units u0 + uu, uu < nu; unit u is
+   (x_k, sites t*kTile .. t*kTile + kTile - 1), k = u / tiles, t = u % tiles;
+   record r = uu * kTile + j */
+template <typename SI>
+__global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, LatticeArgs A, size_t u0,
+                                                         size_t nu, int mixed)
+{
+  const SI *col = column_of<SI>(A);
+  const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nu * kTile;
+       r += (size_t)gridDim.x * blockDim.x) {
+    const size_t u = u0 + r / kTile;
+    const size_t k = u / A.tiles, n = (u % A.tiles) * kTile + r % kTile;
+    if (n >= A.ny) continue;
+    double xv[4], yv[4];
+    for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * k + m]; yv[m] = A.y[4 * n + m]; }
+    const bool f64 = mixed && fp64_assembly(xv, yv);
+    Sink sk;
+    sk.f = nullptr;
+    sk.d = A.rec + r * REC;
+    int status;
+    const int kind = phase_a<SI>(T, xv, yv, sk, status, col ? col + k * per_x : nullptr,
+                                 A.col ? A.col + k * per_x : nullptr, f64);
+    A.code[r] = pair_code(kind, f64, status);
+  }
+}
+
+/* Shared memory of the assembly kernels: per warp the record (REC doubles),
+   the STV components ([200] and [201] = 0, the map's padding target) and the
+   384 components, sized for doubles and reused as floats; per block the map
+   schedules and coefficients and the reduction slots. */
+constexpr int kWarpDoubles = REC + 202 + 384;
+constexpr size_t kSchedBytes = (size_t)(2 * 3072 + 2 * 384) * sizeof(uint16_t);
+
+static size_t asm_smem_bytes(int wpb)
+{
+  return (size_t)wpb * kWarpDoubles * sizeof(double) + 8 * sizeof(double) + 8 * sizeof(float) +
+         kSchedBytes;
+}
+
+size_t smem_bytes_l0(int wpb) { return asm_smem_bytes(wpb); }
+
+struct AsmSmem {
+  double *rec, *stv, *tbuf;        /* this warp's */
+  double *coefd;
+  float *coeff;
+  uint16_t *eg, *ez, *rg, *rz;     /* map schedules */
+};
+
+__device__ __forceinline__ AsmSmem carve_asm(int wpb)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  AsmSmem L;
+  double *w = reinterpret_cast<double *>(smem_raw) + (size_t)(threadIdx.x >> 5) * kWarpDoubles;
+  L.rec = w;
+  L.stv = w + REC;
+  L.tbuf = L.stv + 202;
+  L.coefd = reinterpret_cast<double *>(smem_raw) + (size_t)wpb * kWarpDoubles;
+  L.coeff = reinterpret_cast<float *>(L.coefd + 8);
+  L.eg = reinterpret_cast<uint16_t *>(L.coeff + 8);
+  L.ez = L.eg + 3072;
+  L.rg = L.ez + 3072;
+  L.rz = L.rg + 384;
+  return L;
+}
+
+__device__ __forceinline__ void asm_prologue(const DevMaps &M, AsmSmem &L)
+{
+  if (threadIdx.x < 8) {
+    const float c[8] = {-2.0f, -1.0f, -0.5f, 0.5f, 1.0f, 2.0f, 0.0f, 0.0f};
+    L.coefd[threadIdx.x] = (double)c[threadIdx.x];
+    L.coeff[threadIdx.x] = c[threadIdx.x];
+  }
+  for (int i = threadIdx.x; i < M.gen.total; i += blockDim.x) L.eg[i] = M.ent_gen[i];
+  for (int i = threadIdx.x; i < M.zero.total; i += blockDim.x) L.ez[i] = M.ent_zero[i];
+  for (int i = threadIdx.x; i < 384; i += blockDim.x) { L.rg[i] = M.row_gen[i]; L.rz[i] = M.row_zero[i]; }
+  __syncthreads();
+}
+
+/* the 384 components of one pair into tbuf (type A) */
+template <typename A>
+__device__ __forceinline__ void assemble(const AsmSmem &L, const DevMaps &M, int kind, const A *R,
+                                         A *stv, A *tbuf, const A *coef, int lane)
+{
+  if (lane == 0) { stv[200] = A(0); stv[201] = A(0); }
+  if (kind == K_GEN) stv_generic<A>(R, stv, lane);
+  else if (kind == K_X0) stv_x0<A>(R, stv, lane);
+  else stv_y0<A>(R, stv, lane);
   __syncwarp();
-  return deferred;
-}
-
-/* pair q of the warp: assemble in its precision; returns false for a zero
-   kernel.  On return tbuf64 says which buffer holds the components. */
-template <typename S>
-__device__ __forceinline__ bool assemble_pair(const SmemLayout<S> &L, const DevMaps &M, int q,
-                                              int lane, bool &perm, bool &tbuf64)
-{
-  const int code = L.w.kind[q];
-  const int kind = code & 0xff;
-  perm = (kind == K_Y0PERM);
-  tbuf64 = (NSlots<S>::v == 0) || (code & (1 << 8));
-  if (kind == K_NONE) return false;
-  if (tbuf64) {
-    const double *R = (NSlots<S>::v == 0) ? reinterpret_cast<const double *>(L.w.rec) + q * REC
-                                          : L.w.rec64 + (code >> 9) * REC;
-    assemble<double>(L, M, kind, R, L.w.stvd, L.w.tbufd, L.coefd, lane);
-  } else {
-    const float *R = reinterpret_cast<const float *>(L.w.rec) + q * REC;
-    assemble<float>(L, M, kind, R, reinterpret_cast<float *>(L.w.stvd),
-                    reinterpret_cast<float *>(L.w.tbufd), L.coeff, lane);
-  }
-  return true;
-}
-
-template <typename S>
-__device__ __forceinline__ double kcomp(const SmemLayout<S> &L, bool t64, bool perm, int i)
-{
-  const int j = perm ? mulam(i) : i;
-  const double v = t64 ? L.w.tbufd[j] : (double)reinterpret_cast<const float *>(L.w.tbufd)[j];
-  return perm ? -v : v;
-}
-
-/* Batched L0: out[i][384] */
-template <typename SI, typename S>
-__global__ void __launch_bounds__(128) l0_kernel(DevTables T, DevMaps M, L0Args A, int wpb)
-{
-  SmemLayout<S> L = carve<S>(wpb);
-  block_prologue<S>(M, L);
-  const int lane = threadIdx.x & 31;
-  const size_t tile = (size_t)wpb * 32;
-  for (size_t base = (size_t)blockIdx.x * tile; base < A.n; base += (size_t)gridDim.x * tile) {
-    const size_t wbase = base + (threadIdx.x & ~31);
-    const size_t p = wbase + lane;
-    const bool active = p < A.n;
-    double xv[4] = {0, 0, 0, 0}, yv[4] = {0, 0, 0, 0};
-    if (active)
-      for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * p + m]; yv[m] = A.y[4 * p + m]; }
-    const int nq = (int)min((size_t)32, A.n > wbase ? A.n - wbase : (size_t)0);
-    bool pending = active;
-    for (;;) {
-      int status;
-      const bool deferred =
-          warp_phase_a<SI, S>(T, L, pending, xv, yv, (const SI *)nullptr, (const double *)nullptr,
-                              lane, status);
-      if (pending && !deferred && A.status) A.status[p] = (uint8_t)status;
-      for (int q = 0; q < nq; q++) {
-        if (L.w.kind[q] == K_SKIP) continue;
-        bool perm, t64;
-        const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
-        double *o = A.out + (wbase + q) * 384;
-#pragma unroll
-        for (int r = 0; r < 12; r++) {
-          const int i = r * 32 + lane;
-          o[i] = live ? kcomp<S>(L, t64, perm, i) : 0.0;
-        }
-        __syncwarp();
-      }
-      if (NSlots<S>::v == 0 || !__any_sync(0xffffffffu, deferred)) break;
-      pending = deferred;
-    }
-  }
+  if (kind == K_GEN) apply_map_warp<A>(L.eg, L.rg, M.gen, coef, stv, tbuf, lane);
+  else apply_map_warp<A>(L.ez, L.rz, M.zero, coef, stv, tbuf, lane);
+  __syncwarp();
 }
 
 /* Neumaier compensated add */
@@ -1556,10 +1493,65 @@ __device__ __forceinline__ float d2f_round(double v)
   return __uint_as_float(bits);
 }
 
+/* one pair by the warp, in the assembly precision S (the mixed form's
+   flagged pairs in FP64): record from global memory to shared memory, then
+   assemble.  Returns false for a zero kernel; t64 says whether the
+   components are doubles. */
+template <typename S>
+__device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, const double *grec,
+                                         int code, int lane, bool &perm, bool &t64)
+{
+  const int kind = code & 7;
+  perm = (kind == K_Y0PERM);
+  t64 = sizeof(S) == 8 || (code & 8);
+  if (kind == K_NONE) return false;
+  if (t64) {
+    for (int i = lane; i < REC; i += 32) L.rec[i] = __ldg(grec + i);
+    __syncwarp();
+    assemble<double>(L, M, kind, L.rec, L.stv, L.tbuf, L.coefd, lane);
+  } else {
+    float *rf = reinterpret_cast<float *>(L.rec);
+    for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));
+    __syncwarp();
+    assemble<float>(L, M, kind, rf, reinterpret_cast<float *>(L.stv),
+                    reinterpret_cast<float *>(L.tbuf), L.coeff, lane);
+  }
+  return true;
+}
+
+__device__ __forceinline__ double kcomp(const AsmSmem &L, bool t64, bool perm, int i)
+{
+  const int j = perm ? mulam(i) : i;
+  const double v = t64 ? L.tbuf[j] : (double)reinterpret_cast<const float *>(L.tbuf)[j];
+  return perm ? -v : v;
+}
+
+/* Batched L0 from records p0 + r, r < np: out[p][384], status[p] */
+template <typename S>
+__global__ void __launch_bounds__(256) l0_asm_kernel(DevMaps M, L0Args A, size_t p0, size_t np,
+                                                     int wpb)
+{
+  AsmSmem L = carve_asm(wpb);
+  asm_prologue(M, L);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (size_t r = (size_t)blockIdx.x * wpb + warp; r < np; r += (size_t)gridDim.x * wpb) {
+    const int code = A.code[r];
+    bool perm, t64;
+    const bool live = asm_pair<S>(L, M, A.rec + r * REC, code, lane, perm, t64);
+    double *o = A.out + (p0 + r) * 384;
+#pragma unroll
+    for (int q = 0; q < 12; q++) {
+      const int i = q * 32 + lane;
+      o[i] = live ? kcomp(L, t64, perm, i) : 0.0;
+    }
+    if (lane == 0 && A.status) A.status[p0 + r] = (uint8_t)(code >> 4);
+    __syncwarp();
+  }
+}
+
 /* sum_i K_i Pi_i of one pair, lane-partial: FP64 when the pair was assembled
    in FP64, else float products with the float per-site / per-x terms */
-template <typename S>
-__device__ __forceinline__ double contract(const SmemLayout<S> &L, bool live, bool perm, bool t64,
+__device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool perm, bool t64,
                                            const double *pi, const double *ky, const double *bx,
                                            const float *ky32, const float *bx32, int lane)
 {
@@ -1568,14 +1560,14 @@ __device__ __forceinline__ double contract(const SmemLayout<S> &L, bool live, bo
 #pragma unroll
     for (int r = 0; r < 12; r++) {
       const int i = r * 32 + lane;
-      double kv = live ? kcomp<S>(L, true, perm, i) : 0.0;
+      double kv = live ? kcomp(L, true, perm, i) : 0.0;
       if (ky) kv += __ldg(ky + i);
       if (bx) kv += __ldg(bx + i);
       acc = fma(kv, __ldg(pi + i), acc);
     }
     return acc;
   }
-  const float *tb = reinterpret_cast<const float *>(L.w.tbufd);
+  const float *tb = reinterpret_cast<const float *>(L.tbuf);
   float acc = 0.0f;
 #pragma unroll
   for (int r = 0; r < 12; r++) {
@@ -1588,59 +1580,38 @@ __device__ __forceinline__ double contract(const SmemLayout<S> &L, bool live, bo
   return (double)acc;
 }
 
-template <typename S> __device__ __forceinline__ const S *column_of(const LatticeArgs &A);
-template <> __device__ __forceinline__ const double *column_of<double>(const LatticeArgs &A) { return A.col; }
-template <> __device__ __forceinline__ const float *column_of<float>(const LatticeArgs &A) { return A.col32; }
-
-/* Fused lattice integrand: block (tile, k) sums pairs (x_k, y_n), n in the
-   tile; writes partial[k][tile] = (sum, compensation). */
-template <typename SI, typename S>
-__global__ void __launch_bounds__(128) lattice_kernel(DevTables T, DevMaps M, LatticeArgs A, int wpb)
+/* Fused lattice integrand over units u0 + uu, uu < nu (block per unit, warps
+   over its sites): partial[k][t] = (sum, compensation) of the unit's pairs,
+   warp sums in site order, block sum in warp order. */
+template <typename S>
+__global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, LatticeArgs A, size_t u0,
+                                                          size_t nu, int wpb)
 {
-  SmemLayout<S> L = carve<S>(wpb);
-  block_prologue<S>(M, L);
-  __shared__ double red_s[8], red_c[8];
+  AsmSmem L = carve_asm(wpb);
+  asm_prologue(M, L);
+  __shared__ double red_s[32], red_c[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const size_t tile = (size_t)wpb * 32;
-  const size_t nunits = A.nx * (size_t)A.tiles;
-  const SI *col = column_of<SI>(A);
-  const bool f32 = NSlots<S>::v > 0;
-  for (size_t u = blockIdx.x; u < nunits; u += gridDim.x) {
+  const bool f32 = sizeof(S) == 4;
+  for (size_t uu = blockIdx.x; uu < nu; uu += gridDim.x) {
+    const size_t u = u0 + uu;
     const size_t k = u / A.tiles, t = u % A.tiles;
-    const size_t wbase = t * tile + (size_t)warp * 32;
-    const size_t n = wbase + lane;
-    double xv[4], yv[4] = {0, 0, 0, 0};
-    for (int m = 0; m < 4; m++) xv[m] = A.x[4 * k + m];
-    const bool active = n < A.ny;
-    if (active)
-      for (int m = 0; m < 4; m++) yv[m] = A.y[4 * n + m];
-    const SI *colx = col ? col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
-    const double *c64 = A.col ? A.col + k * (size_t)T.nstpy * T.NK * kRow : nullptr;
     double s = 0.0, c = 0.0;
-    const int nq = (int)min((size_t)32, A.ny > wbase ? A.ny - wbase : (size_t)0);
-    bool pending = active;
-    for (;;) {
-      int status;
-      const bool deferred =
-          warp_phase_a<SI, S>(T, L, pending, xv, yv, colx, c64, lane, status);
-      for (int q = 0; q < nq; q++) {
-        if (L.w.kind[q] == K_SKIP) continue;
-        bool perm, t64;
-        const bool live = assemble_pair<S>(L, M, q, lane, perm, t64);
-        const size_t nn = wbase + q;
-        const double *pi = A.pi + (k * A.ny + nn) * 384;
-        const double *ky = A.Ky ? A.Ky + nn * 384 : nullptr;
-        const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
-        const float *ky32 = (f32 && A.Ky32) ? A.Ky32 + nn * 384 : nullptr;
-        const float *bx32 = (f32 && A.Bx32) ? A.Bx32 + k * 384 : nullptr;
-        double acc = contract<S>(L, live, perm, t64, pi, ky, bx, ky32, bx32, lane);
+    for (int j = warp; j < kTile; j += wpb) {
+      const size_t n = t * kTile + j;
+      if (n >= A.ny) break;
+      const size_t r = uu * kTile + j;
+      bool perm, t64;
+      const bool live = asm_pair<S>(L, M, A.rec + r * REC, A.code[r], lane, perm, t64);
+      const double *pi = A.pi + (k * A.ny + n) * 384;
+      const double *ky = A.Ky ? A.Ky + n * 384 : nullptr;
+      const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
+      const float *ky32 = (f32 && A.Ky32) ? A.Ky32 + n * 384 : nullptr;
+      const float *bx32 = (f32 && A.Bx32) ? A.Bx32 + k * 384 : nullptr;
+      double acc = contract(L, live, perm, t64, pi, ky, bx, ky32, bx32, lane);
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-        kadd(s, c, acc);
-        __syncwarp();
-      }
-      if (NSlots<S>::v == 0 || !__any_sync(0xffffffffu, deferred)) break;
-      pending = deferred;
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      kadd(s, c, acc);
+      __syncwarp();
     }
     if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
     __syncthreads();
@@ -1724,18 +1695,14 @@ static int num_sms()
   return n;
 }
 
-/* persistent grid: resident blocks per SM from the occupancy calculator,
-   capped at 3 for the FP64 kernels (measured: a fourth 2-warp block per SM
-   slows them, the FP64 pipe is already saturated and the extra shared memory
-   comes out of L1, which holds the x columns) and 4 for the float ones */
-static size_t grid_blocks(const void *fn, int wpb, size_t smem, size_t scalar_bytes)
+/* persistent grid: resident blocks per SM from the occupancy calculator */
+static size_t grid_blocks(const void *fn, int threads, size_t smem)
 {
   int per_sm = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
-  const int cap = scalar_bytes == 8 ? 3 : 4;
-  return (size_t)num_sms() * (size_t)min(per_sm, cap);
+  return (size_t)num_sms() * (size_t)per_sm;
 }
 
 static cudaError_t prep_kernel_smem(const void *fn, size_t bytes)
@@ -1743,22 +1710,42 @@ static cudaError_t prep_kernel_smem(const void *fn, size_t bytes)
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+static int asm_warps(const LaunchCfg &cfg)
+{
+  return cfg.warps_per_block > 0 ? std::min(cfg.warps_per_block, 8) : 8;
+}
+
+/* record-kernel grid: thread per pair, 64 threads per block */
+template <typename K>
+static unsigned rec_grid(K fn, size_t n)
+{
+  const size_t g = std::min((n + 63) / 64, grid_blocks((const void *)fn, 64, 0));
+  return (unsigned)std::max<size_t>(g, 1);
+}
+
 template <typename SI, typename S>
 static cudaError_t launch_l0_t(const DevTables &T, const DevMaps &M, const L0Args &a,
                                const LaunchCfg &cfg, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
-  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
-  const size_t smem = smem_bytes<S>(wpb);
-  cudaError_t e = prep_kernel_smem((const void *)l0_kernel<SI, S>, smem);
+  if (!a.rec || !a.code || a.rec_cap == 0) return cudaErrorInvalidValue;
+  const int wpb = asm_warps(cfg);
+  const size_t smem = asm_smem_bytes(wpb);
+  cudaError_t e = prep_kernel_smem((const void *)l0_asm_kernel<S>, smem);
   if (e != cudaSuccess) return e;
-  const size_t tiles = (a.n + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32);
-  const size_t blocks0 = grid_blocks((const void *)l0_kernel<SI, S>, wpb, smem, sizeof(S));
-  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : blocks0;
-  if (blocks > tiles) blocks = tiles;
-  l0_kernel<SI, S><<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
-  g_launches++;
-  return cudaGetLastError();
+  const size_t ablocks0 = grid_blocks((const void *)l0_asm_kernel<S>, wpb * 32, smem);
+  const int mixed = sizeof(S) == 4;
+  for (size_t p0 = 0; p0 < a.n; p0 += a.rec_cap) {
+    const size_t np = std::min(a.rec_cap, a.n - p0);
+    l0_rec_kernel<SI><<<rec_grid(l0_rec_kernel<SI>, np), 64, 0, s>>>(T, a, p0, np, mixed);
+    g_launches++;
+    size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
+    blocks = std::min(blocks, (np + wpb - 1) / wpb);
+    l0_asm_kernel<S><<<(unsigned)blocks, wpb * 32, smem, s>>>(M, a, p0, np, wpb);
+    g_launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a,
@@ -1777,18 +1764,28 @@ template <typename SI, typename S>
 static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                     const LaunchCfg &cfg, cudaStream_t s)
 {
-  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
-  const size_t smem = smem_bytes<S>(wpb);
-  cudaError_t e = prep_kernel_smem((const void *)lattice_kernel<SI, S>, smem);
-  if (e != cudaSuccess) return e;
   const size_t units = a.nx * (size_t)a.tiles;
   if (units == 0) return cudaSuccess;
-  const size_t blocks0 = grid_blocks((const void *)lattice_kernel<SI, S>, wpb, smem, sizeof(S));
-  size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : blocks0;
-  if (blocks > units) blocks = units;
-  lattice_kernel<SI, S><<<(unsigned)blocks, wpb * 32, smem, s>>>(T, M, a, wpb);
-  g_launches++;
-  return cudaGetLastError();
+  if (!a.rec || !a.code || a.rec_cap < (size_t)kTile) return cudaErrorInvalidValue;
+  const int wpb = asm_warps(cfg);
+  const size_t smem = asm_smem_bytes(wpb);
+  cudaError_t e = prep_kernel_smem((const void *)lattice_asm_kernel<S>, smem);
+  if (e != cudaSuccess) return e;
+  const size_t ablocks0 = grid_blocks((const void *)lattice_asm_kernel<S>, wpb * 32, smem);
+  const int mixed = sizeof(S) == 4;
+  const size_t cu = a.rec_cap / kTile;
+  for (size_t u0 = 0; u0 < units; u0 += cu) {
+    const size_t nu = std::min(cu, units - u0);
+    lattice_rec_kernel<SI><<<rec_grid(lattice_rec_kernel<SI>, nu * kTile), 64, 0, s>>>(T, a, u0, nu,
+                                                                                        mixed);
+    g_launches++;
+    size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
+    blocks = std::min(blocks, nu);
+    lattice_asm_kernel<S><<<(unsigned)blocks, wpb * 32, smem, s>>>(M, a, u0, nu, wpb);
+    g_launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
@@ -1798,11 +1795,8 @@ cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const Latt
 }
 
 cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
-                                 const LaunchCfg &cfg, cudaStream_t s, int split)
+                                 const LaunchCfg &cfg, cudaStream_t s)
 {
-  /* split 0: float interpolation, float assembly except the FP64-routed
-     pairs; 2: FP64 interpolation, same assembly (diagnostic) */
-  if (split == 2) return launch_lattice_t<double, float>(T, M, a, cfg, s);
   return launch_lattice_t<float, float>(T, M, a, cfg, s);
 }
 

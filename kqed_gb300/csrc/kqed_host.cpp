@@ -123,7 +123,11 @@ struct Scratch {
   double *get(size_t n)
   {
     if (n > cap) {
-      if (buf) cudaFree(buf);
+      /* work queued on any stream may still use the old buffer */
+      if (buf) {
+        cudaDeviceSynchronize();
+        cudaFree(buf);
+      }
       buf = nullptr;
       cap = 0;
       if (cudaMalloc(&buf, n * sizeof(double)) != cudaSuccess) return nullptr;
@@ -143,8 +147,7 @@ struct Ctx {
   int device = 0;
   DevTables T{};
   DevMaps M{};
-  LaunchCfg cfg{2, 0};
-  int mixed_split = 0;
+  LaunchCfg cfg{8, 0};
   std::vector<void *> allocs;
 };
 
@@ -154,7 +157,7 @@ struct ThreadStage {
   cudaStream_t stream = nullptr, copy_stream = nullptr;
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double *h_pin = nullptr;   /* 8 + 384 doubles */
-  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32;
+  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32, d_rec;
   ~ThreadStage() { reset(); }
   void reset()
   {
@@ -168,6 +171,7 @@ struct ThreadStage {
     copy_stream = nullptr;
     if (h_pin) cudaFreeHost(h_pin);
     d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release(); d_col.release(); d_col32.release();
+    d_rec.release();
     stream = nullptr;
     h_pin = nullptr;
     owner = nullptr;
@@ -175,6 +179,20 @@ struct ThreadStage {
 };
 
 thread_local ThreadStage tl_stage;
+
+static ThreadStage &stage_for(Ctx *c)
+{
+  ThreadStage &st = tl_stage;
+  if (st.owner != c) {
+    st.reset();
+    st.owner = c;
+  }
+  return st;
+}
+
+/* Per-pair records between the record and assembly kernels: room for up to
+   kRecPairs pairs (712 bytes each) per launch pair, a multiple of kTile. */
+constexpr size_t kRecPairs = (size_t)1 << 20;
 
 Ctx *ctx_of(const struct QED_kernel_temps *t)
 {
@@ -434,10 +452,8 @@ static int setup_device(struct Grid_coeffs *G, Ctx *c)
   if (!c->M.ent_gen || !c->M.ent_zero || !c->M.row_gen || !c->M.row_zero) return fail("map upload failed");
   const char *wpb = getenv("KQED_WARPS_PER_BLOCK");
   const char *blk = getenv("KQED_BLOCKS");
-  if (wpb) c->cfg.warps_per_block = std::max(1, std::min(4, atoi(wpb)));
+  if (wpb) c->cfg.warps_per_block = std::max(1, std::min(8, atoi(wpb)));
   if (blk) c->cfg.blocks = std::max(0, atoi(blk));
-  const char *sp = getenv("KQED_MIXED_SPLIT");
-  if (sp) c->mixed_split = std::max(0, std::min(2, atoi(sp)));
   return 0;
 }
 
@@ -536,10 +552,25 @@ static int check_variant_precision(int variant, int precision)
 /* L0 over n pairs on the device */
 static thread_local int tl_precision = KQED_FP64;
 
-static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *dout,
-                  uint8_t *dstatus, cudaStream_t s, bool timed = true, int variant = 0)
+/* record scratch for n pairs (capped at kRecPairs; launches are chunked) */
+static int rec_scratch(ThreadStage &st, size_t n, double **rec, uint8_t **code, size_t *cap)
 {
-  L0Args a{dx, dy, n, dout, dstatus, variant};
+  size_t c = std::min(std::max(n, (size_t)kTile), kRecPairs);
+  c = (c + kTile - 1) / kTile * kTile;
+  double *b = st.d_rec.get(c * kRec + c / 8 + 1);
+  if (!b) return fail("out of device memory for %zu pair records", c);
+  *rec = b;
+  *code = reinterpret_cast<uint8_t *>(b + c * kRec);
+  *cap = c;
+  return 0;
+}
+
+static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *dout,
+                  uint8_t *dstatus, cudaStream_t s, bool timed = true)
+{
+  L0Args a{dx, dy, n, dout, dstatus, nullptr, nullptr, 0};
+  if (n == 0) return 0;
+  if (rec_scratch(stage_for(c), n, &a.rec, &a.code, &a.rec_cap)) return 1;
   TimedLaunch tl{nullptr, nullptr};
   if (timed) prof_begin(s, tl);
   if (tl_precision == KQED_FP32_MIXED && timed) CUDA_OK(launch_l0_mixed(c->T, c->M, a, c->cfg, s));
@@ -552,7 +583,7 @@ static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *
 static int run_variant(Ctx *c, int variant, const double *dx, const double *dy, size_t n,
                        double *dout, uint8_t *dstatus, cudaStream_t s, ThreadStage &st)
 {
-  if (run_l0(c, dx, dy, n, dout, dstatus, s, true, variant)) return 1;
+  if (run_l0(c, dx, dy, n, dout, dstatus, s, true)) return 1;
   if (variant == 0) return 0;
   double *tmp = st.d_tmp.get(n * 384);
   double *zero = st.d_aux.get(n * 4);
@@ -581,16 +612,6 @@ static int run_variant(Ctx *c, int variant, const double *dx, const double *dy, 
     break;
   }
   return 0;
-}
-
-static ThreadStage &stage_for(Ctx *c)
-{
-  ThreadStage &st = tl_stage;
-  if (st.owner != c) {
-    st.reset();
-    st.owner = c;
-  }
-  return st;
 }
 
 extern "C" int kqed_kernel_batch_dev(const struct QED_kernel_temps *t, int variant, size_t n,
@@ -741,8 +762,10 @@ struct LatticeRun {
   Ctx *c;
   const double *d_x, *d_y;
   size_t nx, ny;
-  double *Ky, *Bx, *partial, *col;
+  double *Ky, *Bx, *partial, *col, *rec;
   float *Ky32, *Bx32, *col32;
+  uint8_t *code;
+  size_t rec_cap;
   int tiles, precision, variant;
 };
 
@@ -754,29 +777,27 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.variant = variant;
   R.Ky32 = R.Bx32 = R.col32 = nullptr;
   R.col = nullptr;
+  R.tiles = (int)((ny + kTile - 1) / kTile);
+  /* records first: the kernel-term launches below reuse the same scratch */
+  if (rec_scratch(st, nx * (size_t)R.tiles * kTile, &R.rec, &R.code, &R.rec_cap)) return 1;
   if (lattice_terms(c, variant, d_x, nx, d_y, ny, &R.Ky, &R.Bx, s, st)) return 1;
-  const int wpb = c->cfg.warps_per_block;
-  R.tiles = (int)((ny + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32));
   R.partial = st.d_tmp.get(nx * (size_t)std::max(R.tiles, 1) * 2);
   if (!R.partial) return fail("out of device memory for partial sums");
   const size_t ncol = nx * (size_t)c->T.nstpy * c->T.NK * kRow;
   const bool mixed = precision == KQED_FP32_MIXED;
-  const int split = mixed ? c->mixed_split : -1;
   /* FP64 columns always (the FP64 form, and the float form's pairs near
-     cb = +-1); float columns for the float interpolation of the mixed form */
+     cb = +-1 or assembled in FP64); float columns for the float
+     interpolation of the mixed form */
   R.col = st.d_col.get(ncol);
   if (!R.col) return fail("out of device memory for x-column tables");
   CUDA_OK(launch_build_columns(c->T, d_x, nx, R.col, s));
   if (mixed) {
-    const bool col32 = split != 2;
-    const size_t n32 = (col32 ? ncol : 0) + (R.Ky ? (ny + nx) * 384 : 0);
+    const size_t n32 = ncol + (R.Ky ? (ny + nx) * 384 : 0);
     float *b32 = reinterpret_cast<float *>(st.d_col32.get(n32 / 2 + 2));
     if (!b32) return fail("out of device memory for float tables");
-    if (col32) {
-      R.col32 = b32;
-      b32 += ncol;
-      CUDA_OK(launch_build_columns32(c->T, d_x, nx, R.col32, s));
-    }
+    R.col32 = b32;
+    b32 += ncol;
+    CUDA_OK(launch_build_columns32(c->T, d_x, nx, R.col32, s));
     if (R.Ky) {
       /* the FP64-evaluated per-site / per-x terms, as float */
       R.Ky32 = b32;
@@ -799,10 +820,10 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
                 R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1), R.tiles,
                 R.col ? R.col + per_x * x0 : nullptr,
                 R.Ky32, R.Bx32 ? R.Bx32 + 384 * x0 : nullptr,
-                R.col32 ? R.col32 + per_x * x0 : nullptr, R.variant};
+                R.col32 ? R.col32 + per_x * x0 : nullptr, R.rec, R.code, R.rec_cap};
   TimedLaunch tl;
   prof_begin(s, tl);
-  if (mixed) CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s, R.c->mixed_split));
+  if (mixed) CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s));
   else CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, R.c->cfg, s));
   prof_end(s, tl);
   return 0;

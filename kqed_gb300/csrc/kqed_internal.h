@@ -36,6 +36,8 @@ static const int kShiftOfTable[NFFA] = {0, 0, 1, 0, 1, 2, 0, 0, 1, 0, 1, 2, 1, 0
 
 constexpr int kRow = 28;     /* doubles per (node, U-index) row: 14 tables x (value, y-derivative) */
 constexpr int kNKMax = 64;   /* max Chebyshev length incl. the shift (nfx + 2) */
+constexpr int kRec = 88;     /* doubles in the per-pair record between the two kernels */
+constexpr int kTile = 64;    /* lattice sites per partial sum (unit = one x, kTile sites) */
 
 /* Device-resident tables.  `node` holds, for every grid node (ix, iy) and
    Chebyshev index K (0..NK-1, U_K), the y-power-scaled coefficient of every
@@ -76,14 +78,15 @@ struct LaunchCfg {
   int blocks;
 };
 
-/* Batched plain-FP64 L0: out[i][384] (or, when pi != NULL, the fused
-   contraction; see kqed_fp64.cu). */
+/* Batched L0: out[i][384] for the pairs (x[i], y[i]). */
 struct L0Args {
   const double *x, *y;  /* [n][4] */
   size_t n;
-  double *out;          /* [n][384] or NULL */
+  double *out;          /* [n][384] */
   uint8_t *status;      /* [n] or NULL */
-  int variant;          /* L0..L3 the terms belong to (mixed form: FP64 zone) */
+  double *rec;          /* record scratch [rec_cap][kRec] */
+  uint8_t *code;        /* [rec_cap] */
+  size_t rec_cap;       /* pairs per record kernel launch */
 };
 
 struct LatticeArgs {
@@ -94,10 +97,12 @@ struct LatticeArgs {
   const double *Ky;     /* [ny][384] per-site additive kernel terms or NULL */
   const double *Bx;     /* [nx][384] per-x additive kernel terms or NULL */
   double *partial;      /* [nx][tiles][2]  (sum, compensation) */
-  int tiles;            /* y tiles per x */
+  int tiles;            /* site tiles per x: ceil(ny / kTile) */
   const double *col;    /* per-x column tables [nx][nstpy][NK][kRow] or NULL */
   const float *Ky32, *Bx32, *col32;   /* the same in float, for the mixed form */
-  int variant;
+  double *rec;          /* record scratch [rec_cap][kRec] */
+  uint8_t *code;        /* [rec_cap] */
+  size_t rec_cap;       /* pairs per record kernel launch (a multiple of kTile) */
 };
 
 int upload_map_constants();
@@ -112,7 +117,7 @@ cudaError_t launch_build_columns32(const DevTables &T, const double *xs, size_t 
 cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &a,
                             const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
-                                 const LaunchCfg &cfg, cudaStream_t s, int split = 0);
+                                 const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_to_float(const double *in, float *out, size_t n, cudaStream_t s);
 cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,
                                    cudaStream_t s);

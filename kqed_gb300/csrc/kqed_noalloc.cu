@@ -21,7 +21,10 @@
  *     stream capture;
  *   - problems whose scratch does not fit are rejected with an error that
  *     states the need and the limit; nothing is allocated, here or in any
- *     library routine this function calls;
+ *     library routine this function calls.  The per-pair records passed
+ *     between the record and assembly kernels take whatever room is left
+ *     (at least one tile of kTile pairs); with less room the same kernels
+ *     run in more, smaller launches;
  *   - all calls share the one array and it keeps the last call's contents.
  *     Everything a call reads from it is first written by the same call (the
  *     zero vectors are cleared by a kernel, partial sums and kernel terms are
@@ -73,10 +76,16 @@ int scratch_on_current_device(double **out)
   return 0;
 }
 
+struct Recs {
+  double *rec;
+  uint8_t *code;
+  size_t cap;
+};
+
 int l0(const kqed::DevTables &T, const kqed::DevMaps &M, const kqed::LaunchCfg &cfg,
-       const double *dx, const double *dy, size_t n, double *out, cudaStream_t s)
+       const double *dx, const double *dy, size_t n, double *out, const Recs &R, cudaStream_t s)
 {
-  kqed::L0Args a{dx, dy, n, out, nullptr, 0};
+  kqed::L0Args a{dx, dy, n, out, nullptr, R.rec, R.code, R.cap};
   return kqed::launch_l0_fp64(T, M, a, cfg, s) != cudaSuccess;
 }
 
@@ -93,11 +102,12 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
   if (variant < 0 || variant > 3) return kqed::set_error("variant not in 0..3");
   if (nx == 0) return 0;
   if (!d_x || !d_y || !d_pi || !d_sums) return kqed::set_error("null buffer");
-  const int wpb = cfg.warps_per_block > 0 ? cfg.warps_per_block : 2;
-  const size_t tiles = (ny + (size_t)wpb * 32 - 1) / ((size_t)wpb * 32);
+  const size_t tiles = (ny + kqed::kTile - 1) / kqed::kTile;
   const size_t n_partial = nx * (tiles ? tiles : 1) * 2;
   const size_t n_terms = variant ? ny * 384 + ny * 4 + nx * 384 * 2 + nx * 4 : 0;
-  const size_t need = n_partial + n_terms;
+  /* one tile of records at least: kTile pairs of kRec doubles + their codes */
+  const size_t rec_tile = (size_t)kqed::kTile * kqed::kRec + kqed::kTile / 8;
+  const size_t need = n_partial + n_terms + rec_tile;
   if (need > kNoallocDoubles) {
     char msg[320];
     snprintf(msg, sizeof(msg),
@@ -110,6 +120,16 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
   if (scratch_on_current_device(&S)) return 1;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   double *partial = S;
+  /* records in the room after the partial sums and kernel terms */
+  Recs RC;
+  {
+    const size_t room = kNoallocDoubles - n_partial - n_terms;
+    size_t cap = room * 8 / (8 * (size_t)kqed::kRec + 1);
+    cap = cap / kqed::kTile * kqed::kTile;
+    RC.rec = S + n_partial + n_terms;
+    RC.code = reinterpret_cast<uint8_t *>(RC.rec + cap * kqed::kRec);
+    RC.cap = cap;
+  }
   double *Ky = nullptr, *Bx = nullptr;
   if (variant) {
     Ky = partial + n_partial;
@@ -122,18 +142,18 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
     /* the per-site and per-x terms of QED_kernel_L1..L3, src/LIBFILES/kernels.c:117-177 */
     switch (variant) {
     case 1:
-      bad = bad || l0(T, M, cfg, d_y, d_y, ny, Ky, s) || l0(T, M, cfg, d_x, d_x, nx, Bx, s) ||
+      bad = bad || l0(T, M, cfg, d_y, d_y, ny, Ky, RC, s) || l0(T, M, cfg, d_x, d_x, nx, Bx, RC, s) ||
             kqed::launch_scale(Ky, -0.5, ny * 384, s) != cudaSuccess ||
             kqed::launch_scale(Bx, -0.5, nx * 384, s) != cudaSuccess;
       break;
     case 2:
-      bad = bad || l0(T, M, cfg, zy, d_y, ny, Ky, s) || l0(T, M, cfg, d_x, zx, nx, Bx, s) ||
+      bad = bad || l0(T, M, cfg, zy, d_y, ny, Ky, RC, s) || l0(T, M, cfg, d_x, zx, nx, Bx, RC, s) ||
             kqed::launch_scale(Ky, -1.0, ny * 384, s) != cudaSuccess ||
             kqed::launch_scale(Bx, -1.0, nx * 384, s) != cudaSuccess;
       break;
     default:
-      bad = bad || l0(T, M, cfg, zy, d_y, ny, Ky, s) || l0(T, M, cfg, d_x, d_x, nx, Bx, s) ||
-            l0(T, M, cfg, zx, d_x, nx, bt, s) ||
+      bad = bad || l0(T, M, cfg, zy, d_y, ny, Ky, RC, s) || l0(T, M, cfg, d_x, d_x, nx, Bx, RC, s) ||
+            l0(T, M, cfg, zx, d_x, nx, bt, RC, s) ||
             kqed::launch_scale(Ky, -1.0, ny * 384, s) != cudaSuccess ||
             kqed::launch_scale(Bx, -1.0, nx * 384, s) != cudaSuccess ||
             kqed::launch_axpy(Bx, bt, 1.0, nx * 384, s) != cudaSuccess;
@@ -142,7 +162,7 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
     if (bad) return kqed::set_error("kqed_lattice_sum_noalloc: kernel-term launch failed");
   }
   kqed::LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, (int)tiles, nullptr,
-                      nullptr, nullptr, nullptr, variant};
+                      nullptr, nullptr, nullptr, RC.rec, RC.code, RC.cap};
   if (kqed::launch_lattice_fp64(T, M, a, cfg, s) != cudaSuccess ||
       kqed::launch_reduce_partials(partial, nx, (int)tiles, d_sums, s) != cudaSuccess)
     return kqed::set_error("kqed_lattice_sum_noalloc: lattice kernel launch failed");
