@@ -10,8 +10,12 @@ term.  Pi is 32.6 GB per step, far larger than L2, so no flush is needed.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 Prints one JSON line (rank 0).  `value` times the device entry point with
-inputs resident in HBM; `e2e` times the host entry point (Pi copied from
-pinned host memory every step).  --impl reference times the reference's CPU
+inputs resident in HBM, in the precision form given by --precision (fp64:
+the plain FP64 form, bit-for-bit the reference's algorithm; fp32: the mixed
+form).  Both forms are always timed on the same inputs and reported under
+`forms`, with the mixed form's integrand error against the FP64 sums of the
+same run.  `e2e` times the host entry point (Pi copied from pinned host
+memory every step).  --impl reference times the reference's CPU
 implementation of the same computation on the host cores (the reference
 library compiled from its sources when it is available here, else the CPU
 restatement under oracle/).
@@ -41,7 +45,7 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="fp64", choices=["fp64"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     p.add_argument("--L", type=int, default=24)
     p.add_argument("--spacing", type=float, default=0.1)
     p.add_argument("--nx", type=int, default=32)
@@ -239,7 +243,7 @@ def run_gb300(args):
     torch.cuda.set_device(dev)
     t = K.KernelTemps()
     g = t.grid()
-    prec = {"fp64": K.KQED_FP64}[args.precision]
+    prec = {"fp64": K.KQED_FP64, "fp32": K.KQED_FP32_MIXED}[args.precision]
 
     xs = diagonal_x(args.nx, args.spacing) * x_direction(rank)[None, :]
     ys = lattice_sites(args.L, args.spacing)
@@ -250,9 +254,9 @@ def run_gb300(args):
     sums = torch.empty(nx, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step():
+    def step(p=None):
         K.lattice_sum_dev(t, args.variant, dx.data_ptr(), nx, dy.data_ptr(), ny, pi.data_ptr(),
-                          sums.data_ptr(), prec, stream.cuda_stream)
+                          sums.data_ptr(), prec if p is None else p, stream.cuda_stream)
 
     def barrier():
         if world > 1:
@@ -290,7 +294,37 @@ def run_gb300(args):
         ms_step = float(mt.item())
     value = world * nx * ny / (ms_step / 1e3)
 
-    # ---- roofline of the dominant kernel (the fused lattice kernel)
+    # ---- both precision forms on the same resident inputs: time and the
+    #      mixed form's integrand error against the FP64 sums
+    forms = {}
+    fsums = {}
+    for name, pm in (("fp64", K.KQED_FP64), ("fp32_mixed", K.KQED_FP32_MIXED)):
+        for _ in range(2):
+            step(pm)
+        torch.cuda.synchronize(dev)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            step(pm)
+        f1.record(stream)
+        torch.cuda.synchronize(dev)
+        fms = f0.elapsed_time(f1) / args.steps
+        fsums[name] = sums.cpu().numpy().copy()
+        forms[name] = {"value": world * nx * ny / (fms / 1e3), "ms_per_step": fms}
+    ref = fsums["fp64"]
+    err = np.abs(fsums["fp32_mixed"] - ref)
+    rms = float(np.sqrt(np.mean(ref ** 2)))
+    live = np.abs(ref) > 1e-12 * max(rms, 1e-300)
+    forms["fp32_mixed"].update({
+        "speedup_vs_fp64": forms["fp64"]["ms_per_step"] / forms["fp32_mixed"]["ms_per_step"],
+        "err_vs_fp64": {
+            "definition": "per x: |S_fp32 - S_fp64| / rms_x(S_fp64), S = sum_y L.Pi",
+            "max": float(err.max() / rms) if rms > 0 else None,
+            "median": float(np.median(err) / rms) if rms > 0 else None,
+            "max_rel_own": float((err[live] / np.abs(ref[live])).max()) if live.any() else None}})
+
+    # ---- roofline of the dominant kernels (record + assembly, FP64 form)
     peak_gflops = K.fp64_peak_gflops()
     flops_launch = F.lattice_flops(xs, ys, g["XX"], g["nfx"], args.variant)
     kavg_ms = kern_ms / max(kern_n, 1)
@@ -316,18 +350,44 @@ def run_gb300(args):
 
     e2e_step()
     barrier()
+    K.profile(True)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         e2e_step()
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_kern_ms, _ = K.profile_read()
+    e2e_copy_ms, _ = K.profile_read_copies()
+    K.profile(False)
     if world > 1:
         mt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(mt, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(mt.item())
+    # host->device link rate right after (the same pinned buffer, 1 GB pieces):
+    # Pi crosses the link every step, so e2e cannot beat bytes / this rate
+    scratch = torch.empty(min(pi_host.numel(), 1 << 27), dtype=torch.float64, device=dev)
+    flat = pi_host.view(-1)
+    torch.cuda.synchronize(dev)
+    c0 = time.perf_counter()
+    moved = 0
+    for o in range(0, flat.numel(), scratch.numel()):
+        n = min(scratch.numel(), flat.numel() - o)
+        scratch[:n].copy_(flat[o:o + n], non_blocking=True)
+        moved += n * 8
+    torch.cuda.synchronize(dev)
+    h2d_gbs = moved / (time.perf_counter() - c0) / 1e9
+    del scratch
     e2e = {"value": world * nx * ny / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(pi_host.numel() * 8 + xh.nbytes + yh.nbytes),
-           "d2h_bytes_per_step": int(sh.nbytes)}
+           "d2h_bytes_per_step": int(sh.nbytes),
+           "precision": args.precision,
+           "h2d_link_gbs_measured": h2d_gbs,
+           "ms_per_step": e2e_s * 1e3,
+           "kernel_ms_per_step": e2e_kern_ms / args.e2e_steps,
+           "copy_ms_per_step": e2e_copy_ms / args.e2e_steps,
+           "h2d_gbs_during_step": pi_host.numel() * 8 / (e2e_copy_ms / args.e2e_steps / 1e3) / 1e9
+           if e2e_copy_ms > 0 else None,
+           "copy_bound_evals_per_s": world * nx * ny / (pi_host.numel() * 8 / (h2d_gbs * 1e9))}
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -342,14 +402,18 @@ def run_gb300(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp64": "f64"}[args.precision], "data": "synthetic",
+            "dtype": {"fp64": "f64", "fp32": "f32+f64"}[args.precision], "data": "synthetic",
             "config": workload_config(args, ny),
             "e2e": e2e,
+            "forms": forms,
             "gpu_launches": launches,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_gflops / 1e3,
                          "unit": "TFLOP/s", "frac": achieved / (peak_gflops / 1e3),
                          "traffic": None,
-                         "kernel": "lattice_fp64_kernel", "kernel_ms": kavg_ms,
+                         "kernel": "lattice_rec_kernel<double> + lattice_asm_kernel<double>"
+                                   if args.precision == "fp64" else
+                                   "lattice_rec_kernel<float> + lattice_asm_kernel<float>",
+                         "kernel_ms": kavg_ms,
                          "flops_per_launch": flops_launch,
                          "flops_source": F.table().get("source"),
                          "peak_source": "FP64 FMA-chain probe run by this bench (not in "

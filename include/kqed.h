@@ -158,12 +158,15 @@ const char *kqed_last_error(void);
 uint64_t kqed_launch_count(void);
 
 /* Diagnostics.  kqed_profile(1) starts recording CUDA events on the
-   launching stream around every main kernel (the fused lattice kernel, the
-   batched L0 kernel); kqed_profile_read returns their summed duration and
-   count; kqed_profile(0) stops and clears.  kqed_fp64_peak_gflops runs an
-   FP64 FMA-chain probe on the current device and returns GFLOP/s. */
+   launching stream around every main launch (the record + assembly kernel
+   pair of the lattice sums and of the batched L0) and around every Pi chunk
+   copy of kqed_lattice_sum; kqed_profile_read returns the launches' summed
+   duration and count, kqed_profile_read_copies the copies'; kqed_profile(0)
+   stops and clears.  kqed_fp64_peak_gflops runs an FP64 FMA-chain probe on
+   the current device and returns GFLOP/s.  No reference counterpart. */
 void kqed_profile(int enable);
 int kqed_profile_read(double *total_ms, uint64_t *launches);
+int kqed_profile_read_copies(double *total_ms, uint64_t *copies);
 int kqed_fp64_peak_gflops(double *gflops);
 
 #ifdef __cplusplus

@@ -99,6 +99,8 @@ def lib():
         L.kqed_profile.restype = None
         L.kqed_profile_read.argtypes = [dp, ctypes.POINTER(ctypes.c_uint64)]
         L.kqed_profile_read.restype = ctypes.c_int
+        L.kqed_profile_read_copies.argtypes = [dp, ctypes.POINTER(ctypes.c_uint64)]
+        L.kqed_profile_read_copies.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
         L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
@@ -250,6 +252,14 @@ def profile_read():
     ms = ctypes.c_double()
     n = ctypes.c_uint64()
     _check(lib().kqed_profile_read(ctypes.byref(ms), ctypes.byref(n)))
+    return ms.value, int(n.value)
+
+
+def profile_read_copies():
+    """(total milliseconds, copies) of the Pi chunk copies of lattice_sum."""
+    ms = ctypes.c_double()
+    n = ctypes.c_uint64()
+    _check(lib().kqed_profile_read_copies(ctypes.byref(ms), ctypes.byref(n)))
     return ms.value, int(n.value)
 
 

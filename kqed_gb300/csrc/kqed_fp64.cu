@@ -1334,17 +1334,26 @@ static_assert(REC == kRec, "record size");
    - the x = 0 / y = 0 / x = y forms: there L1..L3 vanish identically
      (kernels.c:117-177) and must come out as exact differences of the FP64
      per-site and per-x terms;
-   - |x - y| < max(|x|, |y|) / 4: these take the x <-> (x-y) swap, whose
-     chain rule (1/|x-y| factors) makes the STV terms large and cancelling,
-     so float assembly would lose about log2(max(|x|,|y|)/|x-y|) bits on the
-     pairs that weigh most in a lattice sum. */
-__device__ __forceinline__ bool fp64_assembly(const double *xv, const double *yv)
+   - |x - y| < max(|x|, |y|) / r (r = near_ratio of the launch, 4 by
+     default): these take the x <-> (x-y) swap, whose chain rule (1/|x-y|
+     factors) makes the STV terms large and cancelling, so float assembly
+     would lose about log2(max(|x|,|y|)/|x-y|) bits on the pairs that weigh
+     most in a lattice sum;
+   - max(|x|, |y|) < R (R = origin_radius of the launch, 0.35 by default):
+     near the origin the kernel is orders of magnitude larger than elsewhere
+     (a few hundred such pairs carry most of a lattice sum at small |x|), so
+     their float rounding, about 1e-7 of each contribution, would dominate
+     the sum's error.
+   near2 = r^2, orig2 = R^2; near2 = 0 selects no pair (the plain FP64 form). */
+__device__ __forceinline__ bool fp64_assembly(const double *xv, const double *yv, double near2,
+                                              double orig2)
 {
   const double xx = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
   const double yy = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
   const double d0 = xv[0] - yv[0], d1 = xv[1] - yv[1], d2 = xv[2] - yv[2], d3 = xv[3] - yv[3];
   const double dd = d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
-  return xx < 1E-28 || yy < 1E-28 || dd < 1E-28 || 16.0 * dd < fmax(xx, yy);
+  const double mm = fmax(xx, yy);
+  return xx < 1E-28 || yy < 1E-28 || dd < 1E-28 || near2 * dd < mm || mm < orig2;
 }
 
 __device__ __forceinline__ uint8_t pair_code(int kind, bool f64, int status)
@@ -1355,14 +1364,14 @@ __device__ __forceinline__ uint8_t pair_code(int kind, bool f64, int status)
 /* records of pairs p0 + r, r < np, of a batch (x[p], y[p]) */
 template <typename SI>
 __global__ void __launch_bounds__(64) l0_rec_kernel(DevTables T, L0Args A, size_t p0, size_t np,
-                                                    int mixed)
+                                                    int mixed, double near2, double orig2)
 {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < np;
        r += (size_t)gridDim.x * blockDim.x) {
     const size_t p = p0 + r;
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * p + m]; yv[m] = A.y[4 * p + m]; }
-    const bool f64 = mixed && fp64_assembly(xv, yv);
+    const bool f64 = mixed && fp64_assembly(xv, yv, near2, orig2);
     Sink sk;
     sk.f = nullptr;
     sk.d = A.rec + r * REC;
@@ -1381,7 +1390,8 @@ template <> __device__ __forceinline__ const float *column_of<float>(const Latti
    record r = uu * kTile + j */
 template <typename SI>
 __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, LatticeArgs A, size_t u0,
-                                                         size_t nu, int mixed)
+                                                         size_t nu, int mixed, double near2,
+                                                         double orig2)
 {
   const SI *col = column_of<SI>(A);
   const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
@@ -1392,7 +1402,7 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, LatticeArg
     if (n >= A.ny) continue;
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * k + m]; yv[m] = A.y[4 * n + m]; }
-    const bool f64 = mixed && fp64_assembly(xv, yv);
+    const bool f64 = mixed && fp64_assembly(xv, yv, near2, orig2);
     Sink sk;
     sk.f = nullptr;
     sk.d = A.rec + r * REC;
@@ -1549,11 +1559,26 @@ __global__ void __launch_bounds__(256) l0_asm_kernel(DevMaps M, L0Args A, size_t
   }
 }
 
-/* sum_i K_i Pi_i of one pair, lane-partial: FP64 when the pair was assembled
-   in FP64, else float products with the float per-site / per-x terms */
+/* exact double value of a float by integer bit manipulation (zero and
+   subnormal floats give zero), so the mixed form spends no FP64-pipe
+   conversions on its float components */
+__device__ __forceinline__ double f2d_exact(float f)
+{
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  return e == 0 ? 0.0 : __hiloint2double((int)hi, (int)(u << 29));
+}
+
+/* sum_i K_i Pi_i of one pair, lane-partial.  FP64 when the pair was
+   assembled in FP64.  Otherwise the float components plus the per-site and
+   per-x terms as float (hi, lo) pairs: the hi parts are added in float,
+   where L1..L3's near-cancelling terms subtract exactly, and each component
+   enters an FP64 product with Pi, so neither Pi nor the sum is rounded to
+   float; the lo parts go through a float accumulator. */
 __device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool perm, bool t64,
                                            const double *pi, const double *ky, const double *bx,
-                                           const float *ky32, const float *bx32, int lane)
+                                           const float2 *ky2, const float2 *bx2, int lane)
 {
   if (t64 || !live) {
     double acc = 0.0;
@@ -1568,16 +1593,19 @@ __device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool per
     return acc;
   }
   const float *tb = reinterpret_cast<const float *>(L.tbuf);
-  float acc = 0.0f;
+  double acc = 0.0;
+  float accl = 0.0f;
 #pragma unroll
   for (int r = 0; r < 12; r++) {
     const int i = r * 32 + lane;
-    float kv = perm ? -tb[mulam(i)] : tb[i];
-    if (ky32) kv += __ldg(ky32 + i);
-    if (bx32) kv += __ldg(bx32 + i);
-    acc = fmaf(kv, d2f_round(__ldg(pi + i)), acc);
+    float kh = perm ? -tb[mulam(i)] : tb[i], kl = 0.0f;
+    if (ky2) { const float2 q = __ldg(ky2 + i); kh += q.x; kl += q.y; }
+    if (bx2) { const float2 q = __ldg(bx2 + i); kh += q.x; kl += q.y; }
+    const double p = __ldg(pi + i);
+    acc = fma(f2d_exact(kh), p, acc);
+    if (ky2 || bx2) accl = fmaf(kl, d2f_round(p), accl);
   }
-  return (double)acc;
+  return acc + f2d_exact(accl);
 }
 
 /* Fused lattice integrand over units u0 + uu, uu < nu (block per unit, warps
@@ -1605,9 +1633,9 @@ __global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, LatticeArgs
       const double *pi = A.pi + (k * A.ny + n) * 384;
       const double *ky = A.Ky ? A.Ky + n * 384 : nullptr;
       const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
-      const float *ky32 = (f32 && A.Ky32) ? A.Ky32 + n * 384 : nullptr;
-      const float *bx32 = (f32 && A.Bx32) ? A.Bx32 + k * 384 : nullptr;
-      double acc = contract(L, live, perm, t64, pi, ky, bx, ky32, bx32, lane);
+      const float2 *ky2 = (f32 && A.Ky2) ? A.Ky2 + n * 384 : nullptr;
+      const float2 *bx2 = (f32 && A.Bx2) ? A.Bx2 + k * 384 : nullptr;
+      double acc = contract(L, live, perm, t64, pi, ky, bx, ky2, bx2, lane);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
       kadd(s, c, acc);
@@ -1625,16 +1653,27 @@ __global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, LatticeArgs
   }
 }
 
-__global__ void reduce_partials_kernel(const double *partial, size_t nx, int tiles, double *sums)
+/* sums[k] = compensated sum of partial[k][*]: block per x, thread j takes
+   tiles j, j + 256, ...; the 256 thread sums are then added in thread order,
+   so the result does not depend on scheduling */
+__global__ void __launch_bounds__(256) reduce_partials_kernel(const double *partial, int tiles,
+                                                              double *sums)
 {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nx) return;
+  __shared__ double ss[256], cc[256];
+  const size_t k = blockIdx.x;
   double s = 0.0, c = 0.0;
-  for (int t = 0; t < tiles; t++) {
+  for (int t = threadIdx.x; t < tiles; t += blockDim.x) {
     kadd(s, c, partial[(k * tiles + t) * 2 + 0]);
     c += partial[(k * tiles + t) * 2 + 1];
   }
-  sums[k] = s + c;
+  ss[threadIdx.x] = s;
+  cc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bs = 0.0, bc = 0.0;
+    for (int j = 0; j < (int)blockDim.x; j++) { kadd(bs, bc, ss[j]); bc += cc[j]; }
+    sums[k] = bs + bc;
+  }
 }
 
 __global__ void axpy_kernel(double *y, const double *x, double a, size_t n)
@@ -1710,6 +1749,18 @@ static cudaError_t prep_kernel_smem(const void *fn, size_t bytes)
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+static double near2_of(const LaunchCfg &cfg)
+{
+  const double r = cfg.near_ratio > 0 ? cfg.near_ratio : 4.0;
+  return r * r;
+}
+
+static double orig2_of(const LaunchCfg &cfg)
+{
+  const double r = cfg.origin_radius >= 0 ? cfg.origin_radius : 0.35;
+  return r * r;
+}
+
 static int asm_warps(const LaunchCfg &cfg)
 {
   return cfg.warps_per_block > 0 ? std::min(cfg.warps_per_block, 8) : 8;
@@ -1737,7 +1788,8 @@ static cudaError_t launch_l0_t(const DevTables &T, const DevMaps &M, const L0Arg
   const int mixed = sizeof(S) == 4;
   for (size_t p0 = 0; p0 < a.n; p0 += a.rec_cap) {
     const size_t np = std::min(a.rec_cap, a.n - p0);
-    l0_rec_kernel<SI><<<rec_grid(l0_rec_kernel<SI>, np), 64, 0, s>>>(T, a, p0, np, mixed);
+    l0_rec_kernel<SI><<<rec_grid(l0_rec_kernel<SI>, np), 64, 0, s>>>(T, a, p0, np, mixed,
+                                                                     near2_of(cfg), orig2_of(cfg));
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
     blocks = std::min(blocks, (np + wpb - 1) / wpb);
@@ -1776,8 +1828,8 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
   const size_t cu = a.rec_cap / kTile;
   for (size_t u0 = 0; u0 < units; u0 += cu) {
     const size_t nu = std::min(cu, units - u0);
-    lattice_rec_kernel<SI><<<rec_grid(lattice_rec_kernel<SI>, nu * kTile), 64, 0, s>>>(T, a, u0, nu,
-                                                                                        mixed);
+    lattice_rec_kernel<SI><<<rec_grid(lattice_rec_kernel<SI>, nu * kTile), 64, 0, s>>>(
+        T, a, u0, nu, mixed, near2_of(cfg), orig2_of(cfg));
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
     blocks = std::min(blocks, nu);
@@ -1824,17 +1876,21 @@ cudaError_t launch_build_columns32(const DevTables &T, const double *xs, size_t 
   return launch_build_columns_t<float>(T, xs, nx, col, s);
 }
 
-__global__ void to_float_kernel(const double *in, float *out, size_t n)
+/* out[i] = (hi, lo): hi = float(in[i]), lo = float(in[i] - hi) */
+__global__ void to_float2_kernel(const double *in, float2 *out, size_t n)
 {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = (float)in[i];
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double v = in[i];
+    const float hi = (float)v;
+    out[i] = make_float2(hi, (float)(v - (double)hi));
+  }
 }
 
-cudaError_t launch_to_float(const double *in, float *out, size_t n, cudaStream_t s)
+cudaError_t launch_to_float2(const double *in, float2 *out, size_t n, cudaStream_t s)
 {
   if (n == 0) return cudaSuccess;
   const size_t b = min((n + 255) / 256, (size_t)num_sms() * 8);
-  to_float_kernel<<<(unsigned)b, 256, 0, s>>>(in, out, n);
+  to_float2_kernel<<<(unsigned)b, 256, 0, s>>>(in, out, n);
   g_launches++;
   return cudaGetLastError();
 }
@@ -1843,7 +1899,7 @@ cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, 
                                    cudaStream_t s)
 {
   if (nx == 0) return cudaSuccess;
-  reduce_partials_kernel<<<(unsigned)((nx + 127) / 128), 128, 0, s>>>(partial, nx, tiles, sums);
+  reduce_partials_kernel<<<(unsigned)nx, 256, 0, s>>>(partial, tiles, sums);
   g_launches++;
   return cudaGetLastError();
 }

@@ -57,18 +57,20 @@ extern "C" uint64_t kqed_launch_count(void) { return kqed::g_launches; }
 
 /* ------------------------------------------------------ kernel timing */
 
-/* CUDA events recorded on the launching stream around every main kernel
-   (the fused lattice kernel and the batched L0 kernel) while enabled */
+/* CUDA events recorded on the launching stream around every main launch
+   (the lattice and batched-L0 kernel pairs; kind 0) and around the chunk
+   copies of the host entry points (kind 1) while enabled */
 namespace {
-struct TimedLaunch { cudaEvent_t a, b; };
+struct TimedLaunch { cudaEvent_t a, b; int kind; };
 std::mutex g_prof_mu;
 std::vector<TimedLaunch> g_prof;
 std::atomic<int> g_prof_on{0};
 } // namespace
 
-static void prof_begin(cudaStream_t s, TimedLaunch &tl)
+static void prof_begin(cudaStream_t s, TimedLaunch &tl, int kind = 0)
 {
   tl.a = tl.b = nullptr;
+  tl.kind = kind;
   if (!g_prof_on) return;
   cudaEventCreate(&tl.a);
   cudaEventCreate(&tl.b);
@@ -91,19 +93,32 @@ extern "C" void kqed_profile(int enable)
   g_prof_on = enable ? 1 : 0;
 }
 
-extern "C" int kqed_profile_read(double *total_ms, uint64_t *launches)
+static int profile_sum(int kind, double *total_ms, uint64_t *count)
 {
   std::lock_guard<std::mutex> g(g_prof_mu);
   double tot = 0;
+  uint64_t n = 0;
   for (auto &t : g_prof) {
+    if (t.kind != kind) continue;
     if (cudaEventSynchronize(t.b) != cudaSuccess) return fail("event sync failed");
     float ms = 0;
     cudaEventElapsedTime(&ms, t.a, t.b);
     tot += ms;
+    n++;
   }
   *total_ms = tot;
-  *launches = g_prof.size();
+  *count = n;
   return 0;
+}
+
+extern "C" int kqed_profile_read(double *total_ms, uint64_t *launches)
+{
+  return profile_sum(0, total_ms, launches);
+}
+
+extern "C" int kqed_profile_read_copies(double *total_ms, uint64_t *copies)
+{
+  return profile_sum(1, total_ms, copies);
 }
 
 extern "C" int kqed_fp64_peak_gflops(double *gflops)
@@ -147,7 +162,7 @@ struct Ctx {
   int device = 0;
   DevTables T{};
   DevMaps M{};
-  LaunchCfg cfg{8, 0};
+  LaunchCfg cfg{8, 0, 4.0, 0.35};
   std::vector<void *> allocs;
 };
 
@@ -454,6 +469,10 @@ static int setup_device(struct Grid_coeffs *G, Ctx *c)
   const char *blk = getenv("KQED_BLOCKS");
   if (wpb) c->cfg.warps_per_block = std::max(1, std::min(8, atoi(wpb)));
   if (blk) c->cfg.blocks = std::max(0, atoi(blk));
+  const char *nr = getenv("KQED_MIXED_NEAR");
+  if (nr) c->cfg.near_ratio = std::max(1.0, std::min(64.0, atof(nr)));
+  const char *orr = getenv("KQED_MIXED_ORIGIN");
+  if (orr) c->cfg.origin_radius = std::max(0.0, std::min(10.0, atof(orr)));
   return 0;
 }
 
@@ -763,7 +782,8 @@ struct LatticeRun {
   const double *d_x, *d_y;
   size_t nx, ny;
   double *Ky, *Bx, *partial, *col, *rec;
-  float *Ky32, *Bx32, *col32;
+  float2 *Ky2, *Bx2;
+  float *col32;
   uint8_t *code;
   size_t rec_cap;
   int tiles, precision, variant;
@@ -775,7 +795,8 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
 {
   R.c = c; R.d_x = d_x; R.d_y = d_y; R.nx = nx; R.ny = ny; R.precision = precision;
   R.variant = variant;
-  R.Ky32 = R.Bx32 = R.col32 = nullptr;
+  R.Ky2 = R.Bx2 = nullptr;
+  R.col32 = nullptr;
   R.col = nullptr;
   R.tiles = (int)((ny + kTile - 1) / kTile);
   /* records first: the kernel-term launches below reuse the same scratch */
@@ -792,18 +813,19 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   if (!R.col) return fail("out of device memory for x-column tables");
   CUDA_OK(launch_build_columns(c->T, d_x, nx, R.col, s));
   if (mixed) {
-    const size_t n32 = ncol + (R.Ky ? (ny + nx) * 384 : 0);
+    /* ncol floats (an even count: kRow = 28 per row), then the float2 terms */
+    const size_t n32 = ncol + (R.Ky ? (ny + nx) * 384 * 2 : 0);
     float *b32 = reinterpret_cast<float *>(st.d_col32.get(n32 / 2 + 2));
     if (!b32) return fail("out of device memory for float tables");
     R.col32 = b32;
     b32 += ncol;
     CUDA_OK(launch_build_columns32(c->T, d_x, nx, R.col32, s));
     if (R.Ky) {
-      /* the FP64-evaluated per-site / per-x terms, as float */
-      R.Ky32 = b32;
-      R.Bx32 = R.Ky32 + ny * 384;
-      CUDA_OK(launch_to_float(R.Ky, R.Ky32, ny * 384, s));
-      CUDA_OK(launch_to_float(R.Bx, R.Bx32, nx * 384, s));
+      /* the FP64-evaluated per-site / per-x terms, as float (hi, lo) pairs */
+      R.Ky2 = reinterpret_cast<float2 *>(b32);
+      R.Bx2 = R.Ky2 + ny * 384;
+      CUDA_OK(launch_to_float2(R.Ky, R.Ky2, ny * 384, s));
+      CUDA_OK(launch_to_float2(R.Bx, R.Bx2, nx * 384, s));
     }
   }
   return 0;
@@ -819,7 +841,7 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
                 R.Ky, R.Bx ? R.Bx + 384 * x0 : nullptr,
                 R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1), R.tiles,
                 R.col ? R.col + per_x * x0 : nullptr,
-                R.Ky32, R.Bx32 ? R.Bx32 + 384 * x0 : nullptr,
+                R.Ky2, R.Bx2 ? R.Bx2 + 384 * x0 : nullptr,
                 R.col32 ? R.col32 + per_x * x0 : nullptr, R.rec, R.code, R.rec_cap};
   TimedLaunch tl;
   prof_begin(s, tl);
@@ -885,8 +907,11 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
     const int b = (int)(ch & 1);
     const size_t x0 = ch * nxc, n = std::min(nxc, nx - x0);
     if (ch >= 2) CUDA_OK(cudaStreamWaitEvent(cs, st.ev_free[b], 0));
+    TimedLaunch tc;
+    prof_begin(cs, tc, 1);
     CUDA_OK(cudaMemcpyAsync(slot[b], pi + x0 * per_x, n * per_x * sizeof(double),
                             cudaMemcpyHostToDevice, cs));
+    prof_end(cs, tc);
     CUDA_OK(cudaEventRecord(st.ev_copied[b], cs));
     CUDA_OK(cudaStreamWaitEvent(s, st.ev_copied[b], 0));
     if (lattice_launch(R, x0, n, slot[b], s)) return 1;

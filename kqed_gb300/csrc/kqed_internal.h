@@ -74,8 +74,10 @@ struct DevMaps {
 
 /* Launch parameters chosen by the host (and the autotuner). */
 struct LaunchCfg {
-  int warps_per_block;
-  int blocks;
+  int warps_per_block;   /* assembly kernels */
+  int blocks;            /* assembly grid (0: occupancy-derived persistent grid) */
+  double near_ratio;     /* mixed form: FP64 assembly when |x-y| < max(|x|,|y|)/near_ratio */
+  double origin_radius;  /* mixed form: FP64 assembly when max(|x|,|y|) < origin_radius */
 };
 
 /* Batched L0: out[i][384] for the pairs (x[i], y[i]). */
@@ -99,7 +101,8 @@ struct LatticeArgs {
   double *partial;      /* [nx][tiles][2]  (sum, compensation) */
   int tiles;            /* site tiles per x: ceil(ny / kTile) */
   const double *col;    /* per-x column tables [nx][nstpy][NK][kRow] or NULL */
-  const float *Ky32, *Bx32, *col32;   /* the same in float, for the mixed form */
+  const float2 *Ky2, *Bx2;   /* Ky, Bx as float (hi, lo) pairs, for the mixed form */
+  const float *col32;        /* column tables in float, for the mixed form */
   double *rec;          /* record scratch [rec_cap][kRec] */
   uint8_t *code;        /* [rec_cap] */
   size_t rec_cap;       /* pairs per record kernel launch (a multiple of kTile) */
@@ -118,7 +121,7 @@ cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &
                             const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                  const LaunchCfg &cfg, cudaStream_t s);
-cudaError_t launch_to_float(const double *in, float *out, size_t n, cudaStream_t s);
+cudaError_t launch_to_float2(const double *in, float2 *out, size_t n, cudaStream_t s);
 cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,
                                    cudaStream_t s);
 cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStream_t s);
