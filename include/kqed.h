@@ -157,6 +157,22 @@ const char *kqed_last_error(void);
 /* Number of this library's GPU kernels launched so far by this process. */
 uint64_t kqed_launch_count(void);
 
+/* Error of the mixed-precision form against the plain FP64 form on n pairs
+   (device buffers d_x, d_y [n][4]), accumulated on the device; no reference
+   counterpart.  For every pair with a nonzero kernel, norm = max_c |L_c|
+   (FP64 form) and r_c = |L_c(mixed) - L_c(FP64)| / max(norm, floor_abs).
+   On return (host buffer of KQED_STATS_LEN doubles):
+     stats[c]        max over pairs of r_c,          c = 0..383
+     stats[384 + c]  root mean square over pairs of r_c
+     stats[768]      max over pairs of max_c r_c
+     stats[769]      mean over pairs of max_c r_c
+     stats[770]      number of pairs counted
+   Runs on `stream` and synchronises it before returning. */
+#define KQED_STATS_LEN 771
+int kqed_precision_stats(const struct QED_kernel_temps *t, int variant, size_t n,
+                         const double *d_x, const double *d_y, double floor_abs, double *stats,
+                         void *stream);
+
 /* Diagnostics.  kqed_profile(1) starts recording CUDA events on the
    launching stream around every main launch (the record + assembly kernel
    pair of the lattice sums and of the batched L0) and around every Pi chunk

@@ -101,6 +101,9 @@ def lib():
         L.kqed_profile_read.restype = ctypes.c_int
         L.kqed_profile_read_copies.argtypes = [dp, ctypes.POINTER(ctypes.c_uint64)]
         L.kqed_profile_read_copies.restype = ctypes.c_int
+        L.kqed_precision_stats.argtypes = [T, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_double, dp, ctypes.c_void_p]
+        L.kqed_precision_stats.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
         L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
@@ -245,6 +248,17 @@ def launch_count():
 def profile(enable):
     """Start (True) or stop (False) event timing of the main kernels."""
     lib().kqed_profile(1 if enable else 0)
+
+
+def precision_stats(t, variant, x_ptr, y_ptr, n, floor=1e-300, stream=None):
+    """Error of the mixed form against the FP64 form of L<variant> on n device
+    pairs, accumulated on the device (kqed_precision_stats): a dict with
+    per-component max and RMS of the norm-relative error, the pair-level max
+    and mean, and the number of pairs counted."""
+    out = np.zeros(771)
+    _check(lib().kqed_precision_stats(t.ptr, variant, n, x_ptr, y_ptr, floor, _dptr(out), stream))
+    return {"comp_max": out[:384].copy(), "comp_rms": out[384:768].copy(),
+            "pair_max": float(out[768]), "pair_mean": float(out[769]), "pairs": int(out[770])}
 
 
 def profile_read():

@@ -1876,6 +1876,75 @@ cudaError_t launch_build_columns32(const DevTables &T, const double *xs, size_t 
   return launch_build_columns_t<float>(T, xs, nx, col, s);
 }
 
+/* Error statistics of a kernel batch B against a reference batch A (both
+   [m][384]): warp per pair, lane l owns components r*32 + l.  Per pair
+   norm = max_c |A_c|; r_c = |B_c - A_c| / max(norm, floor).  acc[0..383]
+   per-component max r_c, acc[384..767] per-component sum of r_c^2,
+   acc[768] max over pairs of max_c r_c, acc[769] sum of that, acc[770]
+   pairs counted (norm > 0 or B nonzero). */
+__global__ void __launch_bounds__(256) stats_kernel(const double *A, const double *B, size_t m,
+                                                    double floor_abs, double *acc)
+{
+  const int lane = threadIdx.x & 31;
+  const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
+  double mx[12], sq[12], pmax = 0.0, psum = 0.0, cnt = 0.0;
+#pragma unroll
+  for (int r = 0; r < 12; r++) { mx[r] = 0.0; sq[r] = 0.0; }
+  for (size_t p = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < m; p += warps) {
+    double a[12], d[12], nrm = 0.0, bn = 0.0;
+#pragma unroll
+    for (int r = 0; r < 12; r++) {
+      a[r] = A[p * 384 + r * 32 + lane];
+      const double b = B[p * 384 + r * 32 + lane];
+      d[r] = fabs(b - a[r]);
+      nrm = fmax(nrm, fabs(a[r]));
+      bn = fmax(bn, fabs(b));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      nrm = fmax(nrm, __shfl_xor_sync(0xffffffffu, nrm, off));
+      bn = fmax(bn, __shfl_xor_sync(0xffffffffu, bn, off));
+    }
+    if (nrm == 0.0 && bn == 0.0) continue;
+    const double inv = 1.0 / fmax(nrm, floor_abs);
+    double pm = 0.0;
+#pragma unroll
+    for (int r = 0; r < 12; r++) {
+      const double e = d[r] * inv;
+      mx[r] = fmax(mx[r], e);
+      sq[r] = fma(e, e, sq[r]);
+      pm = fmax(pm, e);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) pm = fmax(pm, __shfl_xor_sync(0xffffffffu, pm, off));
+    pmax = fmax(pmax, pm);
+    psum += pm;
+    cnt += 1.0;
+  }
+  unsigned long long *amx = reinterpret_cast<unsigned long long *>(acc);
+#pragma unroll
+  for (int r = 0; r < 12; r++) {
+    const int c = r * 32 + lane;
+    if (mx[r] > 0.0) atomicMax(amx + c, (unsigned long long)__double_as_longlong(mx[r]));
+    if (sq[r] > 0.0) atomicAdd(acc + 384 + c, sq[r]);
+  }
+  if (lane == 0 && cnt > 0.0) {
+    atomicMax(amx + 768, (unsigned long long)__double_as_longlong(pmax));
+    atomicAdd(acc + 769, psum);
+    atomicAdd(acc + 770, cnt);
+  }
+}
+
+cudaError_t launch_stats(const double *A, const double *B, size_t m, double floor_abs, double *acc,
+                         cudaStream_t s)
+{
+  if (m == 0) return cudaSuccess;
+  const size_t b = std::min((m + 7) / 8, (size_t)num_sms() * 8);
+  stats_kernel<<<(unsigned)b, 256, 0, s>>>(A, B, m, floor_abs, acc);
+  g_launches++;
+  return cudaGetLastError();
+}
+
 /* out[i] = (hi, lo): hi = float(in[i]), lo = float(in[i] - hi) */
 __global__ void to_float2_kernel(const double *in, float2 *out, size_t n)
 {

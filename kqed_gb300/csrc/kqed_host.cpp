@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdarg>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -172,7 +173,7 @@ struct ThreadStage {
   cudaStream_t stream = nullptr, copy_stream = nullptr;
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double *h_pin = nullptr;   /* 8 + 384 doubles */
-  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32, d_rec;
+  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32, d_rec, d_sa, d_sb;
   ~ThreadStage() { reset(); }
   void reset()
   {
@@ -186,7 +187,7 @@ struct ThreadStage {
     copy_stream = nullptr;
     if (h_pin) cudaFreeHost(h_pin);
     d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release(); d_col.release(); d_col32.release();
-    d_rec.release();
+    d_rec.release(); d_sa.release(); d_sb.release();
     stream = nullptr;
     h_pin = nullptr;
     owner = nullptr;
@@ -645,6 +646,53 @@ extern "C" int kqed_kernel_batch_dev(const struct QED_kernel_temps *t, int varia
   const int rc = run_variant(c, variant, d_x, d_y, n, d_kerv, d_status, (cudaStream_t)stream, stage_for(c));
   tl_precision = KQED_FP64;
   return rc;
+}
+
+/* Error of the mixed form against the FP64 form, accumulated on the device:
+   both forms of L<variant> are evaluated on chunks of pairs and compared by
+   stats_kernel; only the 771 accumulators come back to the host. */
+extern "C" int kqed_precision_stats(const struct QED_kernel_temps *t, int variant, size_t n,
+                                    const double *d_x, const double *d_y, double floor_abs,
+                                    double *stats, void *stream)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (check_variant_precision(variant, KQED_FP64)) return 1;
+  if (!stats) return fail("null buffer");
+  for (int i = 0; i < KQED_STATS_LEN; i++) stats[i] = 0.0;
+  if (n == 0) return 0;
+  if (!d_x || !d_y) return fail("null buffer");
+  if (!(floor_abs > 0.0)) return fail("floor must be positive");
+  cudaStream_t s = (cudaStream_t)stream;
+  ThreadStage &st = stage_for(c);
+  const size_t chunk = std::min(n, (size_t)1 << 18);
+  double *A = st.d_sa.get(chunk * 384 + 771);
+  double *B = st.d_sb.get(chunk * 384);
+  if (!A || !B) return fail("out of device memory for %zu-pair statistics chunks", chunk);
+  double *acc = A + chunk * 384;
+  CUDA_OK(cudaMemsetAsync(acc, 0, 771 * sizeof(double), s));
+  for (size_t p0 = 0; p0 < n; p0 += chunk) {
+    const size_t m = std::min(chunk, n - p0);
+    tl_precision = KQED_FP64;
+    int bad = run_variant(c, variant, d_x + 4 * p0, d_y + 4 * p0, m, A, nullptr, s, st);
+    tl_precision = KQED_FP32_MIXED;
+    bad = bad || run_variant(c, variant, d_x + 4 * p0, d_y + 4 * p0, m, B, nullptr, s, st);
+    tl_precision = KQED_FP64;
+    if (bad) return 1;
+    CUDA_OK(launch_stats(A, B, m, floor_abs, acc, s));
+  }
+  double h[771];
+  CUDA_OK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s));
+  CUDA_OK(cudaStreamSynchronize(s));
+  const double cnt = h[770];
+  for (int i = 0; i < 384; i++) {
+    stats[i] = h[i];
+    stats[384 + i] = cnt > 0 ? std::sqrt(h[384 + i] / cnt) : 0.0;
+  }
+  stats[768] = h[768];
+  stats[769] = cnt > 0 ? h[769] / cnt : 0.0;
+  stats[770] = cnt;
+  return 0;
 }
 
 extern "C" int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, size_t n,

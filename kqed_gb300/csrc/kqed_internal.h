@@ -122,6 +122,8 @@ cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &
 cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                  const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_to_float2(const double *in, float2 *out, size_t n, cudaStream_t s);
+cudaError_t launch_stats(const double *A, const double *B, size_t m, double floor_abs, double *acc,
+                         cudaStream_t s);
 cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,
                                    cudaStream_t s);
 cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStream_t s);
