@@ -143,7 +143,8 @@ int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t n
    scratch comes from a static 16 MiB device array compiled into the library
    (held by every GPU that loads it), so problems needing more scratch are
    rejected with an error: nx * ceil(ny / 64) * 2 doubles, plus, for L1..L3,
-   388 * ny + 772 * nx doubles, must not exceed 2,097,152.  The first call on
+   388 * ny + 772 * nx doubles, plus one tile of pair records (64 * 88 + 8
+   doubles), must not exceed 2,097,152.  The first call on
    a device looks up the array's device address; make it before any stream
    capture.  Calls share the array: calls that overlap on the GPU race and
    must be serialised by the caller.  Allocates nothing. */
@@ -151,11 +152,69 @@ int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int variant, size
                              const double *d_x, size_t ny, const double *d_y, const double *d_pi,
                              double *d_sums, void *stream);
 
+/* Synthetic Pi for benchmark lattices too large to hold Pi in memory (no
+   reference counterpart; the reference's callers supply Pi).  Component c
+   of Pi(x_k, y_n), k the index of x in d_x, is
+     g * exp(-(|y_n| + |x_k - y_n|) / 2),
+     g = (b0 + b1 + b2 + b3 - 510) * sqrt(3) / 256,
+   b0..b3 the bytes of word (c >> 5) & 3 of Philox-4x32-10 with key seed
+   (low word first) and counter (n, k, (c & 31) + 32 * (c >> 7), stream_id):
+   mean 0, variance 1 - 2^-16.
+   kqed_lattice_sum_synth: the fused lattice sum with this Pi generated inside
+   the kernel (nothing of Pi is stored); otherwise as kqed_lattice_sum_dev.
+   kqed_pi_synth_dev: the same Pi written to d_pi [nx][ny][384]. */
+int kqed_lattice_sum_synth(const struct QED_kernel_temps *t, int variant, size_t nx,
+                           const double *d_x, size_t ny, const double *d_y, uint64_t seed,
+                           uint32_t stream_id, double *d_sums, int precision, void *stream);
+int kqed_pi_synth_dev(size_t nx, const double *d_x, size_t ny, const double *d_y, uint64_t seed,
+                      uint32_t stream_id, double *d_pi, void *stream);
+
 /* Message of the last error on the calling thread ("" if none). */
 const char *kqed_last_error(void);
 
 /* Number of this library's GPU kernels launched so far by this process. */
 uint64_t kqed_launch_count(void);
+
+/* Batched lattices (no reference counterpart): many fused lattice sums as
+   one work list, captured once in a CUDA graph and replayed.
+   kqed_batch_plan_create allocates everything the batch needs, runs it once
+   (with tune != 0 it first times candidate launch parameters -- assembly
+   warps per block, assembly grid, record chunk -- on this batch and keeps
+   the fastest, remembered per device, precision and batch size), then
+   captures the batch -- column tables, kernel terms, the record and
+   assembly kernels over all jobs' units, the per-job reductions -- in a CUDA
+   graph.  kqed_batch_plan_launch replays the graph on `stream`: each job's
+   d_sums[k] = sum_y L<variant>(x_k, y).Pi(x_k, y) for the current contents
+   of its buffers (the pointers are fixed at creation).  A job's d_pi NULL
+   selects the generated Pi of kqed_lattice_sum_synth with its
+   (pi_seed, pi_stream). */
+struct kqed_lattice_job {
+  int variant;            /* 0..3 */
+  size_t nx, ny;
+  const double *d_x;      /* [nx][4] device */
+  const double *d_y;      /* [ny][4] device */
+  const double *d_pi;     /* [nx][ny][384] device, or NULL (generated) */
+  uint64_t pi_seed;
+  uint32_t pi_stream;
+  double *d_sums;         /* [nx] device */
+};
+struct kqed_batch_info {
+  int jobs;
+  size_t units;           /* (x, 64-site tile) work units of the batch */
+  size_t pairs;           /* (x, y) evaluations per launch */
+  int warps_per_block;    /* launch parameters in the graph */
+  int blocks;             /* 0: one persistent grid at full occupancy */
+  size_t record_chunk_pairs;
+  size_t graph_kernels;   /* kernel nodes in the graph */
+  double tuned_ms;        /* best time of the main kernels while tuning, or 0 */
+};
+typedef struct kqed_batch_plan kqed_batch_plan;
+int kqed_batch_plan_create(const struct QED_kernel_temps *t, int njobs,
+                           const struct kqed_lattice_job *jobs, int precision, int tune,
+                           kqed_batch_plan **plan);
+int kqed_batch_plan_launch(kqed_batch_plan *plan, void *stream);
+int kqed_batch_plan_info(const kqed_batch_plan *plan, struct kqed_batch_info *info);
+void kqed_batch_plan_destroy(kqed_batch_plan *plan);
 
 /* Error of the mixed-precision form against the plain FP64 form on n pairs
    (device buffers d_x, d_y [n][4]), accumulated on the device; no reference

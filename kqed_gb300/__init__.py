@@ -58,6 +58,22 @@ class QED_kernel_temps(ctypes.Structure):
 _lib = None
 
 
+class LatticeJob(ctypes.Structure):
+    """struct kqed_lattice_job of include/kqed.h"""
+    _fields_ = [("variant", ctypes.c_int), ("nx", ctypes.c_size_t), ("ny", ctypes.c_size_t),
+                ("d_x", ctypes.c_void_p), ("d_y", ctypes.c_void_p), ("d_pi", ctypes.c_void_p),
+                ("pi_seed", ctypes.c_uint64), ("pi_stream", ctypes.c_uint32),
+                ("d_sums", ctypes.c_void_p)]
+
+
+class BatchInfo(ctypes.Structure):
+    """struct kqed_batch_info of include/kqed.h"""
+    _fields_ = [("jobs", ctypes.c_int), ("units", ctypes.c_size_t), ("pairs", ctypes.c_size_t),
+                ("warps_per_block", ctypes.c_int), ("blocks", ctypes.c_int),
+                ("record_chunk_pairs", ctypes.c_size_t), ("graph_kernels", ctypes.c_size_t),
+                ("tuned_ms", ctypes.c_double)]
+
+
 def lib():
     """The loaded C-ABI library (raises if it has not been built)."""
     global _lib
@@ -104,6 +120,25 @@ def lib():
         L.kqed_precision_stats.argtypes = [T, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_double, dp, ctypes.c_void_p]
         L.kqed_precision_stats.restype = ctypes.c_int
+        L.kqed_lattice_sum_synth.argtypes = [T, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
+                                             ctypes.c_size_t, ctypes.c_void_p, ctypes.c_uint64,
+                                             ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_void_p]
+        L.kqed_lattice_sum_synth.restype = ctypes.c_int
+        L.kqed_pi_synth_dev.argtypes = [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                        ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                        ctypes.c_void_p, ctypes.c_void_p]
+        L.kqed_pi_synth_dev.restype = ctypes.c_int
+        L.kqed_batch_plan_create.argtypes = [T, ctypes.c_int, ctypes.POINTER(LatticeJob),
+                                             ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p)]
+        L.kqed_batch_plan_create.restype = ctypes.c_int
+        L.kqed_batch_plan_launch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.kqed_batch_plan_launch.restype = ctypes.c_int
+        L.kqed_batch_plan_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchInfo)]
+        L.kqed_batch_plan_info.restype = ctypes.c_int
+        L.kqed_batch_plan_destroy.argtypes = [ctypes.c_void_p]
+        L.kqed_batch_plan_destroy.restype = None
         L.kqed_fp64_peak_gflops.argtypes = [dp]
         L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
@@ -248,6 +283,54 @@ def launch_count():
 def profile(enable):
     """Start (True) or stop (False) event timing of the main kernels."""
     lib().kqed_profile(1 if enable else 0)
+
+
+def lattice_sum_synth(t, variant, x_ptr, nx, y_ptr, ny, seed, sums_ptr, precision=KQED_FP64,
+                      stream_id=0, stream=None):
+    """Fused lattice sum with the synthetic Pi generated inside the kernel
+    (kqed_lattice_sum_synth); device pointers."""
+    _check(lib().kqed_lattice_sum_synth(t.ptr, variant, nx, x_ptr, ny, y_ptr, seed, stream_id,
+                                        sums_ptr, precision, stream))
+
+
+def pi_synth_dev(x_ptr, nx, y_ptr, ny, seed, pi_ptr, stream_id=0, stream=None):
+    """The synthetic Pi of lattice_sum_synth written to pi_ptr [nx][ny][384]."""
+    _check(lib().kqed_pi_synth_dev(nx, x_ptr, ny, y_ptr, seed, stream_id, pi_ptr, stream))
+
+
+class BatchPlan:
+    """A batch of fused lattice sums captured in one CUDA graph
+    (kqed_batch_plan_*).  jobs: dicts with variant, nx, ny, d_x, d_y, d_pi
+    (or None: generated Pi), pi_seed, pi_stream, d_sums (device pointers)."""
+
+    def __init__(self, t, jobs, precision=KQED_FP64, tune=False):
+        arr = (LatticeJob * len(jobs))()
+        for i, j in enumerate(jobs):
+            arr[i] = LatticeJob(j["variant"], j["nx"], j["ny"], j["d_x"], j["d_y"],
+                                j.get("d_pi") or None, j.get("pi_seed", 0), j.get("pi_stream", 0),
+                                j["d_sums"])
+        self._h = ctypes.c_void_p()
+        _check(lib().kqed_batch_plan_create(t.ptr, len(jobs), arr, precision, 1 if tune else 0,
+                                            ctypes.byref(self._h)))
+
+    def launch(self, stream=None):
+        _check(lib().kqed_batch_plan_launch(self._h, stream))
+
+    def info(self):
+        i = BatchInfo()
+        _check(lib().kqed_batch_plan_info(self._h, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in BatchInfo._fields_}
+
+    def close(self):
+        if self._h:
+            lib().kqed_batch_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def precision_stats(t, variant, x_ptr, y_ptr, n, floor=1e-300, stream=None):

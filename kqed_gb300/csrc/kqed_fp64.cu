@@ -34,6 +34,8 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 namespace kqed {
 
@@ -1356,6 +1358,54 @@ __device__ __forceinline__ bool fp64_assembly(const double *xv, const double *yv
   return xx < 1E-28 || yy < 1E-28 || dd < 1E-28 || near2 * dd < mm || mm < orig2;
 }
 
+/* ---------------------------------------------- synthetic Pi (generated) */
+
+/* Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter c, key (k0, k1) */
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+    const uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+/* Standardised sum of the four bytes of w: (b0+b1+b2+b3 - 510) sqrt(3)/256,
+   mean 0, variance 1 - 2^-16, exact in double up to one rounding. */
+__device__ __forceinline__ double pi_normal(uint32_t w)
+{
+  const int s = (int)(w & 0xffu) + (int)((w >> 8) & 0xffu) + (int)((w >> 16) & 0xffu) + (int)(w >> 24);
+  return (double)(s - 510) * 0.0067658234670659265;
+}
+
+/* The 12 Pi components lane `lane` contracts for pair (x index k, site n):
+   component c = r*32 + lane (r = 0..11) is word (c >> 5) & 3 of the Philox
+   call q = (c & 31) + 32 (c >> 7) with counter (n, k, q, stream), key = seed,
+   times env = exp(-(|y| + |x - y|) / 2). */
+__device__ __forceinline__ void pi_generate(uint64_t seed, uint32_t stream, size_t k, size_t n,
+                                            double env, int lane, double pv[12])
+{
+#pragma unroll
+  for (int g = 0; g < 3; g++) {
+    uint32_t c[4] = {(uint32_t)n, (uint32_t)k, (uint32_t)(lane + 32 * g), stream};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+    for (int w = 0; w < 4; w++) pv[4 * g + w] = pi_normal(c[w]) * env;
+  }
+}
+
+__device__ __forceinline__ double pi_envelope(const double *xv, const double *yv)
+{
+  const double d0 = xv[0] - yv[0], d1 = xv[1] - yv[1], d2 = xv[2] - yv[2], d3 = xv[3] - yv[3];
+  const double ny = sqrt(yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3]);
+  const double nd = sqrt(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
+  return exp(-0.5 * (ny + nd));
+}
+
 __device__ __forceinline__ uint8_t pair_code(int kind, bool f64, int status)
 {
   return (uint8_t)(kind | (f64 ? 8 : 0) | (status << 4));
@@ -1385,31 +1435,50 @@ template <typename S> __device__ __forceinline__ const S *column_of(const Lattic
 template <> __device__ __forceinline__ const double *column_of<double>(const LatticeArgs &A) { return A.col; }
 template <> __device__ __forceinline__ const float *column_of<float>(const LatticeArgs &A) { return A.col32; }
 
-/* records of the pairs of lattice units u0 + uu, uu < nu; unit u is
-   (x_k, sites t*kTile .. t*kTile + kTile - 1), k = u / tiles, t = u % tiles;
-   record r = uu * kTile + j */
-template <typename SI>
-__global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, LatticeArgs A, size_t u0,
-                                                         size_t nu, int mixed, double near2,
-                                                         double orig2)
+/* the lattice (job) of unit u: A itself, or in a batch the job whose unit
+   range holds u */
+__device__ __forceinline__ const LatticeArgs &job_of(const LatticeArgs &A,
+                                                     const LatticeArgs *jobs, int njobs, size_t u)
 {
-  const SI *col = column_of<SI>(A);
+  if (njobs == 0) return A;
+  int lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (jobs[mid].u_begin <= u) lo = mid;
+    else hi = mid;
+  }
+  return jobs[lo];
+}
+
+/* records of the pairs of lattice units u0 + uu, uu < nu; unit u of a
+   lattice is (x_k, sites t*kTile .. t*kTile + kTile - 1), k = u' / tiles,
+   t = u' % tiles, u' = u - u_begin; record r = uu * kTile + j */
+template <typename SI>
+__global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __grid_constant__ LatticeArgs A,
+                                                         const LatticeArgs *jobs, int njobs,
+                                                         size_t u0, size_t nu, int mixed,
+                                                         double near2, double orig2)
+{
   const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nu * kTile;
        r += (size_t)gridDim.x * blockDim.x) {
     const size_t u = u0 + r / kTile;
-    const size_t k = u / A.tiles, n = (u % A.tiles) * kTile + r % kTile;
-    if (n >= A.ny) continue;
+    const LatticeArgs &J = job_of(A, jobs, njobs, u);
+    const size_t ul = u - J.u_begin;
+    const size_t k = ul / J.tiles, n = (ul % J.tiles) * kTile + r % kTile;
+    if (n >= J.ny) continue;
     double xv[4], yv[4];
-    for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * k + m]; yv[m] = A.y[4 * n + m]; }
+    for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
     const bool f64 = mixed && fp64_assembly(xv, yv, near2, orig2);
     Sink sk;
     sk.f = nullptr;
     sk.d = A.rec + r * REC;
     int status;
+    const SI *col = column_of<SI>(J);
     const int kind = phase_a<SI>(T, xv, yv, sk, status, col ? col + k * per_x : nullptr,
-                                 A.col ? A.col + k * per_x : nullptr, f64);
+                                 J.col ? J.col + k * per_x : nullptr, f64);
     A.code[r] = pair_code(kind, f64, status);
+    if (!J.pi) A.env[r] = pi_envelope(xv, yv);
   }
 }
 
@@ -1577,8 +1646,9 @@ __device__ __forceinline__ double f2d_exact(float f)
    enters an FP64 product with Pi, so neither Pi nor the sum is rounded to
    float; the lo parts go through a float accumulator. */
 __device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool perm, bool t64,
-                                           const double *pi, const double *ky, const double *bx,
-                                           const float2 *ky2, const float2 *bx2, int lane)
+                                           const double *pi, const double *pv, const double *ky,
+                                           const double *bx, const float2 *ky2, const float2 *bx2,
+                                           int lane)
 {
   if (t64 || !live) {
     double acc = 0.0;
@@ -1588,7 +1658,7 @@ __device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool per
       double kv = live ? kcomp(L, true, perm, i) : 0.0;
       if (ky) kv += __ldg(ky + i);
       if (bx) kv += __ldg(bx + i);
-      acc = fma(kv, __ldg(pi + i), acc);
+      acc = fma(kv, pv ? pv[r] : __ldg(pi + i), acc);
     }
     return acc;
   }
@@ -1601,7 +1671,7 @@ __device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool per
     float kh = perm ? -tb[mulam(i)] : tb[i], kl = 0.0f;
     if (ky2) { const float2 q = __ldg(ky2 + i); kh += q.x; kl += q.y; }
     if (bx2) { const float2 q = __ldg(bx2 + i); kh += q.x; kl += q.y; }
-    const double p = __ldg(pi + i);
+    const double p = pv ? pv[r] : __ldg(pi + i);
     acc = fma(f2d_exact(kh), p, acc);
     if (ky2 || bx2) accl = fmaf(kl, d2f_round(p), accl);
   }
@@ -1612,8 +1682,9 @@ __device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool per
    over its sites): partial[k][t] = (sum, compensation) of the unit's pairs,
    warp sums in site order, block sum in warp order. */
 template <typename S>
-__global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, LatticeArgs A, size_t u0,
-                                                          size_t nu, int wpb)
+__global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, const __grid_constant__ LatticeArgs A,
+                                                          const LatticeArgs *jobs, int njobs,
+                                                          size_t u0, size_t nu, int wpb)
 {
   AsmSmem L = carve_asm(wpb);
   asm_prologue(M, L);
@@ -1622,20 +1693,24 @@ __global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, LatticeArgs
   const bool f32 = sizeof(S) == 4;
   for (size_t uu = blockIdx.x; uu < nu; uu += gridDim.x) {
     const size_t u = u0 + uu;
-    const size_t k = u / A.tiles, t = u % A.tiles;
+    const LatticeArgs &J = job_of(A, jobs, njobs, u);
+    const size_t ul = u - J.u_begin;
+    const size_t k = ul / J.tiles, t = ul % J.tiles;
     double s = 0.0, c = 0.0;
     for (int j = warp; j < kTile; j += wpb) {
       const size_t n = t * kTile + j;
-      if (n >= A.ny) break;
+      if (n >= J.ny) break;
       const size_t r = uu * kTile + j;
       bool perm, t64;
       const bool live = asm_pair<S>(L, M, A.rec + r * REC, A.code[r], lane, perm, t64);
-      const double *pi = A.pi + (k * A.ny + n) * 384;
-      const double *ky = A.Ky ? A.Ky + n * 384 : nullptr;
-      const double *bx = A.Bx ? A.Bx + k * 384 : nullptr;
-      const float2 *ky2 = (f32 && A.Ky2) ? A.Ky2 + n * 384 : nullptr;
-      const float2 *bx2 = (f32 && A.Bx2) ? A.Bx2 + k * 384 : nullptr;
-      double acc = contract(L, live, perm, t64, pi, ky, bx, ky2, bx2, lane);
+      const double *pi = J.pi ? J.pi + (k * J.ny + n) * 384 : nullptr;
+      double pvv[12];
+      if (!J.pi) pi_generate(J.pi_seed, J.pi_stream, J.k0 + k, n, A.env[r], lane, pvv);
+      const double *ky = J.Ky ? J.Ky + n * 384 : nullptr;
+      const double *bx = J.Bx ? J.Bx + k * 384 : nullptr;
+      const float2 *ky2 = (f32 && J.Ky2) ? J.Ky2 + n * 384 : nullptr;
+      const float2 *bx2 = (f32 && J.Bx2) ? J.Bx2 + k * 384 : nullptr;
+      double acc = contract(L, live, perm, t64, pi, J.pi ? nullptr : pvv, ky, bx, ky2, bx2, lane);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
       kadd(s, c, acc);
@@ -1646,8 +1721,8 @@ __global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, LatticeArgs
     if (threadIdx.x == 0) {
       double bs = 0.0, bc = 0.0;
       for (int w2 = 0; w2 < wpb; w2++) { kadd(bs, bc, red_s[w2]); bc += red_c[w2]; }
-      A.partial[(k * A.tiles + t) * 2 + 0] = bs;
-      A.partial[(k * A.tiles + t) * 2 + 1] = bc;
+      J.partial[(k * J.tiles + t) * 2 + 0] = bs;
+      J.partial[(k * J.tiles + t) * 2 + 1] = bc;
     }
     __syncthreads();
   }
@@ -1734,19 +1809,61 @@ static int num_sms()
   return n;
 }
 
+/* Per-device cache of the launch attributes the host queries before a
+   launch (occupancy, dynamic shared-memory opt-in): after the first launch
+   of a kernel shape they cost nothing, and a stream capture records only
+   launches. */
+struct LaunchAttr {
+  int dev;
+  const void *fn;
+  int threads;
+  size_t smem;
+  size_t blocks;
+};
+static std::mutex g_attr_mu;
+static std::vector<LaunchAttr> g_attr;
+
+static int current_device()
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return dev;
+}
+
 /* persistent grid: resident blocks per SM from the occupancy calculator */
 static size_t grid_blocks(const void *fn, int threads, size_t smem)
 {
+  const int dev = current_device();
+  {
+    std::lock_guard<std::mutex> g(g_attr_mu);
+    for (const auto &a : g_attr)
+      if (a.dev == dev && a.fn == fn && a.threads == threads && a.smem == smem) return a.blocks;
+  }
   int per_sm = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
-  return (size_t)num_sms() * (size_t)per_sm;
+  const size_t b = (size_t)num_sms() * (size_t)per_sm;
+  std::lock_guard<std::mutex> g(g_attr_mu);
+  g_attr.push_back({dev, fn, threads, smem, b});
+  return b;
 }
 
 static cudaError_t prep_kernel_smem(const void *fn, size_t bytes)
 {
-  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  const int dev = current_device();
+  {
+    std::lock_guard<std::mutex> g(g_attr_mu);
+    for (const auto &a : g_attr)
+      if (a.dev == dev && a.fn == fn && a.threads == -1 && a.smem >= bytes) return cudaSuccess;
+  }
+  const cudaError_t e =
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) {
+    std::lock_guard<std::mutex> g(g_attr_mu);
+    g_attr.push_back({dev, fn, -1, bytes, 0});
+  }
+  return e;
 }
 
 static double near2_of(const LaunchCfg &cfg)
@@ -1814,9 +1931,9 @@ cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &
 
 template <typename SI, typename S>
 static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                    const LatticeArgs *jobs, int njobs, size_t units,
                                     const LaunchCfg &cfg, cudaStream_t s)
 {
-  const size_t units = a.nx * (size_t)a.tiles;
   if (units == 0) return cudaSuccess;
   if (!a.rec || !a.code || a.rec_cap < (size_t)kTile) return cudaErrorInvalidValue;
   const int wpb = asm_warps(cfg);
@@ -1829,11 +1946,11 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
   for (size_t u0 = 0; u0 < units; u0 += cu) {
     const size_t nu = std::min(cu, units - u0);
     lattice_rec_kernel<SI><<<rec_grid(lattice_rec_kernel<SI>, nu * kTile), 64, 0, s>>>(
-        T, a, u0, nu, mixed, near2_of(cfg), orig2_of(cfg));
+        T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg));
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
     blocks = std::min(blocks, nu);
-    lattice_asm_kernel<S><<<(unsigned)blocks, wpb * 32, smem, s>>>(M, a, u0, nu, wpb);
+    lattice_asm_kernel<S><<<(unsigned)blocks, wpb * 32, smem, s>>>(M, a, jobs, njobs, u0, nu, wpb);
     g_launches++;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -1843,13 +1960,22 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
 cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                 const LaunchCfg &cfg, cudaStream_t s)
 {
-  return launch_lattice_t<double, double>(T, M, a, cfg, s);
+  return launch_lattice_t<double, double>(T, M, a, nullptr, 0, a.nx * (size_t)a.tiles, cfg, s);
 }
 
 cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                  const LaunchCfg &cfg, cudaStream_t s)
 {
-  return launch_lattice_t<float, float>(T, M, a, cfg, s);
+  return launch_lattice_t<float, float>(T, M, a, nullptr, 0, a.nx * (size_t)a.tiles, cfg, s);
+}
+
+cudaError_t launch_lattice_batch(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                 const LatticeArgs *d_jobs, int njobs, size_t units,
+                                 const LaunchCfg &cfg, cudaStream_t s, bool mixed)
+{
+  if (njobs <= 0) return cudaSuccess;
+  if (mixed) return launch_lattice_t<float, float>(T, M, a, d_jobs, njobs, units, cfg, s);
+  return launch_lattice_t<double, double>(T, M, a, d_jobs, njobs, units, cfg, s);
 }
 
 template <typename S>
@@ -1941,6 +2067,37 @@ cudaError_t launch_stats(const double *A, const double *B, size_t m, double floo
   if (m == 0) return cudaSuccess;
   const size_t b = std::min((m + 7) / 8, (size_t)num_sms() * 8);
   stats_kernel<<<(unsigned)b, 256, 0, s>>>(A, B, m, floor_abs, acc);
+  g_launches++;
+  return cudaGetLastError();
+}
+
+/* The generated Pi written out, [nx][ny][384]: thread per (k, n, call q) */
+__global__ void pi_synth_kernel(const double *xs, size_t nx, const double *ys, size_t ny,
+                                uint64_t seed, uint32_t stream, size_t k0, double *pi)
+{
+  const size_t tot = nx * ny * 96;
+  for (size_t u = (size_t)blockIdx.x * blockDim.x + threadIdx.x; u < tot;
+       u += (size_t)gridDim.x * blockDim.x) {
+    const int q = (int)(u % 96);
+    const size_t kn = u / 96, k = kn / ny, n = kn % ny;
+    const double env = pi_envelope(xs + 4 * k, ys + 4 * n);
+    uint32_t c[4] = {(uint32_t)n, (uint32_t)(k0 + k), (uint32_t)q, stream};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    /* call q serves lane q & 31 of rows r = 4 (q >> 5) + w */
+    for (int w = 0; w < 4; w++) {
+      const int comp = (4 * (q >> 5) + w) * 32 + (q & 31);
+      pi[kn * 384 + comp] = pi_normal(c[w]) * env;
+    }
+  }
+}
+
+cudaError_t launch_pi_synth(const double *xs, size_t nx, const double *ys, size_t ny, uint64_t seed,
+                            uint32_t stream, size_t k0, double *pi, cudaStream_t s)
+{
+  const size_t tot = nx * ny * 96;
+  if (tot == 0) return cudaSuccess;
+  const size_t b = std::min((tot + 255) / 256, (size_t)num_sms() * 16);
+  pi_synth_kernel<<<(unsigned)b, 256, 0, s>>>(xs, nx, ys, ny, seed, stream, k0, pi);
   g_launches++;
   return cudaGetLastError();
 }

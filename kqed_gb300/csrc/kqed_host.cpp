@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -572,25 +573,42 @@ static int check_variant_precision(int variant, int precision)
 /* L0 over n pairs on the device */
 static thread_local int tl_precision = KQED_FP64;
 
-/* record scratch for n pairs (capped at kRecPairs; launches are chunked) */
-static int rec_scratch(ThreadStage &st, size_t n, double **rec, uint8_t **code, size_t *cap)
+/* record scratch for n pairs (capped at kRecPairs; launches are chunked):
+   records [cap][kRec], Pi envelopes [cap], codes [cap] bytes */
+static int rec_scratch(ThreadStage &st, size_t n, double **rec, uint8_t **code, size_t *cap,
+                       double **env = nullptr)
 {
   size_t c = std::min(std::max(n, (size_t)kTile), kRecPairs);
   c = (c + kTile - 1) / kTile * kTile;
-  double *b = st.d_rec.get(c * kRec + c / 8 + 1);
+  double *b = st.d_rec.get(c * kRec + c + c / 8 + 1);
   if (!b) return fail("out of device memory for %zu pair records", c);
   *rec = b;
-  *code = reinterpret_cast<uint8_t *>(b + c * kRec);
+  if (env) *env = b + c * kRec;
+  *code = reinterpret_cast<uint8_t *>(b + c * kRec + c);
   *cap = c;
   return 0;
 }
 
+/* explicit record space (batch plans own theirs) */
+struct RecSpace {
+  double *rec;
+  uint8_t *code;
+  size_t cap;
+};
+
 static int run_l0(Ctx *c, const double *dx, const double *dy, size_t n, double *dout,
-                  uint8_t *dstatus, cudaStream_t s, bool timed = true)
+                  uint8_t *dstatus, cudaStream_t s, bool timed = true,
+                  const RecSpace *rs = nullptr)
 {
   L0Args a{dx, dy, n, dout, dstatus, nullptr, nullptr, 0};
   if (n == 0) return 0;
-  if (rec_scratch(stage_for(c), n, &a.rec, &a.code, &a.rec_cap)) return 1;
+  if (rs) {
+    a.rec = rs->rec;
+    a.code = rs->code;
+    a.rec_cap = rs->cap;
+  } else if (rec_scratch(stage_for(c), n, &a.rec, &a.code, &a.rec_cap)) {
+    return 1;
+  }
   TimedLaunch tl{nullptr, nullptr};
   if (timed) prof_begin(s, tl);
   if (tl_precision == KQED_FP32_MIXED && timed) CUDA_OK(launch_l0_mixed(c->T, c->M, a, c->cfg, s));
@@ -829,12 +847,14 @@ struct LatticeRun {
   Ctx *c;
   const double *d_x, *d_y;
   size_t nx, ny;
-  double *Ky, *Bx, *partial, *col, *rec;
+  double *Ky, *Bx, *partial, *col, *rec, *env;
   float2 *Ky2, *Bx2;
   float *col32;
   uint8_t *code;
   size_t rec_cap;
   int tiles, precision, variant;
+  uint64_t pi_seed;       /* generated Pi (lattice_launch with d_pi == NULL) */
+  uint32_t pi_stream;
 };
 
 static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, size_t ny,
@@ -843,12 +863,15 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
 {
   R.c = c; R.d_x = d_x; R.d_y = d_y; R.nx = nx; R.ny = ny; R.precision = precision;
   R.variant = variant;
+  R.pi_seed = 0;
+  R.pi_stream = 0;
   R.Ky2 = R.Bx2 = nullptr;
   R.col32 = nullptr;
   R.col = nullptr;
   R.tiles = (int)((ny + kTile - 1) / kTile);
   /* records first: the kernel-term launches below reuse the same scratch */
-  if (rec_scratch(st, nx * (size_t)R.tiles * kTile, &R.rec, &R.code, &R.rec_cap)) return 1;
+  if (rec_scratch(st, nx * (size_t)R.tiles * kTile, &R.rec, &R.code, &R.rec_cap, &R.env))
+    return 1;
   if (lattice_terms(c, variant, d_x, nx, d_y, ny, &R.Ky, &R.Bx, s, st)) return 1;
   R.partial = st.d_tmp.get(nx * (size_t)std::max(R.tiles, 1) * 2);
   if (!R.partial) return fail("out of device memory for partial sums");
@@ -890,7 +913,8 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
                 R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1), R.tiles,
                 R.col ? R.col + per_x * x0 : nullptr,
                 R.Ky2, R.Bx2 ? R.Bx2 + 384 * x0 : nullptr,
-                R.col32 ? R.col32 + per_x * x0 : nullptr, R.rec, R.code, R.rec_cap};
+                R.col32 ? R.col32 + per_x * x0 : nullptr, R.rec, R.code, R.rec_cap, R.env,
+                R.pi_seed, R.pi_stream, x0};
   TimedLaunch tl;
   prof_begin(s, tl);
   if (mixed) CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s));
@@ -914,6 +938,36 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
   if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R, precision)) return 1;
   if (lattice_launch(R, 0, nx, d_pi, s)) return 1;
   CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, d_sums, s));
+  return 0;
+}
+
+extern "C" int kqed_lattice_sum_synth(const struct QED_kernel_temps *t, int variant, size_t nx,
+                                      const double *d_x, size_t ny, const double *d_y,
+                                      uint64_t seed, uint32_t stream_id, double *d_sums,
+                                      int precision, void *stream)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (check_variant_precision(variant, precision)) return 1;
+  if (nx == 0) return 0;
+  if (!d_x || !d_y || !d_sums) return fail("null buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  ThreadStage &st = stage_for(c);
+  LatticeRun R;
+  if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R, precision)) return 1;
+  R.pi_seed = seed;
+  R.pi_stream = stream_id;
+  if (lattice_launch(R, 0, nx, nullptr, s)) return 1;
+  CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, d_sums, s));
+  return 0;
+}
+
+extern "C" int kqed_pi_synth_dev(size_t nx, const double *d_x, size_t ny, const double *d_y,
+                                 uint64_t seed, uint32_t stream_id, double *d_pi, void *stream)
+{
+  if (nx == 0 || ny == 0) return 0;
+  if (!d_x || !d_y || !d_pi) return fail("null buffer");
+  CUDA_OK(launch_pi_synth(d_x, nx, d_y, ny, seed, stream_id, 0, d_pi, (cudaStream_t)stream));
   return 0;
 }
 
@@ -992,3 +1046,343 @@ int set_error(const char *msg)
 }
 
 } // namespace kqed
+
+/* ------------------------------------------------- batched lattices */
+
+/* A batch of fused lattice sums as one work list: every lattice (job)
+   contributes its units (one x, kTile sites) to a single unit list, so one
+   record kernel and one assembly kernel per record chunk serve all jobs.
+   The plan owns every buffer the batch needs, runs the batch once eagerly
+   (choosing launch parameters when asked to tune), and captures the whole
+   sequence -- column tables, per-site / per-x kernel terms, the two
+   kernels, the per-job reductions -- in one CUDA graph that
+   kqed_batch_plan_launch replays. */
+struct kqed_batch_plan {
+  Ctx *c = nullptr;
+  int precision = KQED_FP64;
+  std::vector<kqed_lattice_job> jobs;
+  std::vector<LatticeArgs> hj;      /* device-side descriptors, host copy */
+  LatticeArgs *d_jobs = nullptr;
+  LatticeArgs shared{};             /* carries the record scratch */
+  RecSpace rs{};
+  size_t units = 0;
+  LaunchCfg cfg{};
+  std::vector<void *> allocs;
+  /* per-site terms shared by jobs with the same site array and term kind */
+  struct YTerm { const double *d_y; size_t ny; int kind; double *ky; float2 *ky2; };
+  std::vector<YTerm> yterms;
+  std::vector<double *> bx, bt;     /* per job */
+  std::vector<float2 *> bx2;
+  double *zeros = nullptr;          /* max(nx, ny) zero 4-vectors */
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  size_t graph_kernels = 0;
+  double tuned_ms = 0.0;
+};
+
+namespace {
+
+template <typename P> int plan_alloc(kqed_batch_plan *p, P **out, size_t count)
+{
+  void *m = nullptr;
+  if (cudaMalloc(&m, std::max(count, (size_t)1) * sizeof(P)) != cudaSuccess)
+    return fail("out of device memory for a lattice batch plan (%zu bytes)", count * sizeof(P));
+  p->allocs.push_back(m);
+  *out = static_cast<P *>(m);
+  return 0;
+}
+
+/* term kind of the per-site part: 1 = -L0(y,y)/2 (L1), 2 = -L0(0,y) (L2, L3) */
+int yterm_kind(int variant) { return variant == 1 ? 1 : 2; }
+
+int plan_enqueue_terms(kqed_batch_plan *p, cudaStream_t s)
+{
+  Ctx *c = p->c;
+  const bool mixed = p->precision == KQED_FP32_MIXED;
+  for (auto &Y : p->yterms) {
+    if (Y.kind == 1) {
+      if (run_l0(c, Y.d_y, Y.d_y, Y.ny, Y.ky, nullptr, s, false, &p->rs)) return 1;
+      CUDA_OK(launch_scale(Y.ky, -0.5, Y.ny * 384, s));
+    } else {
+      if (run_l0(c, p->zeros, Y.d_y, Y.ny, Y.ky, nullptr, s, false, &p->rs)) return 1;
+      CUDA_OK(launch_scale(Y.ky, -1.0, Y.ny * 384, s));
+    }
+    if (mixed) CUDA_OK(launch_to_float2(Y.ky, Y.ky2, Y.ny * 384, s));
+  }
+  for (size_t j = 0; j < p->jobs.size(); j++) {
+    const kqed_lattice_job &J = p->jobs[j];
+    double *bx = p->bx[j];
+    switch (J.variant) {
+    case 0:
+      continue;
+    case 1: /* -L0(x,x)/2 */
+      if (run_l0(c, J.d_x, J.d_x, J.nx, bx, nullptr, s, false, &p->rs)) return 1;
+      CUDA_OK(launch_scale(bx, -0.5, J.nx * 384, s));
+      break;
+    case 2: /* -L0(x,0) */
+      if (run_l0(c, J.d_x, p->zeros, J.nx, bx, nullptr, s, false, &p->rs)) return 1;
+      CUDA_OK(launch_scale(bx, -1.0, J.nx * 384, s));
+      break;
+    default: /* -L0(x,x) + L0(0,x) */
+      if (run_l0(c, J.d_x, J.d_x, J.nx, bx, nullptr, s, false, &p->rs) ||
+          run_l0(c, p->zeros, J.d_x, J.nx, p->bt[j], nullptr, s, false, &p->rs))
+        return 1;
+      CUDA_OK(launch_scale(bx, -1.0, J.nx * 384, s));
+      CUDA_OK(launch_axpy(bx, p->bt[j], 1.0, J.nx * 384, s));
+      break;
+    }
+    if (mixed) CUDA_OK(launch_to_float2(bx, p->bx2[j], J.nx * 384, s));
+  }
+  return 0;
+}
+
+int plan_enqueue_kernels(kqed_batch_plan *p, const LaunchCfg &cfg, cudaStream_t s)
+{
+  CUDA_OK(launch_lattice_batch(p->c->T, p->c->M, p->shared, p->d_jobs, (int)p->hj.size(),
+                               p->units, cfg, s, p->precision == KQED_FP32_MIXED));
+  return 0;
+}
+
+int plan_enqueue(kqed_batch_plan *p, cudaStream_t s)
+{
+  const bool mixed = p->precision == KQED_FP32_MIXED;
+  for (size_t j = 0; j < p->jobs.size(); j++) {
+    const kqed_lattice_job &J = p->jobs[j];
+    CUDA_OK(launch_build_columns(p->c->T, J.d_x, J.nx, const_cast<double *>(p->hj[j].col), s));
+    if (mixed)
+      CUDA_OK(launch_build_columns32(p->c->T, J.d_x, J.nx, const_cast<float *>(p->hj[j].col32), s));
+  }
+  if (plan_enqueue_terms(p, s)) return 1;
+  if (plan_enqueue_kernels(p, p->cfg, s)) return 1;
+  for (size_t j = 0; j < p->jobs.size(); j++)
+    CUDA_OK(launch_reduce_partials(p->hj[j].partial, p->jobs[j].nx, p->hj[j].tiles,
+                                   p->jobs[j].d_sums, s));
+  return 0;
+}
+
+/* time the two main kernels of the batch under cfg (best of two runs) */
+int plan_time(kqed_batch_plan *p, const LaunchCfg &cfg, cudaStream_t s, double *ms)
+{
+  cudaEvent_t a, b;
+  CUDA_OK(cudaEventCreate(&a));
+  CUDA_OK(cudaEventCreate(&b));
+  double best = 1e300;
+  for (int rep = 0; rep < 2; rep++) {
+    CUDA_OK(cudaEventRecord(a, s));
+    if (plan_enqueue_kernels(p, cfg, s)) return 1;
+    CUDA_OK(cudaEventRecord(b, s));
+    CUDA_OK(cudaEventSynchronize(b));
+    float t = 0;
+    CUDA_OK(cudaEventElapsedTime(&t, a, b));
+    best = std::min(best, (double)t);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = best;
+  return 0;
+}
+
+/* launch-parameter sweep: assembly warps per block, assembly grid, record
+   chunk; results kept per (device, precision, log2 of the batch's units) */
+struct TuneKey { int dev, precision, lg; LaunchCfg cfg; size_t chunk; };
+std::mutex g_tune_mu;
+std::vector<TuneKey> g_tuned;
+
+int plan_tune(kqed_batch_plan *p, cudaStream_t s)
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int lg = 0;
+  for (size_t u = p->units; u > 1; u >>= 1) lg++;
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    for (const auto &t : g_tuned)
+      if (t.dev == dev && t.precision == p->precision && t.lg == lg && t.chunk <= p->rs.cap) {
+        p->cfg = t.cfg;
+        p->shared.rec_cap = t.chunk;
+        return 0;
+      }
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t full = p->rs.cap;
+  const size_t chunks[2] = {full, std::max((size_t)kTile, full / 4 / kTile * kTile)};
+  double best = 1e300;
+  LaunchCfg bc = p->cfg;
+  size_t bchunk = full;
+  for (int w : {4, 8})
+    for (int bpsm : {0, 2, 1})
+      for (size_t ch : chunks) {
+        LaunchCfg cfg = p->cfg;
+        cfg.warps_per_block = w;
+        cfg.blocks = bpsm ? bpsm * sms : 0;
+        p->shared.rec_cap = ch;
+        double ms = 0;
+        if (plan_time(p, cfg, s, &ms)) return 1;
+        if (ms < best) { best = ms; bc = cfg; bchunk = ch; }
+      }
+  p->cfg = bc;
+  p->shared.rec_cap = bchunk;
+  p->tuned_ms = best;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tuned.push_back({dev, p->precision, lg, bc, bchunk});
+  return 0;
+}
+
+} // namespace
+
+extern "C" void kqed_batch_plan_destroy(kqed_batch_plan *p)
+{
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->cap) cudaStreamDestroy(p->cap);
+  for (void *m : p->allocs) cudaFree(m);
+  delete p;
+}
+
+extern "C" int kqed_batch_plan_create(const struct QED_kernel_temps *t, int njobs,
+                                      const struct kqed_lattice_job *jobs, int precision,
+                                      int tune, kqed_batch_plan **plan)
+{
+  if (!plan) return fail("null plan pointer");
+  *plan = nullptr;
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (njobs <= 0 || !jobs) return fail("empty batch");
+  if (check_variant_precision(0, precision)) return 1;
+  std::unique_ptr<kqed_batch_plan> P(new kqed_batch_plan);
+  kqed_batch_plan *p = P.get();
+  p->c = c;
+  p->precision = precision;
+  p->cfg = c->cfg;
+  p->jobs.assign(jobs, jobs + njobs);
+  const bool mixed = precision == KQED_FP32_MIXED;
+  const size_t per_x = (size_t)c->T.nstpy * c->T.NK * kRow;
+  size_t zmax = 0, total_pairs = 0;
+  for (int j = 0; j < njobs; j++) {
+    const kqed_lattice_job &J = jobs[j];
+    if (J.variant < 0 || J.variant > 3) return fail("job %d: variant %d not in 0..3", j, J.variant);
+    if (J.nx == 0 || J.ny == 0) return fail("job %d: empty lattice", j);
+    if (!J.d_x || !J.d_y || !J.d_sums) return fail("job %d: null buffer", j);
+    zmax = std::max(zmax, std::max(J.nx, J.ny));
+  }
+  if (plan_alloc(p, &p->zeros, zmax * 4)) return 1;
+  CUDA_OK(cudaMemset(p->zeros, 0, zmax * 4 * sizeof(double)));
+  p->hj.resize(njobs);
+  p->bx.assign(njobs, nullptr);
+  p->bt.assign(njobs, nullptr);
+  p->bx2.assign(njobs, nullptr);
+  for (int j = 0; j < njobs; j++) {
+    const kqed_lattice_job &J = jobs[j];
+    LatticeArgs &A = p->hj[j];
+    A = LatticeArgs{};
+    A.x = J.d_x;
+    A.y = J.d_y;
+    A.nx = J.nx;
+    A.ny = J.ny;
+    A.pi = J.d_pi;
+    A.pi_seed = J.pi_seed;
+    A.pi_stream = J.pi_stream;
+    A.k0 = 0;
+    A.tiles = (int)((J.ny + kTile - 1) / kTile);
+    A.u_begin = p->units;
+    p->units += J.nx * (size_t)A.tiles;
+    total_pairs += J.nx * (size_t)A.tiles * kTile;
+    if (plan_alloc(p, &A.partial, J.nx * (size_t)A.tiles * 2)) return 1;
+    double *col = nullptr;
+    if (plan_alloc(p, &col, J.nx * per_x)) return 1;
+    A.col = col;
+    if (mixed) {
+      float *c32 = nullptr;
+      if (plan_alloc(p, &c32, J.nx * per_x)) return 1;
+      A.col32 = c32;
+    }
+    if (J.variant) {
+      /* per-site term, shared with earlier jobs on the same sites */
+      const int kind = yterm_kind(J.variant);
+      kqed_batch_plan::YTerm *Y = nullptr;
+      for (auto &q : p->yterms)
+        if (q.d_y == J.d_y && q.ny == J.ny && q.kind == kind) Y = &q;
+      if (!Y) {
+        p->yterms.push_back({J.d_y, J.ny, kind, nullptr, nullptr});
+        Y = &p->yterms.back();
+        if (plan_alloc(p, &Y->ky, J.ny * 384)) return 1;
+        if (mixed && plan_alloc(p, &Y->ky2, J.ny * 384)) return 1;
+      }
+      A.Ky = Y->ky;
+      A.Ky2 = Y->ky2;
+      if (plan_alloc(p, &p->bx[j], J.nx * 384)) return 1;
+      if (J.variant == 3 && plan_alloc(p, &p->bt[j], J.nx * 384)) return 1;
+      if (mixed && plan_alloc(p, &p->bx2[j], J.nx * 384)) return 1;
+      A.Bx = p->bx[j];
+      A.Bx2 = p->bx2[j];
+    }
+  }
+  /* record space: the batch's kernels and the term launches share it */
+  size_t cap = std::min(std::max(total_pairs, zmax), kRecPairs);
+  cap = (cap + kTile - 1) / kTile * kTile;
+  double *rb = nullptr;
+  if (plan_alloc(p, &rb, cap * kRec + cap + cap / 8 + 1)) return 1;
+  p->rs = {rb, reinterpret_cast<uint8_t *>(rb + cap * kRec + cap), cap};
+  p->shared = LatticeArgs{};
+  p->shared.rec = rb;
+  p->shared.env = rb + cap * kRec;
+  p->shared.code = p->rs.code;
+  p->shared.rec_cap = cap;
+  if (plan_alloc(p, &p->d_jobs, njobs)) return 1;
+  CUDA_OK(cudaMemcpy(p->d_jobs, p->hj.data(), njobs * sizeof(LatticeArgs), cudaMemcpyHostToDevice));
+  CUDA_OK(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+  /* eager run: sets every launch attribute, fills the tables, and (tune)
+     times the candidate launch parameters on the real batch */
+  if (plan_enqueue(p, p->cap)) return 1;
+  if (tune && plan_tune(p, p->cap)) return 1;
+  CUDA_OK(cudaStreamSynchronize(p->cap));
+  /* capture */
+  CUDA_OK(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+  const int rc = plan_enqueue(p, p->cap);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(p->cap, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return 1;
+  }
+  CUDA_OK(ec);
+  p->graph = g;
+  CUDA_OK(cudaGraphInstantiate(&p->exec, p->graph, 0));
+  size_t nodes = 0;
+  CUDA_OK(cudaGraphGetNodes(p->graph, nullptr, &nodes));
+  std::vector<cudaGraphNode_t> nv(nodes);
+  CUDA_OK(cudaGraphGetNodes(p->graph, nv.data(), &nodes));
+  for (auto n : nv) {
+    cudaGraphNodeType ty;
+    if (cudaGraphNodeGetType(n, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+      p->graph_kernels++;
+  }
+  *plan = P.release();
+  return 0;
+}
+
+extern "C" int kqed_batch_plan_launch(kqed_batch_plan *p, void *stream)
+{
+  if (!p || !p->exec) return fail("invalid batch plan");
+  CUDA_OK(cudaGraphLaunch(p->exec, (cudaStream_t)stream));
+  g_launches += p->graph_kernels;
+  return 0;
+}
+
+extern "C" int kqed_batch_plan_info(const kqed_batch_plan *p, struct kqed_batch_info *info)
+{
+  if (!p || !info) return fail("null argument");
+  info->jobs = (int)p->jobs.size();
+  info->units = p->units;
+  info->pairs = 0;
+  for (const auto &J : p->jobs) info->pairs += J.nx * J.ny;
+  info->warps_per_block = p->cfg.warps_per_block;
+  info->blocks = p->cfg.blocks;
+  info->record_chunk_pairs = p->shared.rec_cap;
+  info->graph_kernels = p->graph_kernels;
+  info->tuned_ms = p->tuned_ms;
+  return 0;
+}

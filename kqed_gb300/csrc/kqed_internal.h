@@ -91,11 +91,14 @@ struct L0Args {
   size_t rec_cap;       /* pairs per record kernel launch */
 };
 
+/* One fused lattice sum (or, in a batch, one job of it).  The record
+   scratch fields are those of the launch (a batch uses the first
+   descriptor's); u_begin is the job's first unit in the batch's unit list. */
 struct LatticeArgs {
   const double *x;      /* [nx][4] */
   const double *y;      /* [ny][4] */
   size_t nx, ny;
-  const double *pi;     /* [nx][ny][384] */
+  const double *pi;     /* [nx][ny][384], or NULL: generated (pi_seed, pi_stream, k0) */
   const double *Ky;     /* [ny][384] per-site additive kernel terms or NULL */
   const double *Bx;     /* [nx][384] per-x additive kernel terms or NULL */
   double *partial;      /* [nx][tiles][2]  (sum, compensation) */
@@ -106,6 +109,11 @@ struct LatticeArgs {
   double *rec;          /* record scratch [rec_cap][kRec] */
   uint8_t *code;        /* [rec_cap] */
   size_t rec_cap;       /* pairs per record kernel launch (a multiple of kTile) */
+  double *env;          /* [rec_cap] Pi envelope per record (generated Pi) */
+  uint64_t pi_seed;     /* generated Pi: Philox key */
+  uint32_t pi_stream;   /* generated Pi: fourth counter word */
+  size_t k0;            /* generated Pi: global index of x[0] */
+  size_t u_begin;       /* batch: first unit of this job */
 };
 
 int upload_map_constants();
@@ -113,6 +121,11 @@ cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a
                            const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                 const LaunchCfg &cfg, cudaStream_t s);
+/* a batch of lattices: d_jobs [njobs] on the device (u_begin ascending from
+   0), `a` carries the record scratch; units = total units of all jobs */
+cudaError_t launch_lattice_batch(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                 const LatticeArgs *d_jobs, int njobs, size_t units,
+                                 const LaunchCfg &cfg, cudaStream_t s, bool mixed);
 cudaError_t launch_build_columns(const DevTables &T, const double *xs, size_t nx, double *col,
                                  cudaStream_t s);
 cudaError_t launch_build_columns32(const DevTables &T, const double *xs, size_t nx, float *col,
@@ -122,6 +135,8 @@ cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &
 cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                  const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_to_float2(const double *in, float2 *out, size_t n, cudaStream_t s);
+cudaError_t launch_pi_synth(const double *xs, size_t nx, const double *ys, size_t ny, uint64_t seed,
+                            uint32_t stream, size_t k0, double *pi, cudaStream_t s);
 cudaError_t launch_stats(const double *A, const double *B, size_t m, double floor_abs, double *acc,
                          cudaStream_t s);
 cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,

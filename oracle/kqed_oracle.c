@@ -1257,3 +1257,50 @@ int oracle_weights(long n, const double *X, const double *Y, const double *CB, d
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Synthetic Pi of the generated-Pi lattice sums (a benchmark input, not part
+   of the reference): Philox-4x32-10 (Salmon et al., SC'11) keyed by the
+   seed, counter (n, k, q, stream); component c takes word (c >> 5) & 3 of
+   call q = (c & 31) + 32 (c >> 7); value (b0+b1+b2+b3 - 510) sqrt(3)/256 of
+   that word's bytes, times exp(-(|y| + |x - y|) / 2). */
+static void philox10(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+  for (int r = 0; r < 10; r++) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = (uint32_t)p1;
+    c[2] = n2;
+    c[3] = (uint32_t)p0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+int oracle_pi_synth(long nx, const double *x, long ny, const double *y, uint64_t seed,
+                    uint32_t stream, long k0, double *pi)
+{
+  for (long k = 0; k < nx; k++)
+    for (long n = 0; n < ny; n++) {
+      const double *xv = x + 4 * k, *yv = y + 4 * n;
+      const double d0 = xv[0] - yv[0], d1 = xv[1] - yv[1], d2 = xv[2] - yv[2], d3 = xv[3] - yv[3];
+      const double nyv = sqrt(yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3]);
+      const double nd = sqrt(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
+      const double env = exp(-0.5 * (nyv + nd));
+      double *out = pi + (k * ny + n) * 384;
+      for (int q = 0; q < 96; q++) {
+        uint32_t c[4] = {(uint32_t)n, (uint32_t)(k0 + k), (uint32_t)q, stream};
+        philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        for (int w = 0; w < 4; w++) {
+          const uint32_t v = c[w];
+          const int s = (int)(v & 0xffu) + (int)((v >> 8) & 0xffu) + (int)((v >> 16) & 0xffu) +
+                        (int)(v >> 24);
+          out[(4 * (q >> 5) + w) * 32 + (q & 31)] = (double)(s - 510) * 0.0067658234670659265 * env;
+        }
+      }
+    }
+  return 0;
+}

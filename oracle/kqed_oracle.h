@@ -15,6 +15,8 @@
 #ifndef KQED_ORACLE_H
 #define KQED_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -46,6 +48,11 @@ int oracle_branch(long n, const double *x, const double *y, int *code);
    learned surrogate.  out[n][37]; returns 0. */
 int oracle_weights(long n, const double *X, const double *Y, const double *CB, double *out,
                    int nthreads);
+
+/* The synthetic Pi of kqed_lattice_sum_synth / kqed_pi_synth_dev (a
+   benchmark input): pi[nx][ny][384] for x indices k0 .. k0 + nx - 1. */
+int oracle_pi_synth(long nx, const double *x, long ny, const double *y, uint64_t seed,
+                    uint32_t stream, long k0, double *pi);
 
 #ifdef __cplusplus
 }

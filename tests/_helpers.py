@@ -82,3 +82,17 @@ def neumaier(v):
         c += (s - t) + x if abs(s) >= abs(x) else (x - t) + s
         s = t
     return s + c
+
+
+def oracle_pi_synth(x, y, seed, stream=0, k0=0):
+    """The synthetic Pi of kqed_lattice_sum_synth, [nx][ny][384], from the
+    oracle's restatement of the generator."""
+    O = oracle()
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.zeros((len(x), len(y), 384))
+    O.oracle_pi_synth.argtypes = [ctypes.c_long, _dp, ctypes.c_long, _dp, ctypes.c_uint64,
+                                  ctypes.c_uint32, ctypes.c_long, _dp]
+    assert O.oracle_pi_synth(len(x), x.ctypes.data_as(_dp), len(y), y.ctypes.data_as(_dp), seed,
+                             stream, k0, out.ctypes.data_as(_dp)) == 0
+    return out

@@ -148,3 +148,30 @@ def test_batch_rejects_uninitialised_tables(lib):
     dp = ctypes.POINTER(ctypes.c_double)
     assert lib.kqed_kernel_batch(ctypes.byref(t), 0, 0, None, None, None, None, 0) == 1
     assert b"not initialised" in lib.kqed_last_error()
+
+
+def test_batch_structs_match_ctypes(tmp_path):
+    """struct kqed_lattice_job / kqed_batch_info as the C compiler lays
+    them out equal the ctypes mirrors the Python binding passes"""
+    import kqed_gb300 as K
+    prog = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "kqed.h"
+int main(void){
+  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(struct kqed_lattice_job),
+    offsetof(struct kqed_lattice_job, d_pi), offsetof(struct kqed_lattice_job, pi_stream),
+    offsetof(struct kqed_lattice_job, d_sums), sizeof(struct kqed_batch_info),
+    offsetof(struct kqed_batch_info, tuned_ms));
+  return 0; }
+'''
+    c = tmp_path / "b.c"
+    c.write_text(prog)
+    exe = str(tmp_path / "b")
+    subprocess.run(["gcc", "-I", os.path.dirname(HDR), "-o", exe, str(c)], check=True,
+                   capture_output=True)
+    got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    J, I = K.LatticeJob, K.BatchInfo
+    assert got == [ctypes.sizeof(J), J.d_pi.offset, J.pi_stream.offset, J.d_sums.offset,
+                   ctypes.sizeof(I), I.tuned_ms.offset]

@@ -1,0 +1,74 @@
+"""Generated-Pi lattice sums (kqed_lattice_sum_synth, kqed_pi_synth_dev)
+against the oracle's restatement of the generator and the stored-Pi entry
+point.  Tolerances: generated Pi equal to the oracle's to 1e-15 relative
+(the exponential of the envelope may differ in its last bit between the
+device and the host C library); the fused sum with generated Pi equal bit
+for bit to the stored-Pi sum over the same Pi written out; FP64 sums within
+1e-12 of the oracle's contraction (relative to the largest |sum|)."""
+import numpy as np
+import pytest
+
+from _helpers import oracle_contract, oracle_pi_synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def temps():
+    from kqed_gb300 import build as B
+    B.build()
+    import kqed_gb300 as K
+    t = K.KernelTemps()
+    yield t
+    t.free()
+
+
+def K():
+    import kqed_gb300
+    return kqed_gb300
+
+
+def _inputs():
+    from kqed_gb300.workloads import diagonal_x, lattice_sites
+    ys = lattice_sites(6, 0.25)
+    xs = np.vstack([diagonal_x(4, 0.25), [[0.3, -0.2, 0.5, 0.1]]])
+    return xs, ys
+
+
+def test_generated_pi_matches_oracle(temps):
+    import torch
+    xs, ys = _inputs()
+    dx = torch.as_tensor(xs, device="cuda")
+    dy = torch.as_tensor(ys, device="cuda")
+    pi = torch.empty((len(xs), len(ys), 384), dtype=torch.float64, device="cuda")
+    K().pi_synth_dev(dx.data_ptr(), len(xs), dy.data_ptr(), len(ys), 99, pi.data_ptr(),
+                     stream_id=3)
+    torch.cuda.synchronize()
+    ref = oracle_pi_synth(xs, ys, 99, stream=3)
+    got = pi.cpu().numpy()
+    assert np.allclose(got, ref, rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("variant", [0, 2, 3])
+def test_lattice_sum_synth_equals_stored_pi_sum(temps, variant):
+    import torch
+    xs, ys = _inputs()
+    dx = torch.as_tensor(xs, device="cuda")
+    dy = torch.as_tensor(ys, device="cuda")
+    pi = torch.empty((len(xs), len(ys), 384), dtype=torch.float64, device="cuda")
+    K().pi_synth_dev(dx.data_ptr(), len(xs), dy.data_ptr(), len(ys), 5, pi.data_ptr())
+    fp64 = None
+    for prec in (K().KQED_FP64, K().KQED_FP32_MIXED):
+        a = torch.zeros(len(xs), dtype=torch.float64, device="cuda")
+        b = torch.zeros(len(xs), dtype=torch.float64, device="cuda")
+        K().lattice_sum_dev(temps, variant, dx.data_ptr(), len(xs), dy.data_ptr(), len(ys),
+                            pi.data_ptr(), a.data_ptr(), prec)
+        K().lattice_sum_synth(temps, variant, dx.data_ptr(), len(xs), dy.data_ptr(), len(ys), 5,
+                              b.data_ptr(), prec)
+        torch.cuda.synchronize()
+        assert np.array_equal(a.cpu().numpy(), b.cpu().numpy()), prec
+        if fp64 is None:
+            fp64 = a.cpu().numpy()
+    ref = oracle_contract(variant, np.repeat(xs, len(ys), 0), np.tile(ys, (len(xs), 1)),
+                          oracle_pi_synth(xs, ys, 5).reshape(-1, 384)).reshape(len(xs), -1).sum(1)
+    assert np.abs(fp64 - ref).max() <= 1e-12 * np.abs(ref).max()

@@ -174,3 +174,26 @@ def test_corrupt_table_is_rejected(tmp_path):
         assert O.oracle_load(str(tmp_path).encode()) != 0
     finally:
         assert O.oracle_load(PKG.encode()) == 0
+
+
+def test_synthetic_pi_generator_statistics():
+    """The generated-Pi benchmark input: g values standardised (mean 0,
+    variance 1 - 2^-16), bounded by 510 sqrt(3)/256, envelope 1 at x = y = 0,
+    and distinct for distinct seeds, streams and x indices"""
+    from _helpers import oracle_pi_synth
+    x = np.zeros((1, 4))
+    y = np.zeros((64, 4))
+    g = oracle_pi_synth(x, y, seed=12345).ravel()
+    assert abs(g.mean()) < 0.02 and abs(g.var() - 1.0) < 0.03
+    assert np.abs(g).max() <= 510 * np.sqrt(3) / 256 + 1e-12
+    q = np.round(g / (np.sqrt(3) / 256)).astype(int)
+    assert np.allclose(q * (np.sqrt(3) / 256), g, rtol=0, atol=1e-13)
+    assert not np.array_equal(g, oracle_pi_synth(x, y, seed=12346).ravel())
+    assert not np.array_equal(g, oracle_pi_synth(x, y, seed=12345, stream=1).ravel())
+    assert not np.array_equal(g, oracle_pi_synth(x, y, seed=12345, k0=1).ravel())
+    y2 = np.array([[0.3, 0.0, 0.4, 0.0]])
+    x2 = np.array([[0.0, 0.0, 0.0, 0.0]])
+    p = oracle_pi_synth(x2, y2, seed=7)[0, 0]
+    p0 = oracle_pi_synth(x, y2, seed=7)[0, 0]
+    assert np.array_equal(p, p0)
+    np.testing.assert_allclose(p / oracle_pi_synth(x, y2 * 0, seed=7)[0, 0], np.exp(-0.5), rtol=1e-15)
