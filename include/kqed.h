@@ -179,7 +179,8 @@ uint64_t kqed_launch_count(void);
    one work list, captured once in a CUDA graph and replayed.
    kqed_batch_plan_create allocates everything the batch needs, runs it once
    (with tune != 0 it first times candidate launch parameters -- assembly
-   warps per block, assembly grid, record chunk -- on this batch and keeps
+   warps per block, assembly grid, record chunk -- on this batch's first
+   131,072 units (8.4 M pairs) and keeps
    the fastest, remembered per device, precision and batch size), then
    captures the batch -- column tables, kernel terms, the record and
    assembly kernels over all jobs' units, the per-job reductions -- in a CUDA

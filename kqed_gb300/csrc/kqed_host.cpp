@@ -1137,12 +1137,17 @@ int plan_enqueue_terms(kqed_batch_plan *p, cudaStream_t s)
   return 0;
 }
 
-int plan_enqueue_kernels(kqed_batch_plan *p, const LaunchCfg &cfg, cudaStream_t s)
+int plan_enqueue_kernels(kqed_batch_plan *p, const LaunchCfg &cfg, cudaStream_t s,
+                         size_t units = 0)
 {
   CUDA_OK(launch_lattice_batch(p->c->T, p->c->M, p->shared, p->d_jobs, (int)p->hj.size(),
-                               p->units, cfg, s, p->precision == KQED_FP32_MIXED));
+                               units ? units : p->units, cfg, s,
+                               p->precision == KQED_FP32_MIXED));
   return 0;
 }
+
+/* the tuner times the batch's first kTuneUnits units (8.4 M pairs) */
+constexpr size_t kTuneUnits = (size_t)1 << 17;
 
 int plan_enqueue(kqed_batch_plan *p, cudaStream_t s)
 {
@@ -1170,7 +1175,7 @@ int plan_time(kqed_batch_plan *p, const LaunchCfg &cfg, cudaStream_t s, double *
   double best = 1e300;
   for (int rep = 0; rep < 2; rep++) {
     CUDA_OK(cudaEventRecord(a, s));
-    if (plan_enqueue_kernels(p, cfg, s)) return 1;
+    if (plan_enqueue_kernels(p, cfg, s, std::min(p->units, kTuneUnits))) return 1;
     CUDA_OK(cudaEventRecord(b, s));
     CUDA_OK(cudaEventSynchronize(b));
     float t = 0;
