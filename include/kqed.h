@@ -158,16 +158,20 @@ int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int variant, size
      g * exp(-(|y_n| + |x_k - y_n|) / 2),
      g = (b0 + b1 + b2 + b3 - 510) * sqrt(3) / 256,
    b0..b3 the bytes of word (c >> 5) & 3 of Philox-4x32-10 with key seed
-   (low word first) and counter (n, k, (c & 31) + 32 * (c >> 7), stream_id):
-   mean 0, variance 1 - 2^-16.
+   (low word first) and counter (y_offset + n, x_offset + k,
+   (c & 31) + 32 * (c >> 7), stream_id): mean 0, variance 1 - 2^-16.  The
+   offsets are the global indices of d_x[0] and d_y[0], so a lattice split
+   into slabs of sites (or of x points) sees the same Pi in every piece.
    kqed_lattice_sum_synth: the fused lattice sum with this Pi generated inside
    the kernel (nothing of Pi is stored); otherwise as kqed_lattice_sum_dev.
    kqed_pi_synth_dev: the same Pi written to d_pi [nx][ny][384]. */
 int kqed_lattice_sum_synth(const struct QED_kernel_temps *t, int variant, size_t nx,
                            const double *d_x, size_t ny, const double *d_y, uint64_t seed,
-                           uint32_t stream_id, double *d_sums, int precision, void *stream);
+                           uint32_t stream_id, size_t x_offset, size_t y_offset, double *d_sums,
+                           int precision, void *stream);
 int kqed_pi_synth_dev(size_t nx, const double *d_x, size_t ny, const double *d_y, uint64_t seed,
-                      uint32_t stream_id, double *d_pi, void *stream);
+                      uint32_t stream_id, size_t x_offset, size_t y_offset, double *d_pi,
+                      void *stream);
 
 /* Message of the last error on the calling thread ("" if none). */
 const char *kqed_last_error(void);

@@ -122,12 +122,13 @@ def lib():
         L.kqed_precision_stats.restype = ctypes.c_int
         L.kqed_lattice_sum_synth.argtypes = [T, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
                                              ctypes.c_size_t, ctypes.c_void_p, ctypes.c_uint64,
-                                             ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int,
-                                             ctypes.c_void_p]
+                                             ctypes.c_uint32, ctypes.c_size_t, ctypes.c_size_t,
+                                             ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.kqed_lattice_sum_synth.restype = ctypes.c_int
         L.kqed_pi_synth_dev.argtypes = [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
                                         ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
-                                        ctypes.c_void_p, ctypes.c_void_p]
+                                        ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p,
+                                        ctypes.c_void_p]
         L.kqed_pi_synth_dev.restype = ctypes.c_int
         L.kqed_batch_plan_create.argtypes = [T, ctypes.c_int, ctypes.POINTER(LatticeJob),
                                              ctypes.c_int, ctypes.c_int,
@@ -286,16 +287,19 @@ def profile(enable):
 
 
 def lattice_sum_synth(t, variant, x_ptr, nx, y_ptr, ny, seed, sums_ptr, precision=KQED_FP64,
-                      stream_id=0, stream=None):
+                      stream_id=0, x_offset=0, y_offset=0, stream=None):
     """Fused lattice sum with the synthetic Pi generated inside the kernel
-    (kqed_lattice_sum_synth); device pointers."""
+    (kqed_lattice_sum_synth); device pointers.  x_offset / y_offset: global
+    indices of the first x / site (a slab of a larger lattice)."""
     _check(lib().kqed_lattice_sum_synth(t.ptr, variant, nx, x_ptr, ny, y_ptr, seed, stream_id,
-                                        sums_ptr, precision, stream))
+                                        x_offset, y_offset, sums_ptr, precision, stream))
 
 
-def pi_synth_dev(x_ptr, nx, y_ptr, ny, seed, pi_ptr, stream_id=0, stream=None):
+def pi_synth_dev(x_ptr, nx, y_ptr, ny, seed, pi_ptr, stream_id=0, x_offset=0, y_offset=0,
+                 stream=None):
     """The synthetic Pi of lattice_sum_synth written to pi_ptr [nx][ny][384]."""
-    _check(lib().kqed_pi_synth_dev(nx, x_ptr, ny, y_ptr, seed, stream_id, pi_ptr, stream))
+    _check(lib().kqed_pi_synth_dev(nx, x_ptr, ny, y_ptr, seed, stream_id, x_offset, y_offset,
+                                   pi_ptr, stream))
 
 
 class BatchPlan:

@@ -1705,7 +1705,7 @@ __global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, const __gri
       const bool live = asm_pair<S>(L, M, A.rec + r * REC, A.code[r], lane, perm, t64);
       const double *pi = J.pi ? J.pi + (k * J.ny + n) * 384 : nullptr;
       double pvv[12];
-      if (!J.pi) pi_generate(J.pi_seed, J.pi_stream, J.k0 + k, n, A.env[r], lane, pvv);
+      if (!J.pi) pi_generate(J.pi_seed, J.pi_stream, J.k0 + k, J.n0 + n, A.env[r], lane, pvv);
       const double *ky = J.Ky ? J.Ky + n * 384 : nullptr;
       const double *bx = J.Bx ? J.Bx + k * 384 : nullptr;
       const float2 *ky2 = (f32 && J.Ky2) ? J.Ky2 + n * 384 : nullptr;
@@ -2073,7 +2073,7 @@ cudaError_t launch_stats(const double *A, const double *B, size_t m, double floo
 
 /* The generated Pi written out, [nx][ny][384]: thread per (k, n, call q) */
 __global__ void pi_synth_kernel(const double *xs, size_t nx, const double *ys, size_t ny,
-                                uint64_t seed, uint32_t stream, size_t k0, double *pi)
+                                uint64_t seed, uint32_t stream, size_t k0, size_t n0, double *pi)
 {
   const size_t tot = nx * ny * 96;
   for (size_t u = (size_t)blockIdx.x * blockDim.x + threadIdx.x; u < tot;
@@ -2081,7 +2081,7 @@ __global__ void pi_synth_kernel(const double *xs, size_t nx, const double *ys, s
     const int q = (int)(u % 96);
     const size_t kn = u / 96, k = kn / ny, n = kn % ny;
     const double env = pi_envelope(xs + 4 * k, ys + 4 * n);
-    uint32_t c[4] = {(uint32_t)n, (uint32_t)(k0 + k), (uint32_t)q, stream};
+    uint32_t c[4] = {(uint32_t)(n0 + n), (uint32_t)(k0 + k), (uint32_t)q, stream};
     philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
     /* call q serves lane q & 31 of rows r = 4 (q >> 5) + w */
     for (int w = 0; w < 4; w++) {
@@ -2092,12 +2092,12 @@ __global__ void pi_synth_kernel(const double *xs, size_t nx, const double *ys, s
 }
 
 cudaError_t launch_pi_synth(const double *xs, size_t nx, const double *ys, size_t ny, uint64_t seed,
-                            uint32_t stream, size_t k0, double *pi, cudaStream_t s)
+                            uint32_t stream, size_t k0, size_t n0, double *pi, cudaStream_t s)
 {
   const size_t tot = nx * ny * 96;
   if (tot == 0) return cudaSuccess;
   const size_t b = std::min((tot + 255) / 256, (size_t)num_sms() * 16);
-  pi_synth_kernel<<<(unsigned)b, 256, 0, s>>>(xs, nx, ys, ny, seed, stream, k0, pi);
+  pi_synth_kernel<<<(unsigned)b, 256, 0, s>>>(xs, nx, ys, ny, seed, stream, k0, n0, pi);
   g_launches++;
   return cudaGetLastError();
 }

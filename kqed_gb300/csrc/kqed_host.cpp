@@ -855,6 +855,7 @@ struct LatticeRun {
   int tiles, precision, variant;
   uint64_t pi_seed;       /* generated Pi (lattice_launch with d_pi == NULL) */
   uint32_t pi_stream;
+  size_t x_offset, y_offset;   /* generated Pi: global indices of x[0], y[0] */
 };
 
 static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, size_t ny,
@@ -865,6 +866,7 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.variant = variant;
   R.pi_seed = 0;
   R.pi_stream = 0;
+  R.x_offset = R.y_offset = 0;
   R.Ky2 = R.Bx2 = nullptr;
   R.col32 = nullptr;
   R.col = nullptr;
@@ -914,7 +916,7 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
                 R.col ? R.col + per_x * x0 : nullptr,
                 R.Ky2, R.Bx2 ? R.Bx2 + 384 * x0 : nullptr,
                 R.col32 ? R.col32 + per_x * x0 : nullptr, R.rec, R.code, R.rec_cap, R.env,
-                R.pi_seed, R.pi_stream, x0};
+                R.pi_seed, R.pi_stream, R.x_offset + x0, R.y_offset};
   TimedLaunch tl;
   prof_begin(s, tl);
   if (mixed) CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s));
@@ -943,8 +945,9 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
 
 extern "C" int kqed_lattice_sum_synth(const struct QED_kernel_temps *t, int variant, size_t nx,
                                       const double *d_x, size_t ny, const double *d_y,
-                                      uint64_t seed, uint32_t stream_id, double *d_sums,
-                                      int precision, void *stream)
+                                      uint64_t seed, uint32_t stream_id, size_t x_offset,
+                                      size_t y_offset, double *d_sums, int precision,
+                                      void *stream)
 {
   Ctx *c = ctx_of(t);
   if (!c) return fail("tables not initialised");
@@ -957,17 +960,21 @@ extern "C" int kqed_lattice_sum_synth(const struct QED_kernel_temps *t, int vari
   if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R, precision)) return 1;
   R.pi_seed = seed;
   R.pi_stream = stream_id;
+  R.x_offset = x_offset;
+  R.y_offset = y_offset;
   if (lattice_launch(R, 0, nx, nullptr, s)) return 1;
   CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, d_sums, s));
   return 0;
 }
 
 extern "C" int kqed_pi_synth_dev(size_t nx, const double *d_x, size_t ny, const double *d_y,
-                                 uint64_t seed, uint32_t stream_id, double *d_pi, void *stream)
+                                 uint64_t seed, uint32_t stream_id, size_t x_offset,
+                                 size_t y_offset, double *d_pi, void *stream)
 {
   if (nx == 0 || ny == 0) return 0;
   if (!d_x || !d_y || !d_pi) return fail("null buffer");
-  CUDA_OK(launch_pi_synth(d_x, nx, d_y, ny, seed, stream_id, 0, d_pi, (cudaStream_t)stream));
+  CUDA_OK(launch_pi_synth(d_x, nx, d_y, ny, seed, stream_id, x_offset, y_offset, d_pi,
+                          (cudaStream_t)stream));
   return 0;
 }
 

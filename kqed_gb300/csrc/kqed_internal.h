@@ -113,6 +113,7 @@ struct LatticeArgs {
   uint64_t pi_seed;     /* generated Pi: Philox key */
   uint32_t pi_stream;   /* generated Pi: fourth counter word */
   size_t k0;            /* generated Pi: global index of x[0] */
+  size_t n0;            /* generated Pi: global index of y[0] */
   size_t u_begin;       /* batch: first unit of this job */
 };
 
@@ -136,7 +137,7 @@ cudaError_t launch_lattice_mixed(const DevTables &T, const DevMaps &M, const Lat
                                  const LaunchCfg &cfg, cudaStream_t s);
 cudaError_t launch_to_float2(const double *in, float2 *out, size_t n, cudaStream_t s);
 cudaError_t launch_pi_synth(const double *xs, size_t nx, const double *ys, size_t ny, uint64_t seed,
-                            uint32_t stream, size_t k0, double *pi, cudaStream_t s);
+                            uint32_t stream, size_t k0, size_t n0, double *pi, cudaStream_t s);
 cudaError_t launch_stats(const double *A, const double *B, size_t m, double floor_abs, double *acc,
                          cudaStream_t s);
 cudaError_t launch_reduce_partials(const double *partial, size_t nx, int tiles, double *sums,

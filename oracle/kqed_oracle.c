@@ -1261,7 +1261,7 @@ int oracle_weights(long n, const double *X, const double *Y, const double *CB, d
 /* ------------------------------------------------------------------ */
 /* Synthetic Pi of the generated-Pi lattice sums (a benchmark input, not part
    of the reference): Philox-4x32-10 (Salmon et al., SC'11) keyed by the
-   seed, counter (n, k, q, stream); component c takes word (c >> 5) & 3 of
+   seed, counter (n0 + n, k0 + k, q, stream); component c takes word (c >> 5) & 3 of
    call q = (c & 31) + 32 (c >> 7); value (b0+b1+b2+b3 - 510) sqrt(3)/256 of
    that word's bytes, times exp(-(|y| + |x - y|) / 2). */
 static void philox10(uint32_t c[4], uint32_t k0, uint32_t k1)
@@ -1281,7 +1281,7 @@ static void philox10(uint32_t c[4], uint32_t k0, uint32_t k1)
 }
 
 int oracle_pi_synth(long nx, const double *x, long ny, const double *y, uint64_t seed,
-                    uint32_t stream, long k0, double *pi)
+                    uint32_t stream, long k0, long n0, double *pi)
 {
   for (long k = 0; k < nx; k++)
     for (long n = 0; n < ny; n++) {
@@ -1292,7 +1292,7 @@ int oracle_pi_synth(long nx, const double *x, long ny, const double *y, uint64_t
       const double env = exp(-0.5 * (nyv + nd));
       double *out = pi + (k * ny + n) * 384;
       for (int q = 0; q < 96; q++) {
-        uint32_t c[4] = {(uint32_t)n, (uint32_t)(k0 + k), (uint32_t)q, stream};
+        uint32_t c[4] = {(uint32_t)(n0 + n), (uint32_t)(k0 + k), (uint32_t)q, stream};
         philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
         for (int w = 0; w < 4; w++) {
           const uint32_t v = c[w];

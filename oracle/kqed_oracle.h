@@ -50,9 +50,10 @@ int oracle_weights(long n, const double *X, const double *Y, const double *CB, d
                    int nthreads);
 
 /* The synthetic Pi of kqed_lattice_sum_synth / kqed_pi_synth_dev (a
-   benchmark input): pi[nx][ny][384] for x indices k0 .. k0 + nx - 1. */
+   benchmark input): pi[nx][ny][384] for x indices k0 .. k0 + nx - 1 and
+   site indices n0 .. n0 + ny - 1. */
 int oracle_pi_synth(long nx, const double *x, long ny, const double *y, uint64_t seed,
-                    uint32_t stream, long k0, double *pi);
+                    uint32_t stream, long k0, long n0, double *pi);
 
 #ifdef __cplusplus
 }

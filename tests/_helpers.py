@@ -84,7 +84,7 @@ def neumaier(v):
     return s + c
 
 
-def oracle_pi_synth(x, y, seed, stream=0, k0=0):
+def oracle_pi_synth(x, y, seed, stream=0, k0=0, n0=0):
     """The synthetic Pi of kqed_lattice_sum_synth, [nx][ny][384], from the
     oracle's restatement of the generator."""
     O = oracle()
@@ -92,7 +92,7 @@ def oracle_pi_synth(x, y, seed, stream=0, k0=0):
     y = np.ascontiguousarray(y, np.float64)
     out = np.zeros((len(x), len(y), 384))
     O.oracle_pi_synth.argtypes = [ctypes.c_long, _dp, ctypes.c_long, _dp, ctypes.c_uint64,
-                                  ctypes.c_uint32, ctypes.c_long, _dp]
+                                  ctypes.c_uint32, ctypes.c_long, ctypes.c_long, _dp]
     assert O.oracle_pi_synth(len(x), x.ctypes.data_as(_dp), len(y), y.ctypes.data_as(_dp), seed,
-                             stream, k0, out.ctypes.data_as(_dp)) == 0
+                             stream, k0, n0, out.ctypes.data_as(_dp)) == 0
     return out

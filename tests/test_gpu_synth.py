@@ -72,3 +72,18 @@ def test_lattice_sum_synth_equals_stored_pi_sum(temps, variant):
     ref = oracle_contract(variant, np.repeat(xs, len(ys), 0), np.tile(ys, (len(xs), 1)),
                           oracle_pi_synth(xs, ys, 5).reshape(-1, 384)).reshape(len(xs), -1).sum(1)
     assert np.abs(fp64 - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_site_slabs_with_offsets_reproduce_the_full_sum(temps):
+    """the per-rank GPU evaluation of a sharded sum: slabs of sites with
+    their global offsets, combined in rank order, give the whole lattice's
+    generated-Pi sum (relative 1e-13)"""
+    from kqed_gb300.shard import _gpu_local_sum, combine_rank_order, site_slab
+    xs, ys = _inputs()
+    full = _gpu_local_sum(temps, 2, xs, ys, 0, None, 17, 4, K().KQED_FP64)
+    parts = []
+    for r in range(3):
+        lo, hi = site_slab(len(ys), r, 3)
+        parts.append(_gpu_local_sum(temps, 2, xs, ys[lo:hi], lo, None, 17, 4, K().KQED_FP64))
+    got = combine_rank_order(parts)
+    assert np.abs(got - full).max() <= 1e-13 * np.abs(full).max()
