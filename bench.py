@@ -331,63 +331,71 @@ def run_gb300(args):
     achieved = flops_launch / (kavg_ms / 1e3) / 1e12
 
     # ---- end to end through the host entry point (Pi from pinned memory)
-    pi_host = torch.empty(pi.shape, dtype=torch.float64, pin_memory=True)
-    pi_host.copy_(pi)
-    del pi
-    torch.cuda.empty_cache()
-    xh = np.ascontiguousarray(xs)
-    yh = np.ascontiguousarray(ys)
-    sh = np.zeros(nx)
-    dp = ctypes.POINTER(ctypes.c_double)
-    lib = K.lib()
+    def measure_e2e(pi):
+        pi_host = torch.empty(pi.shape, dtype=torch.float64, pin_memory=True)
+        pi_host.copy_(pi)
+        xh = np.ascontiguousarray(xs)
+        yh = np.ascontiguousarray(ys)
+        sh = np.zeros(nx)
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib = K.lib()
 
-    def e2e_step():
-        rc = lib.kqed_lattice_sum(t.ptr, args.variant, nx, xh.ctypes.data_as(dp), ny,
-                                  yh.ctypes.data_as(dp),
-                                  ctypes.cast(pi_host.data_ptr(), dp), sh.ctypes.data_as(dp), prec)
-        if rc != 0:
-            raise RuntimeError(lib.kqed_last_error().decode())
+        def e2e_step():
+            rc = lib.kqed_lattice_sum(t.ptr, args.variant, nx, xh.ctypes.data_as(dp), ny,
+                                      yh.ctypes.data_as(dp),
+                                      ctypes.cast(pi_host.data_ptr(), dp), sh.ctypes.data_as(dp), prec)
+            if rc != 0:
+                raise RuntimeError(lib.kqed_last_error().decode())
 
-    e2e_step()
-    barrier()
-    K.profile(True)
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
         e2e_step()
-    barrier()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    e2e_kern_ms, _ = K.profile_read()
-    e2e_copy_ms, _ = K.profile_read_copies()
-    K.profile(False)
-    if world > 1:
-        mt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(mt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(mt.item())
-    # host->device link rate right after (the same pinned buffer, 1 GB pieces):
-    # Pi crosses the link every step, so e2e cannot beat bytes / this rate
-    scratch = torch.empty(min(pi_host.numel(), 1 << 27), dtype=torch.float64, device=dev)
-    flat = pi_host.view(-1)
-    torch.cuda.synchronize(dev)
-    c0 = time.perf_counter()
-    moved = 0
-    for o in range(0, flat.numel(), scratch.numel()):
-        n = min(scratch.numel(), flat.numel() - o)
-        scratch[:n].copy_(flat[o:o + n], non_blocking=True)
-        moved += n * 8
-    torch.cuda.synchronize(dev)
-    h2d_gbs = moved / (time.perf_counter() - c0) / 1e9
-    del scratch
-    e2e = {"value": world * nx * ny / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(pi_host.numel() * 8 + xh.nbytes + yh.nbytes),
-           "d2h_bytes_per_step": int(sh.nbytes),
-           "precision": args.precision,
-           "h2d_link_gbs_measured": h2d_gbs,
-           "ms_per_step": e2e_s * 1e3,
-           "kernel_ms_per_step": e2e_kern_ms / args.e2e_steps,
-           "copy_ms_per_step": e2e_copy_ms / args.e2e_steps,
-           "h2d_gbs_during_step": pi_host.numel() * 8 / (e2e_copy_ms / args.e2e_steps / 1e3) / 1e9
-           if e2e_copy_ms > 0 else None,
-           "copy_bound_evals_per_s": world * nx * ny / (pi_host.numel() * 8 / (h2d_gbs * 1e9))}
+        barrier()
+        K.profile(True)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        e2e_kern_ms, _ = K.profile_read()
+        e2e_copy_ms, _ = K.profile_read_copies()
+        K.profile(False)
+        if world > 1:
+            mt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(mt, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(mt.item())
+        # host->device link rate right after (the same pinned buffer, 1 GB pieces):
+        # Pi crosses the link every step, so e2e cannot beat bytes / this rate
+        scratch = torch.empty(min(pi_host.numel(), 1 << 27), dtype=torch.float64, device=dev)
+        flat = pi_host.view(-1)
+        torch.cuda.synchronize(dev)
+        c0 = time.perf_counter()
+        moved = 0
+        for o in range(0, flat.numel(), scratch.numel()):
+            n = min(scratch.numel(), flat.numel() - o)
+            scratch[:n].copy_(flat[o:o + n], non_blocking=True)
+            moved += n * 8
+        torch.cuda.synchronize(dev)
+        h2d_gbs = moved / (time.perf_counter() - c0) / 1e9
+        del scratch
+        e2e = {"value": world * nx * ny / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(pi_host.numel() * 8 + xh.nbytes + yh.nbytes),
+               "d2h_bytes_per_step": int(sh.nbytes),
+               "precision": args.precision,
+               "h2d_link_gbs_measured": h2d_gbs,
+               "ms_per_step": e2e_s * 1e3,
+               "kernel_ms_per_step": e2e_kern_ms / args.e2e_steps,
+               "copy_ms_per_step": e2e_copy_ms / args.e2e_steps,
+               "h2d_gbs_during_step": pi_host.numel() * 8 / (e2e_copy_ms / args.e2e_steps / 1e3) / 1e9
+               if e2e_copy_ms > 0 else None,
+               "copy_bound_evals_per_s": world * nx * ny / (pi_host.numel() * 8 / (h2d_gbs * 1e9))}
+        return e2e, pi_host
+
+    if args.e2e_steps > 0:
+        e2e, pi_host = measure_e2e(pi)
+        del pi
+        torch.cuda.empty_cache()
+    else:
+        e2e, pi_host = None, pi.cpu()
+        del pi
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -420,7 +428,7 @@ def run_gb300(args):
                                         "MEASURED_PEAKS.json)"},
             "cpu_baseline": cpu,
             "clocks": clk,
-            "checksum": [float(v) for v in sh[:4]],
+            "checksum": [float(v) for v in fsums["fp64"][:4]],
         }
         print(json.dumps(line), flush=True)
     t.free()

@@ -1453,7 +1453,7 @@ __device__ __forceinline__ const LatticeArgs &job_of(const LatticeArgs &A,
 /* records of the pairs of lattice units u0 + uu, uu < nu; unit u of a
    lattice is (x_k, sites t*kTile .. t*kTile + kTile - 1), k = u' / tiles,
    t = u' % tiles, u' = u - u_begin; record r = uu * kTile + j */
-template <typename SI>
+template <typename SI, bool BATCH>
 __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __grid_constant__ LatticeArgs A,
                                                          const LatticeArgs *jobs, int njobs,
                                                          size_t u0, size_t nu, int mixed,
@@ -1463,7 +1463,7 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nu * kTile;
        r += (size_t)gridDim.x * blockDim.x) {
     const size_t u = u0 + r / kTile;
-    const LatticeArgs &J = job_of(A, jobs, njobs, u);
+    const LatticeArgs &J = BATCH ? job_of(A, jobs, njobs, u) : A;
     const size_t ul = u - J.u_begin;
     const size_t k = ul / J.tiles, n = (ul % J.tiles) * kTile + r % kTile;
     if (n >= J.ny) continue;
@@ -1639,82 +1639,132 @@ __device__ __forceinline__ double f2d_exact(float f)
   return e == 0 ? 0.0 : __hiloint2double((int)hi, (int)(u << 29));
 }
 
-/* sum_i K_i Pi_i of one pair, lane-partial.  FP64 when the pair was
+/* Pi component r*32 + lane of a pair, r = 4g + w: stored (pi) or, GEN,
+   word w of the pair's generated call g (pi_generate's layout) */
+template <bool GEN> struct PiSrc;
+template <> struct PiSrc<false> {
+  const double *pi;
+  __device__ __forceinline__ void group(int, double (&v)[4], int lane) const
+  {
+  }
+  __device__ __forceinline__ double get(int r, const double (&)[4], int lane) const
+  {
+    return __ldg(pi + r * 32 + lane);
+  }
+};
+template <> struct PiSrc<true> {
+  uint64_t seed;
+  uint32_t stream;
+  size_t k, n;
+  double env;
+  __device__ __forceinline__ void group(int g, double (&v)[4], int lane) const
+  {
+    uint32_t c[4] = {(uint32_t)n, (uint32_t)k, (uint32_t)(lane + 32 * g), stream};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+    for (int w = 0; w < 4; w++) v[w] = pi_normal(c[w]) * env;
+  }
+  __device__ __forceinline__ double get(int r, const double (&v)[4], int) const { return v[r & 3]; }
+};
+
+/* acc += sum_i K_i Pi_i of one pair, lane-partial.  FP64 when the pair was
    assembled in FP64.  Otherwise the float components plus the per-site and
    per-x terms as float (hi, lo) pairs: the hi parts are added in float,
    where L1..L3's near-cancelling terms subtract exactly, and each component
    enters an FP64 product with Pi, so neither Pi nor the sum is rounded to
    float; the lo parts go through a float accumulator. */
-__device__ __forceinline__ double contract(const AsmSmem &L, bool live, bool perm, bool t64,
-                                           const double *pi, const double *pv, const double *ky,
-                                           const double *bx, const float2 *ky2, const float2 *bx2,
-                                           int lane)
+template <bool GEN>
+__device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm, bool t64,
+                                         const PiSrc<GEN> &P, const double *ky, const double *bx,
+                                         const float2 *ky2, const float2 *bx2, int lane,
+                                         double (&acc)[2])
 {
+  double pg[4];
   if (t64 || !live) {
-    double acc = 0.0;
 #pragma unroll
     for (int r = 0; r < 12; r++) {
+      if ((r & 3) == 0) P.group(r >> 2, pg, lane);
       const int i = r * 32 + lane;
       double kv = live ? kcomp(L, true, perm, i) : 0.0;
       if (ky) kv += __ldg(ky + i);
       if (bx) kv += __ldg(bx + i);
-      acc = fma(kv, pv ? pv[r] : __ldg(pi + i), acc);
+      acc[r & 1] = fma(kv, P.get(r, pg, lane), acc[r & 1]);
     }
-    return acc;
+    return;
   }
   const float *tb = reinterpret_cast<const float *>(L.tbuf);
-  double acc = 0.0;
   float accl = 0.0f;
 #pragma unroll
   for (int r = 0; r < 12; r++) {
+    if ((r & 3) == 0) P.group(r >> 2, pg, lane);
     const int i = r * 32 + lane;
     float kh = perm ? -tb[mulam(i)] : tb[i], kl = 0.0f;
     if (ky2) { const float2 q = __ldg(ky2 + i); kh += q.x; kl += q.y; }
     if (bx2) { const float2 q = __ldg(bx2 + i); kh += q.x; kl += q.y; }
-    const double p = pv ? pv[r] : __ldg(pi + i);
-    acc = fma(f2d_exact(kh), p, acc);
+    const double p = P.get(r, pg, lane);
+    acc[r & 1] = fma(f2d_exact(kh), p, acc[r & 1]);
     if (ky2 || bx2) accl = fmaf(kl, d2f_round(p), accl);
   }
-  return acc + f2d_exact(accl);
+  if (ky2 || bx2) acc[1] += f2d_exact(accl);
 }
 
 /* Fused lattice integrand over units u0 + uu, uu < nu (block per unit, warps
    over its sites): partial[k][t] = (sum, compensation) of the unit's pairs,
    warp sums in site order, block sum in warp order. */
-template <typename S>
-__global__ void __launch_bounds__(256) lattice_asm_kernel(DevMaps M, const __grid_constant__ LatticeArgs A,
+/* 4-warp blocks, up to 6 per SM (<= 80 registers): the assembly is latency
+   bound, and 24 resident warps per SM beat 16 unconstrained ones */
+template <typename S, bool BATCH>
+__global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __grid_constant__ LatticeArgs A,
                                                           const LatticeArgs *jobs, int njobs,
                                                           size_t u0, size_t nu, int wpb)
 {
   AsmSmem L = carve_asm(wpb);
   asm_prologue(M, L);
   __shared__ double red_s[32], red_c[32];
+  /* a batch's job descriptor is staged in shared memory per unit; a single
+     lattice reads its own from the kernel parameters */
+  __shared__ LatticeArgs sj;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool f32 = sizeof(S) == 4;
   for (size_t uu = blockIdx.x; uu < nu; uu += gridDim.x) {
     const size_t u = u0 + uu;
-    const LatticeArgs &J = job_of(A, jobs, njobs, u);
+    if (BATCH) {
+      if (threadIdx.x == 0) sj = job_of(A, jobs, njobs, u);
+      __syncthreads();
+    }
+    const LatticeArgs &J = BATCH ? sj : A;
     const size_t ul = u - J.u_begin;
     const size_t k = ul / J.tiles, t = ul % J.tiles;
-    double s = 0.0, c = 0.0;
+    /* each lane accumulates its components over the warp's pairs of the
+       unit in FP64 (a fixed order); one warp reduction per unit */
+    double acc[2] = {0.0, 0.0};
     for (int j = warp; j < kTile; j += wpb) {
       const size_t n = t * kTile + j;
       if (n >= J.ny) break;
       const size_t r = uu * kTile + j;
       bool perm, t64;
       const bool live = asm_pair<S>(L, M, A.rec + r * REC, A.code[r], lane, perm, t64);
-      const double *pi = J.pi ? J.pi + (k * J.ny + n) * 384 : nullptr;
-      double pvv[12];
-      if (!J.pi) pi_generate(J.pi_seed, J.pi_stream, J.k0 + k, J.n0 + n, A.env[r], lane, pvv);
-      const double *ky = J.Ky ? J.Ky + n * 384 : nullptr;
-      const double *bx = J.Bx ? J.Bx + k * 384 : nullptr;
+      const double *ky = J.Ky ? J.Ky + n * 384 : nullptr, *bx = J.Bx ? J.Bx + k * 384 : nullptr;
       const float2 *ky2 = (f32 && J.Ky2) ? J.Ky2 + n * 384 : nullptr;
       const float2 *bx2 = (f32 && J.Bx2) ? J.Bx2 + k * 384 : nullptr;
-      double acc = contract(L, live, perm, t64, pi, J.pi ? nullptr : pvv, ky, bx, ky2, bx2, lane);
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-      kadd(s, c, acc);
+      if (J.pi) {
+        const PiSrc<false> P{J.pi + (k * J.ny + n) * 384};
+        contract<false>(L, live, perm, t64, P, ky, bx, ky2, bx2, lane, acc);
+      } else {
+        const PiSrc<true> P{J.pi_seed, J.pi_stream, J.k0 + k, J.n0 + n, A.env[r]};
+        contract<true>(L, live, perm, t64, P, ky, bx, ky2, bx2, lane, acc);
+      }
       __syncwarp();
+    }
+    /* lanes combined in a fixed tree with compensation */
+    double s = acc[0], c = 0.0;
+    kadd(s, c, acc[1]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double so = __shfl_xor_sync(0xffffffffu, s, off);
+      const double co = __shfl_xor_sync(0xffffffffu, c, off);
+      kadd(s, c, so);
+      c += co;
     }
     if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
     __syncthreads();
@@ -1857,8 +1907,10 @@ static cudaError_t prep_kernel_smem(const void *fn, size_t bytes)
     for (const auto &a : g_attr)
       if (a.dev == dev && a.fn == fn && a.threads == -1 && a.smem >= bytes) return cudaSuccess;
   }
-  const cudaError_t e =
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess) {
     std::lock_guard<std::mutex> g(g_attr_mu);
     g_attr.push_back({dev, fn, -1, bytes, 0});
@@ -1878,9 +1930,10 @@ static double orig2_of(const LaunchCfg &cfg)
   return r * r;
 }
 
+/* warps per assembly block: at most 4 (the lattice kernel's launch bound) */
 static int asm_warps(const LaunchCfg &cfg)
 {
-  return cfg.warps_per_block > 0 ? std::min(cfg.warps_per_block, 8) : 8;
+  return cfg.warps_per_block > 0 ? std::min(cfg.warps_per_block, 4) : 4;
 }
 
 /* record-kernel grid: thread per pair, 64 threads per block */
@@ -1938,19 +1991,31 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
   if (!a.rec || !a.code || a.rec_cap < (size_t)kTile) return cudaErrorInvalidValue;
   const int wpb = asm_warps(cfg);
   const size_t smem = asm_smem_bytes(wpb);
-  cudaError_t e = prep_kernel_smem((const void *)lattice_asm_kernel<S>, smem);
+  const void *afn = njobs ? (const void *)lattice_asm_kernel<S, true>
+                          : (const void *)lattice_asm_kernel<S, false>;
+  cudaError_t e = prep_kernel_smem(afn, smem);
   if (e != cudaSuccess) return e;
-  const size_t ablocks0 = grid_blocks((const void *)lattice_asm_kernel<S>, wpb * 32, smem);
+  const size_t ablocks0 = grid_blocks(afn, wpb * 32, smem);
   const int mixed = sizeof(S) == 4;
   const size_t cu = a.rec_cap / kTile;
   for (size_t u0 = 0; u0 < units; u0 += cu) {
     const size_t nu = std::min(cu, units - u0);
-    lattice_rec_kernel<SI><<<rec_grid(lattice_rec_kernel<SI>, nu * kTile), 64, 0, s>>>(
-        T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg));
+    if (njobs)
+      lattice_rec_kernel<SI, true><<<rec_grid(lattice_rec_kernel<SI, true>, nu * kTile), 64, 0, s>>>(
+          T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg));
+    else
+      lattice_rec_kernel<SI, false><<<rec_grid(lattice_rec_kernel<SI, false>, nu * kTile), 64, 0,
+                                      s>>>(T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg),
+                                           orig2_of(cfg));
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
     blocks = std::min(blocks, nu);
-    lattice_asm_kernel<S><<<(unsigned)blocks, wpb * 32, smem, s>>>(M, a, jobs, njobs, u0, nu, wpb);
+    if (njobs)
+      lattice_asm_kernel<S, true><<<(unsigned)blocks, wpb * 32, smem, s>>>(M, a, jobs, njobs, u0,
+                                                                             nu, wpb);
+    else
+      lattice_asm_kernel<S, false><<<(unsigned)blocks, wpb * 32, smem, s>>>(M, a, jobs, njobs, u0,
+                                                                              nu, wpb);
     g_launches++;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }

@@ -164,7 +164,7 @@ struct Ctx {
   int device = 0;
   DevTables T{};
   DevMaps M{};
-  LaunchCfg cfg{8, 0, 4.0, 0.35};
+  LaunchCfg cfg{4, 0, 4.0, 0.35};
   std::vector<void *> allocs;
 };
 
@@ -469,7 +469,7 @@ static int setup_device(struct Grid_coeffs *G, Ctx *c)
   if (!c->M.ent_gen || !c->M.ent_zero || !c->M.row_gen || !c->M.row_zero) return fail("map upload failed");
   const char *wpb = getenv("KQED_WARPS_PER_BLOCK");
   const char *blk = getenv("KQED_BLOCKS");
-  if (wpb) c->cfg.warps_per_block = std::max(1, std::min(8, atoi(wpb)));
+  if (wpb) c->cfg.warps_per_block = std::max(1, std::min(4, atoi(wpb)));
   if (blk) c->cfg.blocks = std::max(0, atoi(blk));
   const char *nr = getenv("KQED_MIXED_NEAR");
   if (nr) c->cfg.near_ratio = std::max(1.0, std::min(64.0, atof(nr)));
@@ -1223,7 +1223,7 @@ int plan_tune(kqed_batch_plan *p, cudaStream_t s)
   double best = 1e300;
   LaunchCfg bc = p->cfg;
   size_t bchunk = full;
-  for (int w : {4, 8})
+  for (int w : {2, 4})
     for (int bpsm : {0, 2, 1})
       for (size_t ch : chunks) {
         LaunchCfg cfg = p->cfg;

@@ -88,7 +88,7 @@ def test_tuned_batch_plan(temps):
     plan.close()
     tuned = K().BatchPlan(temps, jobs, precision=0, tune=True)
     info = tuned.info()
-    assert info["tuned_ms"] > 0 and info["warps_per_block"] in (4, 8)
+    assert info["tuned_ms"] > 0 and info["warps_per_block"] in (2, 4)
     tuned.launch()
     torch.cuda.synchronize()
     for b, k in zip(base, keep):
