@@ -417,7 +417,10 @@ def run_gb300(args):
             "gpu_launches": launches,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_gflops / 1e3,
                          "unit": "TFLOP/s", "frac": achieved / (peak_gflops / 1e3),
-                         "traffic": None,
+                         "traffic": (F.table().get("TRAFFIC_BYTES_PER_PAIR", 0) * nx * ny
+                                     if args.precision == "fp64" else None),
+                         "traffic_unit": "bytes per launch (record + assembly kernels)",
+                         "traffic_source": F.table().get("traffic_source"),
                          "kernel": "lattice_rec_kernel<double> + lattice_asm_kernel<double>"
                                    if args.precision == "fp64" else
                                    "lattice_rec_kernel<float> + lattice_asm_kernel<float>",

@@ -1,15 +1,18 @@
 """Calibration of the FP64 work model in flops.py.
 
   python -m kqed_gb300.calibrate --run            launches one fused lattice sum (L2)
-                                                  per branch-uniform case; run it under
-                                                  ncu with the FP64 instruction counters
+                                                  per branch-uniform case (a record kernel
+                                                  and an assembly kernel each); run it
+                                                  under ncu with the FP64 instruction
+                                                  counters
   python -m kqed_gb300.calibrate --fit CSV        fits PER_K / FIXED / AXIS from the ncu CSV
                                                   and writes flops_table.json
 
 Cases: one x point against 4096 sites of a shifted 8^4 lattice (no site is 0
 or equal to x), at |x| in several grid cells (different Chebyshev lengths),
 plus x = 0 (every pair takes the x = 0 form).  Per-pair FP64 flops are the
-executed DFMA x 2 + DADD + DMUL of the launch divided by its pairs.
+executed DFMA x 2 + DADD + DMUL of the case's lattice record and assembly
+kernels divided by its pairs.
 """
 import argparse
 import csv
@@ -78,13 +81,18 @@ def fit(path, cases_path):
         if not hdr or len(r) != len(hdr):
             continue
         d = dict(zip(hdr, r))
-        if "lattice_fp64" not in d["Kernel Name"]:
+        name = d["Kernel Name"]
+        if "lattice_rec_kernel" not in name and "lattice_asm_kernel" not in name:
             continue
         v = float(d["Metric Value"].replace(",", ""))
         per_launch.setdefault(int(d["ID"]), {})[d["Metric Name"]] = v
-    launches = [per_launch[k] for k in sorted(per_launch)]
-    if len(launches) != len(cases):
-        raise SystemExit("expected %d lattice launches, found %d" % (len(cases), len(launches)))
+    ids = sorted(per_launch)
+    if len(ids) != 2 * len(cases):
+        raise SystemExit("expected %d lattice kernel launches, found %d" % (2 * len(cases), len(ids)))
+    launches = []
+    for i in range(len(cases)):
+        a, b = per_launch[ids[2 * i]], per_launch[ids[2 * i + 1]]
+        launches.append({m: a.get(m, 0.0) + b.get(m, 0.0) for m in set(a) | set(b)})
     pts = []
     axis = None
     for c, m in zip(cases, launches):
@@ -103,7 +111,8 @@ def fit(path, cases_path):
     (per_k, fixed), res, _, _ = np.linalg.lstsq(A, fl, rcond=None)
     table = {"PER_K": float(per_k), "FIXED": float(fixed), "AXIS": float(axis), "CONTRACT": 0.0,
              "CONTRACT_EXTRA": 0.0,
-             "source": "ncu executed FP64 ops of lattice_fp64_kernel, L2, calibrate.py",
+             "source": "ncu executed FP64 ops of lattice_rec_kernel + lattice_asm_kernel "
+                       "(FP64 form), L2, kqed_gb300/calibrate.py",
              "cases": cases}
     with open(os.path.join(HERE, "flops_table.json"), "w") as f:
         json.dump(table, f, indent=1)
