@@ -196,7 +196,7 @@ __device__ __noinline__ void interp_generic(const S *__restrict__ b00,
                                             const S *__restrict__ b01,
                                             const S *__restrict__ b10,
                                             const S *__restrict__ b11, int Ktop,
-                                            const Wts<S> &w, S twox, double *W)
+                                            const Wts<S> &w, S twox, S *W)
 {
   /* ---- pass 1: (QG0,dxQG0) (QL2,dxQL2) (QL4,dxQL4) (QG1,dxQG1) ---- */
   {
@@ -317,7 +317,7 @@ __device__ __noinline__ void interp_generic(const S *__restrict__ b00,
 template <typename S>
 __device__ __noinline__ void interp_column(const S *__restrict__ r0,
                                            const S *__restrict__ r1, int Ktop, const Wts<S> &w,
-                                           S twox, double *W)
+                                           S twox, S *W)
 {
   {
     Rc<S> A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
@@ -505,10 +505,12 @@ __device__ double accessv_d(const DevTables &T, int flag_hy, int use_y_derivs, i
 
 /* ------------------------------------------------------------ invariants */
 
-struct Inv {
-  double x, cb, y, xsq, ysq, xdoty, cborig, yorig, xmysq, xmy;
+/* pair invariants; F = double, or float for the mixed form's chain rule */
+template <typename F> struct InvT {
+  F x, cb, y, xsq, ysq, xdoty, cborig, yorig, xmysq, xmy;
   int flag2, ix, iy;
 };
+using Inv = InvT<double>;
 
 /* set_invariants, src/LIBFILES/getff-new.c:315-370 (grid search included) */
 __device__ __forceinline__ void invariants(const DevTables &T, const double *xv, const double *yv,
@@ -541,50 +543,54 @@ __device__ __forceinline__ void invariants(const DevTables &T, const double *xv,
 
 /* ------------------------------------------- chnr scalar parts (generic) */
 
-struct TS {
-  double ell1, ell2, ell3, d1x, d1y, d1cb, d2x, d2y, d2cb, d3x, d3y, d3cb;
+template <typename F> struct TSt {
+  F ell1, ell2, ell3, d1x, d1y, d1cb, d2x, d2y, d2cb, d3x, d3y, d3cb;
 };
+using TS = TSt<double>;
 
-struct VS {
-  double g2, dg1dx, dg1dy, dg1dcb, dg2dx, dg2dy, dg2dcb, dg3dx, dg3dy, dg3dcb;
-  double ddg2dxdx, ddg2dxdy, ddg2dxdcb, ddg2dydcb, ddg2dcbdcb;
-  double ddg3dxdx, ddg3dxdy, ddg3dxdcb, ddg3dydcb, ddg3dcbdcb;
-  double ddg1dxdx, ddg1dxdy, ddg1dxdcb, ddg1dydcb, ddg1dcbdcb;
-  double ddg1dydy, ddg2dydy;
+template <typename F> struct VSt {
+  F g2, dg1dx, dg1dy, dg1dcb, dg2dx, dg2dy, dg2dcb, dg3dx, dg3dy, dg3dcb;
+  F ddg2dxdx, ddg2dxdy, ddg2dxdcb, ddg2dydcb, ddg2dcbdcb;
+  F ddg3dxdx, ddg3dxdy, ddg3dxdcb, ddg3dydcb, ddg3dcbdcb;
+  F ddg1dxdx, ddg1dxdy, ddg1dxdcb, ddg1dydcb, ddg1dcbdcb;
+  F ddg1dydy, ddg2dydy;
 };
+using VS = VSt<double>;
 
 /* Constants of the x <-> (x-y) chain rule (chnr_dS.c:74-83, chnr_dT.c:240-275,
    chnr_dV.c:194-274), computed once per pair with reciprocals so the many
    divisions by |x-y| and |x-y|^2 of the reference become multiplications. */
-struct SwapK {
-  double ca, cd, or_, pc, q1, q2;   /* first derivatives */
-  double r, r2, k1, k2, k3, k4, k5, k6, k7, k8, k9, k10, qa, qb;   /* second derivatives */
+template <typename F> struct SwapKt {
+  F ca, cd, or_, pc, q1, q2;   /* first derivatives */
+  F r, r2, k1, k2, k3, k4, k5, k6, k7, k8, k9, k10, qa, qb;   /* second derivatives */
 };
+using SwapK = SwapKt<double>;
 
-__device__ __forceinline__ SwapK swap_consts(const Inv &I)
+template <typename F>
+__device__ __forceinline__ SwapKt<F> swap_consts(const InvT<F> &I)
 {
-  SwapK k;
-  const double x = I.x, y = I.yorig, xmy = I.xmy, xmysq = I.xmysq, ysq = I.ysq;
-  const double ca = I.cb, cb = I.cborig;
-  k.r = 1.0 / xmy;
-  k.r2 = 1.0 / xmysq;
-  const double r = k.r, r2 = k.r2, r3 = r2 * r, r4 = r2 * r2;
+  SwapKt<F> k;
+  const F x = I.x, y = I.yorig, xmy = I.xmy, xmysq = I.xmysq, ysq = I.ysq;
+  const F ca = I.cb, cb = I.cborig;
+  k.r = F(1.0) / xmy;
+  k.r2 = F(1.0) / xmysq;
+  const F r = k.r, r2 = k.r2, r3 = r2 * r, r4 = r2 * r2;
   k.ca = ca;
   k.cd = (y - x * cb) * r;
-  const double cd = k.cd, omc = 1.0 - ca * ca;
+  const F cd = k.cd, omc = F(1.0) - ca * ca;
   k.or_ = omc * r;
   k.pc = -(cb + ca * cd) * r;
   k.q1 = ysq * cd * r2;
   k.q2 = x * y * xmy * r2;
-  k.k1 = -3.0 * ca * omc * r2;
-  k.k2 = ysq * r3 * (cb + 3.0 * ca * cd);
+  k.k1 = -F(3.0) * ca * omc * r2;
+  k.k2 = ysq * r3 * (cb + F(3.0) * ca * cd);
   k.k3 = ysq * r2 * cd;
   k.k4 = y * r2 * (x * ca - xmy);
   k.k5 = x * y * r;
-  k.k6 = (2.0 * ca * cb + cd * (3.0 * ca * ca - 1.0)) * r2;
-  k.k7 = y * r3 * ((3.0 * cd * cd - 1.0) * y - 2.0 * xmy * cd);
+  k.k6 = (F(2.0) * ca * cb + cd * (F(3.0) * ca * ca - F(1.0))) * r2;
+  k.k7 = y * r3 * ((F(3.0) * cd * cd - F(1.0)) * y - F(2.0) * xmy * cd);
   k.k8 = x * r2 * (y * cd - xmy);
-  k.k9 = x * ysq * r4 * (xmy - 3.0 * y * cd);
+  k.k9 = x * ysq * r4 * (xmy - F(3.0) * y * cd);
   k.k10 = I.xsq * ysq * r3;
   k.qa = ysq * cd * r2;
   k.qb = x * y * xmy * r2;
@@ -592,62 +598,66 @@ __device__ __forceinline__ SwapK swap_consts(const Inv &I)
 }
 
 /* derivatives of g(x, ca, |x-y|) -> derivatives of g(x, cb, |y|) */
-__device__ __forceinline__ void swap3(const SwapK &k, double &dx, double &dcb, double &dy)
+template <typename F>
+__device__ __forceinline__ void swap3(const SwapKt<F> &k, F &dx, F &dcb, F &dy)
 {
-  const double ox = dx, ocb = dcb, oy = dy;
+  const F ox = dx, ocb = dcb, oy = dy;
   dx = ox + k.or_ * ocb + k.ca * oy;
   dcb = -(k.q1 * ocb + k.q2 * oy);
   dy = k.pc * ocb + k.cd * oy;
 }
 
 /* generic T scalars from the weights, chnr_dT.c:297-347 */
-__device__ void T_generic(const Inv &I, const double *W, TS &T)
+template <typename F>
+__device__ void T_generic(const InvT<F> &I, const F *W, TSt<F> &T)
 {
-  const double X = I.x, Y = I.y, cb = I.cb, xsq = I.xsq;
-  const double ysq = I.flag2 ? I.xmysq : I.ysq;
-  const double rX = 1.0 / X, rY = 1.0 / Y, rxsq = rX * rX, rysq = 1.0 / ysq;
-  const double c43 = (4.0 / 3.0) * rxsq * rxsq;
+  const F X = I.x, Y = I.y, cb = I.cb, xsq = I.xsq;
+  const F ysq = I.flag2 ? I.xmysq : I.ysq;
+  const F rX = F(1.0) / X, rY = F(1.0) / Y, rxsq = rX * rX, rysq = F(1.0) / ysq;
+  const F c43 = (F(4.0) / F(3.0)) * rxsq * rxsq;
   T.d2x = W[5]; T.d2y = W[6]; T.ell2 = W[7]; T.d2cb = W[4];
-  const double ell4 = W[11], d4x = W[9], d4y = W[10], d4cb = W[8];
-  const double v1 = W[15], dv1dx = W[13], dv1dy = W[14], dv1dcb = W[12];
-  const double ccq = cb * cb - 0.25;
-  const double xy = X * Y, xsqysq = xsq * ysq;
-  T.ell3 = 0.5 * ell4 * rxsq * rysq - Y * cb * T.ell2 * rX;
-  T.ell1 = c43 * (v1 - xsqysq * ccq * T.ell2 - 1.5 * xsq * xy * cb * T.ell3);
-  T.d3y = (-ell4 * rysq * rY + 0.5 * d4y * rysq - cb * X * T.ell2 - xy * cb * T.d2y) * rxsq;
-  T.d3cb = (0.5 * d4cb * rX * rysq - Y * T.ell2 - Y * cb * T.d2cb) * rX;
-  T.d3x = (-ell4 * rX * rysq + 0.5 * d4x * rysq + Y * cb * T.ell2 - xy * cb * T.d2x) * rxsq;
-  T.d1y = c43 * (dv1dy - 2.0 * xsq * Y * ccq * T.ell2 - xsqysq * ccq * T.d2y -
-                 1.5 * xsq * X * cb * T.ell3 - 1.5 * xsq * xy * cb * T.d3y);
-  T.d1cb = c43 * (dv1dcb - 2.0 * xsqysq * cb * T.ell2 - xsqysq * ccq * T.d2cb -
-                  1.5 * xsq * xy * T.ell3 - 1.5 * xsq * xy * cb * T.d3cb);
-  T.d1x = -4.0 * T.ell1 * rX +
-          c43 * (dv1dx - 2.0 * X * ysq * ccq * T.ell2 - xsqysq * ccq * T.d2x -
-                 4.5 * xsq * Y * cb * T.ell3 - 1.5 * xsq * xy * cb * T.d3x);
+  const F ell4 = W[11], d4x = W[9], d4y = W[10], d4cb = W[8];
+  const F v1 = W[15], dv1dx = W[13], dv1dy = W[14], dv1dcb = W[12];
+  const F ccq = cb * cb - F(0.25);
+  const F xy = X * Y, xsqysq = xsq * ysq;
+  T.ell3 = F(0.5) * ell4 * rxsq * rysq - Y * cb * T.ell2 * rX;
+  T.ell1 = c43 * (v1 - xsqysq * ccq * T.ell2 - F(1.5) * xsq * xy * cb * T.ell3);
+  T.d3y = (-ell4 * rysq * rY + F(0.5) * d4y * rysq - cb * X * T.ell2 - xy * cb * T.d2y) * rxsq;
+  T.d3cb = (F(0.5) * d4cb * rX * rysq - Y * T.ell2 - Y * cb * T.d2cb) * rX;
+  T.d3x = (-ell4 * rX * rysq + F(0.5) * d4x * rysq + Y * cb * T.ell2 - xy * cb * T.d2x) * rxsq;
+  T.d1y = c43 * (dv1dy - F(2.0) * xsq * Y * ccq * T.ell2 - xsqysq * ccq * T.d2y -
+                 F(1.5) * xsq * X * cb * T.ell3 - F(1.5) * xsq * xy * cb * T.d3y);
+  T.d1cb = c43 * (dv1dcb - F(2.0) * xsqysq * cb * T.ell2 - xsqysq * ccq * T.d2cb -
+                  F(1.5) * xsq * xy * T.ell3 - F(1.5) * xsq * xy * cb * T.d3cb);
+  T.d1x = -F(4.0) * T.ell1 * rX +
+          c43 * (dv1dx - F(2.0) * X * ysq * ccq * T.ell2 - xsqysq * ccq * T.d2x -
+                 F(4.5) * xsq * Y * cb * T.ell3 - F(1.5) * xsq * xy * cb * T.d3x);
 }
 
 /* XMYSWAP_T_contrib, chnr_dT.c:240-275 */
-__device__ void T_swap(const SwapK &k, TS &T)
+template <typename F>
+__device__ void T_swap(const SwapKt<F> &k, TSt<F> &T)
 {
   swap3(k, T.d2x, T.d2cb, T.d2y);
-  double e3x = -T.d3x, e3cb = -T.d3cb, e3y = -T.d3y;
+  F e3x = -T.d3x, e3cb = -T.d3cb, e3y = -T.d3y;
   T.ell3 = -T.ell3 - T.ell2;
   swap3(k, e3x, e3cb, e3y);
   T.d3x = e3x - T.d2x; T.d3cb = e3cb - T.d2cb; T.d3y = e3y - T.d2y;
-  double e1x = T.d1x, e1cb = T.d1cb, e1y = T.d1y;
-  T.ell1 = T.ell1 - T.ell2 - 2.0 * T.ell3;
+  F e1x = T.d1x, e1cb = T.d1cb, e1y = T.d1y;
+  T.ell1 = T.ell1 - T.ell2 - F(2.0) * T.ell3;
   swap3(k, e1x, e1cb, e1y);
-  T.d1x = e1x - T.d2x - 2.0 * T.d3x;
-  T.d1cb = e1cb - T.d2cb - 2.0 * T.d3cb;
-  T.d1y = e1y - T.d2y - 2.0 * T.d3y;
+  T.d1x = e1x - T.d2x - F(2.0) * T.d3x;
+  T.d1cb = e1cb - T.d2cb - F(2.0) * T.d3cb;
+  T.d1y = e1y - T.d2y - F(2.0) * T.d3y;
 }
 
 /* generic V scalars from the weights, chnr_dV.c:380-466 */
-__device__ void V_generic(const Inv &I, const double *W, double ystp, VS &D)
+template <typename F>
+__device__ void V_generic(const InvT<F> &I, const F *W, F ystp, VSt<F> &D)
 {
-  const double X = I.x, Y = I.y, cb = I.cb;
-  const double rX = 1.0 / X, rxsq = rX * rX;
-  const double yx = Y * rX, yxx = Y * rxsq, cbx = cb * rX;
+  const F X = I.x, Y = I.y, cb = I.cb;
+  const F rX = F(1.0) / X, rxsq = rX * rX;
+  const F yx = Y * rX, yxx = Y * rxsq, cbx = cb * rX;
   D.dg3dy = W[36];
   D.g2 = W[19]; D.dg2dy = W[18];
   D.ddg2dxdx = W[21]; D.dg2dx = W[23]; D.ddg2dxdy = W[22]; D.ddg2dxdcb = W[20];
@@ -657,45 +667,46 @@ __device__ void V_generic(const Inv &I, const double *W, double ystp, VS &D)
   D.dg1dx = D.dg3dx + yxx * cb * D.g2 - yx * cb * D.dg2dx;
   D.dg1dy = D.dg3dy - cbx * D.g2 - yx * cb * D.dg2dy;
   D.dg1dcb = D.dg3dcb - yx * D.g2 - yx * cb * D.dg2dcb;
-  D.ddg1dxdx = D.ddg3dxdx - 2.0 * yxx * rX * cb * D.g2 + 2.0 * yxx * cb * D.dg2dx - yx * cb * D.ddg2dxdx;
+  D.ddg1dxdx = D.ddg3dxdx - F(2.0) * yxx * rX * cb * D.g2 + F(2.0) * yxx * cb * D.dg2dx - yx * cb * D.ddg2dxdx;
   D.ddg1dxdy = D.ddg3dxdy + cb * rxsq * D.g2 + yxx * cb * D.dg2dy - cbx * D.dg2dx - yx * cb * D.ddg2dxdy;
   D.ddg1dxdcb = D.ddg3dxdcb + yxx * D.g2 + yxx * cb * D.dg2dcb - yx * D.dg2dx - yx * cb * D.ddg2dxdcb;
   D.ddg1dydcb = D.ddg3dydcb - D.g2 * rX - cbx * D.dg2dcb - yx * D.dg2dy - yx * cb * D.ddg2dydcb;
-  D.ddg1dcbdcb = D.ddg3dcbdcb - 2.0 * yx * D.dg2dcb - yx * cb * D.ddg2dcbdcb;
-  D.ddg2dydy = 0.0; D.ddg1dydy = 0.0;
+  D.ddg1dcbdcb = D.ddg3dcbdcb - F(2.0) * yx * D.dg2dcb - yx * cb * D.ddg2dcbdcb;
+  D.ddg2dydy = F(0.0); D.ddg1dydy = F(0.0);
   if (I.flag2) {
-    const double rs = 1.0 / ystp;
+    const F rs = F(1.0) / ystp;
     D.ddg2dydy = W[37] * rs;
-    const double ddg3dydy = W[38] * rs;
-    D.ddg1dydy = ddg3dydy - (Y * D.ddg2dydy + 2.0 * D.dg2dy) * cbx;
+    const F ddg3dydy = W[38] * rs;
+    D.ddg1dydy = ddg3dydy - (Y * D.ddg2dydy + F(2.0) * D.dg2dy) * cbx;
   }
 }
 
 /* XMYSWAP_V_contrib with v_flip2, chnr_dV.c:176-274, with the per-pair
-   constants of SwapK */
-__device__ void V_swap(VS *Dp, const SwapK &k)
+   constants of SwapKt<F> */
+template <typename F>
+__device__ void V_swap(VSt<F> *Dp, const SwapKt<F> &k)
 {
-  VS &D = *Dp;
-  VS F = D;
-  F.g2 = -D.g2; F.dg2dx = -D.dg2dx; F.dg2dy = -D.dg2dy; F.dg2dcb = -D.dg2dcb;
-  F.ddg2dxdx = -D.ddg2dxdx; F.ddg2dxdy = -D.ddg2dxdy; F.ddg2dydy = -D.ddg2dydy;
-  F.ddg2dxdcb = -D.ddg2dxdcb; F.ddg2dydcb = -D.ddg2dydcb; F.ddg2dcbdcb = -D.ddg2dcbdcb;
-  const double ca = k.ca, cd = k.cd, oR = k.or_, pc = k.pc;
-  D.g2 = F.g2;
-  D.dg2dx = F.dg2dx + oR * F.dg2dcb + ca * F.dg2dy;
-  D.dg2dcb = -(k.q1 * F.dg2dcb + k.q2 * F.dg2dy);
-  D.dg2dy = pc * F.dg2dcb + cd * F.dg2dy;
-  D.dg1dx = F.dg1dx + oR * F.dg1dcb + ca * F.dg1dy - D.dg2dx;
-  D.dg1dcb = -(k.q1 * F.dg1dcb + k.q2 * F.dg1dy) - D.dg2dcb;
-  D.dg1dy = pc * F.dg1dcb + cd * F.dg1dy - D.dg2dy;
+  VSt<F> &D = *Dp;
+  VSt<F> Fl = D;
+  Fl.g2 = -D.g2; Fl.dg2dx = -D.dg2dx; Fl.dg2dy = -D.dg2dy; Fl.dg2dcb = -D.dg2dcb;
+  Fl.ddg2dxdx = -D.ddg2dxdx; Fl.ddg2dxdy = -D.ddg2dxdy; Fl.ddg2dydy = -D.ddg2dydy;
+  Fl.ddg2dxdcb = -D.ddg2dxdcb; Fl.ddg2dydcb = -D.ddg2dydcb; Fl.ddg2dcbdcb = -D.ddg2dcbdcb;
+  const F ca = k.ca, cd = k.cd, oR = k.or_, pc = k.pc;
+  D.g2 = Fl.g2;
+  D.dg2dx = Fl.dg2dx + oR * Fl.dg2dcb + ca * Fl.dg2dy;
+  D.dg2dcb = -(k.q1 * Fl.dg2dcb + k.q2 * Fl.dg2dy);
+  D.dg2dy = pc * Fl.dg2dcb + cd * Fl.dg2dy;
+  D.dg1dx = Fl.dg1dx + oR * Fl.dg1dcb + ca * Fl.dg1dy - D.dg2dx;
+  D.dg1dcb = -(k.q1 * Fl.dg1dcb + k.q2 * Fl.dg1dy) - D.dg2dcb;
+  D.dg1dy = pc * Fl.dg1dcb + cd * Fl.dg1dy - D.dg2dy;
 #define SECOND(g, DXDX, DXDCB, DXDY, DYDCB, DCBDCB)                                           \
   {                                                                                           \
-    const double a = F.ddg##g##dxdx, b = F.ddg##g##dxdcb, c = F.ddg##g##dxdy;                 \
-    const double e = F.ddg##g##dcbdcb, f = F.ddg##g##dydcb, h = F.ddg##g##dydy;               \
-    const double gcb = F.dg##g##dcb, gy = F.dg##g##dy;                                        \
-    const double Bq = b + oR * e + ca * f, Cq = c + oR * f + ca * h;                          \
-    const double Pe = pc * e + cd * f, Pf = pc * f + cd * h;                                  \
-    const double Qe = k.qa * e + k.qb * f, Qf = k.qa * f + k.qb * h;                          \
+    const F a = Fl.ddg##g##dxdx, b = Fl.ddg##g##dxdcb, c = Fl.ddg##g##dxdy;                 \
+    const F e = Fl.ddg##g##dcbdcb, f = Fl.ddg##g##dydcb, h = Fl.ddg##g##dydy;               \
+    const F gcb = Fl.dg##g##dcb, gy = Fl.dg##g##dy;                                        \
+    const F Bq = b + oR * e + ca * f, Cq = c + oR * f + ca * h;                          \
+    const F Pe = pc * e + cd * f, Pf = pc * f + cd * h;                                  \
+    const F Qe = k.qa * e + k.qb * f, Qf = k.qa * f + k.qb * h;                          \
     DXDX = (a + oR * b + ca * c) + k.k1 * gcb + oR * Bq + oR * gy + ca * Cq;                  \
     DXDCB = k.k2 * gcb - k.k3 * Bq + k.k4 * gy - k.k5 * Cq;                                   \
     DXDY = (pc * b + cd * c) + k.k6 * gcb + oR * Pe + pc * gy + ca * Pf;                      \
@@ -703,7 +714,7 @@ __device__ void V_swap(VS *Dp, const SwapK &k)
     DCBDCB = k.k9 * gcb + k.k3 * Qe - k.k10 * gy + k.k5 * Qf;                                 \
   }
   SECOND(2, D.ddg2dxdx, D.ddg2dxdcb, D.ddg2dxdy, D.ddg2dydcb, D.ddg2dcbdcb)
-  double t1, t2, t3, t4, t5;
+  F t1, t2, t3, t4, t5;
   SECOND(1, t1, t2, t3, t4, t5)
 #undef SECOND
   D.ddg1dxdx = t1 - D.ddg2dxdx;
@@ -882,6 +893,8 @@ __device__ int V_taylor(const DevTables &T, VS &D, double x, double y, double xs
 /* --------------------------------------------------- records (phase A) */
 
 /* Destination of a pair's record: float (mixed form) or double */
+__device__ __forceinline__ double f2d_exact(float f);
+
 struct Sink {
   float *f;
   double *d;
@@ -890,21 +903,31 @@ struct Sink {
     if (d) d[i] = v;
     else f[i] = (float)v;
   }
+  /* float values (the mixed form's chain rule) enter FP64 records exactly,
+     without FP64-pipe conversions */
+  __device__ __forceinline__ void put(int i, float v) const
+  {
+    if (d) d[i] = f2d_exact(v);
+    else f[i] = v;
+  }
 };
 
 /* everything phase B needs about a generic pair, given its S/T/V scalars
    (post swap): the per-index vectors of chnr_dS/dT loops and get_dv
    (chnr_dV.c:277-325) */
-__device__ void fill_generic_record(const Sink &R, const double *xv, const double *yv, const Inv &I,
-                                    double dg0dx, double dg0dy, double dg0dcb, const TS &T,
-                                    const VS &D)
+template <typename F>
+__device__ void fill_generic_record(const Sink &R, const double *xvd, const double *yvd, const InvT<F> &I,
+                                    F dg0dx, F dg0dy, F dg0dcb, const TSt<F> &T,
+                                    const VSt<F> &D)
 {
-  const double x = I.x, y = I.yorig, cb = I.cborig;
-  const double rX = 1.0 / x, rY = 1.0 / y;
+  F xv[4], yv[4];
+  for (int m = 0; m < 4; m++) { xv[m] = F(xvd[m]); yv[m] = F(yvd[m]); }
+  const F x = I.x, y = I.yorig, cb = I.cborig;
+  const F rX = F(1.0) / x, rY = F(1.0) / y;
   for (int m = 0; m < 4; m++) {
     R.put(R_XV + m, xv[m]);
     R.put(R_YV + m, yv[m]);
-    const double xh = xv[m] * rX, yh = yv[m] * rY;
+    const F xh = xv[m] * rX, yh = yv[m] * rY;
     R.put(R_XH + m, xh);
     R.put(R_YH + m, yh);
     R.put(R_C2 + m, (xh - cb * yh) * rY);
@@ -928,8 +951,8 @@ __device__ void fill_generic_record(const Sink &R, const double *xv, const doubl
     R.put(R_VD + 28 + m, (xv[m] * D.dg1dcb + yv[m] * D.dg2dcb) * rX);
   }
   for (int m = 0; m < 4; m++) {
-    const double xh = xv[m] * rX, yh = yv[m] * rY;
-    const double c4 = (yh - cb * xh) * rX;
+    const F xh = xv[m] * rX, yh = yv[m] * rY;
+    const F c4 = (yh - cb * xh) * rX;
     R.put(R_VA + m, (D.dg1dx + D.dg2dx) * xh + (D.dg1dcb + D.dg2dcb) * c4);
     R.put(R_VB + m, (D.dg1dx * xh + D.dg1dy * yh + D.dg1dcb * (xh * rY + yh * rX - cb * (xh * rX + yh * rY))));
   }
@@ -1039,11 +1062,41 @@ __device__ __forceinline__ bool is_zero4(const double *v)
   return (v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3]) < 1E-28;
 }
 
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(float v) { return f2d_exact(v); }
+__device__ __forceinline__ float d2f_round(double v);
+
+/* the chain rule of a generic pair in float (mixed form), from the float
+   weight functions; FP64 invariants rounded to float */
+__device__ __noinline__ void fill_record_f32(const Sink &R, const double *xv, const double *yv,
+                                             const Inv &I, const float *W, double ystp)
+{
+  InvT<float> If;
+  If.x = d2f_round(I.x); If.cb = d2f_round(I.cb); If.y = d2f_round(I.y);
+  If.xsq = d2f_round(I.xsq); If.ysq = d2f_round(I.ysq); If.xdoty = d2f_round(I.xdoty);
+  If.cborig = d2f_round(I.cborig); If.yorig = d2f_round(I.yorig);
+  If.xmysq = d2f_round(I.xmysq); If.xmy = d2f_round(I.xmy);
+  If.flag2 = I.flag2; If.ix = I.ix; If.iy = I.iy;
+  float dg0dcb = W[0], dg0dx = W[1], dg0dy = W[2];
+  TSt<float> Ts;
+  VSt<float> D;
+  T_generic<float>(If, W, Ts);
+  V_generic<float>(If, W, d2f_round(ystp), D);
+  if (If.flag2) {
+    const SwapKt<float> k = swap_consts<float>(If);
+    swap3<float>(k, dg0dx, dg0dcb, dg0dy);
+    T_swap<float>(k, Ts);
+    V_swap<float>(&D, k);
+  }
+  fill_generic_record<float>(R, xv, yv, If, dg0dx, dg0dy, dg0dcb, Ts, D);
+}
+
 /* Phase A for one pair: classify (QED_kernel_L0, kernels.c:81-115), fill the
    record, return the kind and status bits. */
 template <typename S>
 __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, const Sink &R,
-                       int &status, const S *colx, const double *col64, bool f64pair)
+                       int &status, const S *colx, const double *col64, bool f64pair,
+                       bool chnr32 = false)
 {
   status = 0;
   /* non-finite input: the reference's grid search would run off the tables;
@@ -1111,7 +1164,11 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
     w.dd = (I.flag2 && !flag_hy && iy0 + 1 < T.nstpy - 1) ? 1.0 : 0.0;
     const int NK = T.NK;
     const int Ktop = max(__ldg(T.nfx + ix0), __ldg(T.nfx + ix1)) + 2;
-    double W[39];
+    /* the weight functions: FP64 (Wd) or, from the float interpolation,
+       float (Ws) */
+    double Wd[39];
+    S Ws[39];
+    bool wsf = false;
     Wts<S> ws;
     ws.xA = (S)w.xA; ws.xB = (S)w.xB; ws.xC1 = (S)w.xC1; ws.xC2 = (S)w.xC2; ws.lAx = (S)w.lAx;
     ws.yA = (S)w.yA; ws.yB = (S)w.yB; ws.yC1 = (S)w.yC1; ws.yC2 = (S)w.yC2; ws.lAy = (S)w.lAy;
@@ -1123,24 +1180,36 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
     if (cb64 && col64) {
       Wts<double> wd = w;
       interp_column<double>(col64 + (size_t)iy0 * NK * kRow, col64 + (size_t)iy1 * NK * kRow, Ktop,
-                            wd, 2.0 * I.cb, W);
+                            wd, 2.0 * I.cb, Wd);
     } else if (cb64) {
       const double *node = T.node;
       interp_generic<double>(node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow,
                              node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow,
                              node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow,
-                             node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, w, 2.0 * I.cb, W);
-    } else if (colx) {
-      interp_column<S>(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, ws,
-                       (S)(2.0 * I.cb), W);
+                             node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, w, 2.0 * I.cb, Wd);
     } else {
-      const S *node = node_table<S>(T);
-      const S *b00 = node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow;
-      const S *b01 = node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow;
-      const S *b10 = node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow;
-      const S *b11 = node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow;
-      interp_generic<S>(b00, b01, b10, b11, Ktop, ws, (S)(2.0 * I.cb), W);
+      if (colx) {
+        interp_column<S>(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, ws,
+                         (S)(2.0 * I.cb), Ws);
+      } else {
+        const S *node = node_table<S>(T);
+        const S *b00 = node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow;
+        const S *b01 = node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow;
+        const S *b10 = node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow;
+        const S *b11 = node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow;
+        interp_generic<S>(b00, b01, b10, b11, Ktop, ws, (S)(2.0 * I.cb), Ws);
+      }
+      wsf = true;
     }
+    if (sizeof(S) == 4 && wsf && chnr32) {
+      /* the mixed form's chain rule in float for the pairs it assembles in
+         float: S/T/V scalars, the x <-> (x-y) swap and the record */
+      fill_record_f32(R, xv, yv, I, reinterpret_cast<const float *>(Ws), T.ystp);
+      return K_GEN;
+    }
+    if (wsf)
+      for (int i = 0; i < 39; i++) Wd[i] = to_double(Ws[i]);
+    const double *W = Wd;
     dg0dcb = W[0]; dg0dx = W[1]; dg0dy = W[2];
     T_generic(I, W, Ts);
     V_generic(I, W, T.ystp, D);
@@ -1414,7 +1483,8 @@ __device__ __forceinline__ uint8_t pair_code(int kind, bool f64, int status)
 /* records of pairs p0 + r, r < np, of a batch (x[p], y[p]) */
 template <typename SI>
 __global__ void __launch_bounds__(64) l0_rec_kernel(DevTables T, L0Args A, size_t p0, size_t np,
-                                                    int mixed, double near2, double orig2)
+                                                    int mixed, double near2, double orig2,
+                                                    int chnr32)
 {
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < np;
        r += (size_t)gridDim.x * blockDim.x) {
@@ -1426,7 +1496,8 @@ __global__ void __launch_bounds__(64) l0_rec_kernel(DevTables T, L0Args A, size_
     sk.f = nullptr;
     sk.d = A.rec + r * REC;
     int status;
-    const int kind = phase_a<SI>(T, xv, yv, sk, status, (const SI *)nullptr, nullptr, f64);
+    const int kind = phase_a<SI>(T, xv, yv, sk, status, (const SI *)nullptr, nullptr, f64,
+                                 chnr32 != 0);
     A.code[r] = pair_code(kind, f64, status);
   }
 }
@@ -1457,7 +1528,7 @@ template <typename SI, bool BATCH>
 __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __grid_constant__ LatticeArgs A,
                                                          const LatticeArgs *jobs, int njobs,
                                                          size_t u0, size_t nu, int mixed,
-                                                         double near2, double orig2)
+                                                         double near2, double orig2, int chnr32)
 {
   const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
   for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nu * kTile;
@@ -1476,7 +1547,7 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
     int status;
     const SI *col = column_of<SI>(J);
     const int kind = phase_a<SI>(T, xv, yv, sk, status, col ? col + k * per_x : nullptr,
-                                 J.col ? J.col + k * per_x : nullptr, f64);
+                                 J.col ? J.col + k * per_x : nullptr, f64, chnr32 != 0);
     A.code[r] = pair_code(kind, f64, status);
     if (!J.pi) A.env[r] = pi_envelope(xv, yv);
   }
@@ -1958,8 +2029,8 @@ static cudaError_t launch_l0_t(const DevTables &T, const DevMaps &M, const L0Arg
   const int mixed = sizeof(S) == 4;
   for (size_t p0 = 0; p0 < a.n; p0 += a.rec_cap) {
     const size_t np = std::min(a.rec_cap, a.n - p0);
-    l0_rec_kernel<SI><<<rec_grid(l0_rec_kernel<SI>, np), 64, 0, s>>>(T, a, p0, np, mixed,
-                                                                     near2_of(cfg), orig2_of(cfg));
+    l0_rec_kernel<SI><<<rec_grid(l0_rec_kernel<SI>, np), 64, 0, s>>>(
+        T, a, p0, np, mixed, near2_of(cfg), orig2_of(cfg), cfg.chnr32);
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
     blocks = std::min(blocks, (np + wpb - 1) / wpb);
@@ -2002,11 +2073,11 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
     const size_t nu = std::min(cu, units - u0);
     if (njobs)
       lattice_rec_kernel<SI, true><<<rec_grid(lattice_rec_kernel<SI, true>, nu * kTile), 64, 0, s>>>(
-          T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg));
+          T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg), cfg.chnr32);
     else
       lattice_rec_kernel<SI, false><<<rec_grid(lattice_rec_kernel<SI, false>, nu * kTile), 64, 0,
                                       s>>>(T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg),
-                                           orig2_of(cfg));
+                                           orig2_of(cfg), cfg.chnr32);
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
     blocks = std::min(blocks, nu);

@@ -164,7 +164,7 @@ struct Ctx {
   int device = 0;
   DevTables T{};
   DevMaps M{};
-  LaunchCfg cfg{4, 0, 4.0, 0.35};
+  LaunchCfg cfg{4, 0, 4.0, 0.35, 0};
   std::vector<void *> allocs;
 };
 
@@ -475,6 +475,8 @@ static int setup_device(struct Grid_coeffs *G, Ctx *c)
   if (nr) c->cfg.near_ratio = std::max(1.0, std::min(64.0, atof(nr)));
   const char *orr = getenv("KQED_MIXED_ORIGIN");
   if (orr) c->cfg.origin_radius = std::max(0.0, std::min(10.0, atof(orr)));
+  const char *c32 = getenv("KQED_MIXED_CHNR32");
+  if (c32) c->cfg.chnr32 = atoi(c32) ? 1 : 0;
   return 0;
 }
 

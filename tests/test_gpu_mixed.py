@@ -7,7 +7,8 @@ Tolerances, written here and in the assertions:
     and sums);
   * pairs the mixed form assembles in FP64 (x = 0, y = 0, x = y,
     |x - y| < max(|x|, |y|) / 4 and max(|x|, |y|) < 0.35) equal the FP64
-    form bit for bit;
+    form to 1e-13 per pair (the same FP64 code, compiled into a different
+    kernel, may contract a*b + c*d into FMAs differently);
   * fused lattice sums: per x, |S_mixed - S_fp64| <= 1e-6 * rms_x(S_fp64),
     the integrand error the mixed form is built to meet.
 """
@@ -21,6 +22,7 @@ pytestmark = pytest.mark.gpu
 PAIR_MAX = 2e-5
 PAIR_MEDIAN = 1e-6
 SUM_TOL = 1e-6
+ROUTED_TOL = 1e-13
 
 
 @pytest.fixture(scope="module")
@@ -81,7 +83,8 @@ def test_mixed_fp64_routed_pairs_are_exact(temps):
     assert routed.all()
     a = K().kernel_batch(temps, 0, x, y, precision=K().KQED_FP64)
     b = K().kernel_batch(temps, 0, x, y, precision=K().KQED_FP32_MIXED)
-    assert np.array_equal(a, b)
+    err = norm_rel(b, a)
+    assert err.max() <= ROUTED_TOL, err.max()
 
 
 @pytest.mark.parametrize("variant", [0, 2, 3])
