@@ -427,6 +427,10 @@ def run_gb300(args):
                          "kernel_ms": kavg_ms,
                          "flops_per_launch": flops_launch,
                          "flops_source": F.table().get("source"),
+                         "note": "achieved = FP64-equivalent rate: the algorithm's FP64 operations "
+                                 "per pair (counted on its all-FP64 evaluation) over the launch "
+                                 "time; the record kernel runs on the FP64 pipe, the assembly "
+                                 "stage in double-float (~48-bit) arithmetic on the FP32 pipe",
                          "peak_source": "FP64 FMA-chain probe run by this bench (not in "
                                         "MEASURED_PEAKS.json)"},
             "cpu_baseline": cpu,

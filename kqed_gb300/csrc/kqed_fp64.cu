@@ -30,6 +30,7 @@
  * Everything is FP64.  The kernel is bound by GB300's FP64 pipe.
  */
 #include "kqed_internal.h"
+#include "kqed_df.h"
 
 #include <stdio.h>
 
@@ -1377,6 +1378,36 @@ __device__ __forceinline__ void apply_map_warp(const uint16_t *ent, const uint16
   }
 }
 
+/* the map in double-float (FP64 form): coefficients are 0, +-1/2, +-1, +-2,
+   so each product is an exact scaling; sums in double-float */
+__device__ __forceinline__ void apply_map_warp_df(const uint16_t *ent, const uint16_t *rows,
+                                                  const MapSched &M, const float *coef,
+                                                  const df *stv, df *tbuf, int lane)
+{
+#pragma unroll 1
+  for (int r = 0; r < kMapRounds; r++) {
+    const uint16_t *e = ent + M.off[r] + lane;
+    const int len = M.len[r];
+    df acc(0.0f, 0.0f);
+#pragma unroll 4
+    for (int q = 0; q < len; q++) {
+      const uint16_t v = e[q * 32];
+      acc += scale_exact(stv[v & 0xff], coef[v >> 8]);
+    }
+    tbuf[rows[r * 32 + lane]] = acc;
+  }
+}
+
+/* double -> double-float (hi = v rounded to float, lo = the rest rounded):
+   integer conversions and one exact FP64 subtraction */
+__device__ __forceinline__ df split_d(double v)
+{
+  const float h = d2f_round(v);
+  return df(h, d2f_round(v - f2d_exact(h)));
+}
+
+__device__ __forceinline__ double df_to_d(df a) { return f2d_exact(a.hi) + f2d_exact(a.lo); }
+
 __device__ __forceinline__ int mulam(int i)
 {
   const int rs = i >> 6, mu = (i >> 4) & 3, nu = (i >> 2) & 3, la = i & 3;
@@ -1605,6 +1636,20 @@ __device__ __forceinline__ void asm_prologue(const DevMaps &M, AsmSmem &L)
   __syncthreads();
 }
 
+/* the 384 components of one pair into tbuf, in double-float */
+__device__ __forceinline__ void assemble_df(const AsmSmem &L, const DevMaps &M, int kind,
+                                            const df *R, df *stv, df *tbuf, int lane)
+{
+  if (lane == 0) { stv[200] = df(0.0f, 0.0f); stv[201] = df(0.0f, 0.0f); }
+  if (kind == K_GEN) stv_generic<df>(R, stv, lane);
+  else if (kind == K_X0) stv_x0<df>(R, stv, lane);
+  else stv_y0<df>(R, stv, lane);
+  __syncwarp();
+  if (kind == K_GEN) apply_map_warp_df(L.eg, L.rg, M.gen, L.coeff, stv, tbuf, lane);
+  else apply_map_warp_df(L.ez, L.rz, M.zero, L.coeff, stv, tbuf, lane);
+  __syncwarp();
+}
+
 /* the 384 components of one pair into tbuf (type A) */
 template <typename A>
 __device__ __forceinline__ void assemble(const AsmSmem &L, const DevMaps &M, int kind, const A *R,
@@ -1656,9 +1701,12 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
   t64 = sizeof(S) == 8 || (code & 8);
   if (kind == K_NONE) return false;
   if (t64) {
-    for (int i = lane; i < REC; i += 32) L.rec[i] = __ldg(grec + i);
+    /* FP64 records assembled in double-float on the FP32 pipe */
+    df *rd = reinterpret_cast<df *>(L.rec);
+    for (int i = lane; i < REC; i += 32) rd[i] = split_d(__ldg(grec + i));
     __syncwarp();
-    assemble<double>(L, M, kind, L.rec, L.stv, L.tbuf, L.coefd, lane);
+    assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), reinterpret_cast<df *>(L.tbuf),
+                lane);
   } else {
     float *rf = reinterpret_cast<float *>(L.rec);
     for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));
@@ -1672,7 +1720,14 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
 __device__ __forceinline__ double kcomp(const AsmSmem &L, bool t64, bool perm, int i)
 {
   const int j = perm ? mulam(i) : i;
-  const double v = t64 ? L.tbuf[j] : (double)reinterpret_cast<const float *>(L.tbuf)[j];
+  const double v = t64 ? df_to_d(reinterpret_cast<const df *>(L.tbuf)[j])
+                       : (double)reinterpret_cast<const float *>(L.tbuf)[j];
+  return perm ? -v : v;
+}
+
+__device__ __forceinline__ df kcomp_df(const AsmSmem &L, bool perm, int i)
+{
+  const df v = reinterpret_cast<const df *>(L.tbuf)[perm ? mulam(i) : i];
   return perm ? -v : v;
 }
 
@@ -1752,15 +1807,21 @@ __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm,
 {
   double pg[4];
   if (t64 || !live) {
+    /* double-float components, terms and products; the pair's lane partial
+       joins the FP64 lane accumulator once */
+    df pacc(0.0f, 0.0f);
 #pragma unroll
     for (int r = 0; r < 12; r++) {
       if ((r & 3) == 0) P.group(r >> 2, pg, lane);
       const int i = r * 32 + lane;
-      double kv = live ? kcomp(L, true, perm, i) : 0.0;
-      if (ky) kv += __ldg(ky + i);
-      if (bx) kv += __ldg(bx + i);
-      acc[r & 1] = fma(kv, P.get(r, pg, lane), acc[r & 1]);
+      df kv = live ? kcomp_df(L, perm, i) : df(0.0f, 0.0f);
+      if (ky2) { const float2 q = __ldg(ky2 + i); kv += df(q.x, q.y); }
+      else if (ky) kv += split_d(__ldg(ky + i));
+      if (bx2) { const float2 q = __ldg(bx2 + i); kv += df(q.x, q.y); }
+      else if (bx) kv += split_d(__ldg(bx + i));
+      pacc += kv * split_d(P.get(r, pg, lane));
     }
+    acc[0] += df_to_d(pacc);
     return;
   }
   const float *tb = reinterpret_cast<const float *>(L.tbuf);
@@ -1796,7 +1857,6 @@ __global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __
      lattice reads its own from the kernel parameters */
   __shared__ LatticeArgs sj;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const bool f32 = sizeof(S) == 4;
   for (size_t uu = blockIdx.x; uu < nu; uu += gridDim.x) {
     const size_t u = u0 + uu;
     if (BATCH) {
@@ -1816,8 +1876,8 @@ __global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __
       bool perm, t64;
       const bool live = asm_pair<S>(L, M, A.rec + r * REC, A.code[r], lane, perm, t64);
       const double *ky = J.Ky ? J.Ky + n * 384 : nullptr, *bx = J.Bx ? J.Bx + k * 384 : nullptr;
-      const float2 *ky2 = (f32 && J.Ky2) ? J.Ky2 + n * 384 : nullptr;
-      const float2 *bx2 = (f32 && J.Bx2) ? J.Bx2 + k * 384 : nullptr;
+      const float2 *ky2 = J.Ky2 ? J.Ky2 + n * 384 : nullptr;
+      const float2 *bx2 = J.Bx2 ? J.Bx2 + k * 384 : nullptr;
       if (J.pi) {
         const PiSrc<false> P{J.pi + (k * J.ny + n) * 384};
         contract<false>(L, live, perm, t64, P, ky, bx, ky2, bx2, lane, acc);

@@ -887,14 +887,18 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.col = st.d_col.get(ncol);
   if (!R.col) return fail("out of device memory for x-column tables");
   CUDA_OK(launch_build_columns(c->T, d_x, nx, R.col, s));
-  if (mixed) {
-    /* ncol floats (an even count: kRow = 28 per row), then the float2 terms */
-    const size_t n32 = ncol + (R.Ky ? (ny + nx) * 384 * 2 : 0);
+  if (mixed || R.Ky) {
+    /* (mixed form) ncol floats, an even count (kRow = 28 per row); then the
+       per-site / per-x terms as float2 (both forms: the FP64 form contracts
+       in double-float) */
+    const size_t n32 = (mixed ? ncol : 0) + (R.Ky ? (ny + nx) * 384 * 2 : 0);
     float *b32 = reinterpret_cast<float *>(st.d_col32.get(n32 / 2 + 2));
     if (!b32) return fail("out of device memory for float tables");
-    R.col32 = b32;
-    b32 += ncol;
-    CUDA_OK(launch_build_columns32(c->T, d_x, nx, R.col32, s));
+    if (mixed) {
+      R.col32 = b32;
+      b32 += ncol;
+      CUDA_OK(launch_build_columns32(c->T, d_x, nx, R.col32, s));
+    }
     if (R.Ky) {
       /* the FP64-evaluated per-site / per-x terms, as float (hi, lo) pairs */
       R.Ky2 = reinterpret_cast<float2 *>(b32);
@@ -1117,7 +1121,7 @@ int plan_enqueue_terms(kqed_batch_plan *p, cudaStream_t s)
       if (run_l0(c, p->zeros, Y.d_y, Y.ny, Y.ky, nullptr, s, false, &p->rs)) return 1;
       CUDA_OK(launch_scale(Y.ky, -1.0, Y.ny * 384, s));
     }
-    if (mixed) CUDA_OK(launch_to_float2(Y.ky, Y.ky2, Y.ny * 384, s));
+    CUDA_OK(launch_to_float2(Y.ky, Y.ky2, Y.ny * 384, s));
   }
   for (size_t j = 0; j < p->jobs.size(); j++) {
     const kqed_lattice_job &J = p->jobs[j];
@@ -1141,7 +1145,7 @@ int plan_enqueue_terms(kqed_batch_plan *p, cudaStream_t s)
       CUDA_OK(launch_axpy(bx, p->bt[j], 1.0, J.nx * 384, s));
       break;
     }
-    if (mixed) CUDA_OK(launch_to_float2(bx, p->bx2[j], J.nx * 384, s));
+    CUDA_OK(launch_to_float2(bx, p->bx2[j], J.nx * 384, s));
   }
   return 0;
 }
@@ -1323,13 +1327,13 @@ extern "C" int kqed_batch_plan_create(const struct QED_kernel_temps *t, int njob
         p->yterms.push_back({J.d_y, J.ny, kind, nullptr, nullptr});
         Y = &p->yterms.back();
         if (plan_alloc(p, &Y->ky, J.ny * 384)) return 1;
-        if (mixed && plan_alloc(p, &Y->ky2, J.ny * 384)) return 1;
+        if (plan_alloc(p, &Y->ky2, J.ny * 384)) return 1;
       }
       A.Ky = Y->ky;
       A.Ky2 = Y->ky2;
       if (plan_alloc(p, &p->bx[j], J.nx * 384)) return 1;
       if (J.variant == 3 && plan_alloc(p, &p->bt[j], J.nx * 384)) return 1;
-      if (mixed && plan_alloc(p, &p->bx2[j], J.nx * 384)) return 1;
+      if (plan_alloc(p, &p->bx2[j], J.nx * 384)) return 1;
       A.Bx = p->bx[j];
       A.Bx2 = p->bx2[j];
     }
