@@ -1754,6 +1754,11 @@ __global__ void __launch_bounds__(256) l0_asm_kernel(DevMaps M, L0Args A, size_t
   }
 }
 
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 /* exact double value of a float by integer bit manipulation (zero and
    subnormal floats give zero), so the mixed form spends no FP64-pipe
    conversions on its float components */
@@ -1873,6 +1878,14 @@ __global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __
       const size_t n = t * kTile + j;
       if (n >= J.ny) break;
       const size_t r = uu * kTile + j;
+      /* the warp's next pair streams Pi (3 KB) and its per-site terms from
+         DRAM: start them towards L2 now, one 128-byte line per lane, so the
+         contraction after this pair's assembly finds them there */
+      const size_t nn = n + wpb;
+      if (nn < J.ny && j + wpb < kTile && lane < 24) {
+        if (J.pi) prefetch_l2(J.pi + (k * J.ny + nn) * 384 + lane * 16);
+        if (J.Ky2) prefetch_l2(J.Ky2 + nn * 384 + lane * 16);
+      }
       bool perm, t64;
       const bool live = asm_pair<S>(L, M, A.rec + r * REC, A.code[r], lane, perm, t64);
       const double *ky = J.Ky ? J.Ky + n * 384 : nullptr, *bx = J.Bx ? J.Bx + k * 384 : nullptr;
