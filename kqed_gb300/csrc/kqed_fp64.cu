@@ -1225,6 +1225,62 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
   return K_GEN;
 }
 
+/* The mixed form's lean phase A: only the pairs that are evaluated in float
+   end to end -- generic, on the grid (|x| >= XX[0]), not assembled in FP64,
+   |cb| <= 0.99 -- with float interpolation and the float chain rule.  It
+   returns -1 for every other pair, which the full phase A then handles; so
+   the lean record kernel carries none of the FP64 code paths (Taylor
+   branches, axis forms, FP64 Chebyshev sums) and their registers. */
+__device__ int phase_a_lean(const DevTables &T, const double *xv, const double *yv,
+                            const Sink &R, int &status, const float *colx)
+{
+  status = 0;
+  if (!isfinite(fabs(xv[0]) + fabs(xv[1]) + fabs(xv[2]) + fabs(xv[3]) + fabs(yv[0]) +
+                fabs(yv[1]) + fabs(yv[2]) + fabs(yv[3])))
+    return -1;
+  Inv I;
+  invariants(T, xv, yv, I);
+  const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
+  if (I.x > xhi || I.x < xlo || fabs(I.cb) > 0.99) return -1;
+  if (I.flag2) status |= 4;
+  const int flag_hx = (I.x >= xhi);
+  const int flag_hy = (I.y >= __ldg(T.YY + T.nstpy - 1));
+  const int ix0 = I.ix, ix1 = flag_hx ? I.ix : I.ix + 1;
+  const int iy0 = I.iy, iy1 = flag_hy ? I.iy : I.iy + 1;
+  Wts<float> ws;
+  if (flag_hx) {
+    ws.xA = 1.0f; ws.xB = 0.0f; ws.xC1 = 0.0f; ws.xC2 = 0.0f; ws.lAx = 1.0f;
+  } else {
+    const Herm h = herm(I.x, __ldg(T.XX + ix0), __ldg(T.XX + ix1));
+    ws.xA = d2f_round(h.A * h.D); ws.xB = d2f_round(h.B * h.D); ws.xC1 = d2f_round(h.C1 * h.D);
+    ws.xC2 = d2f_round(h.C2 * h.D); ws.lAx = d2f_round(h.lA);
+  }
+  if (flag_hy) {
+    ws.yA = 1.0f; ws.yB = 0.0f; ws.yC1 = 0.0f; ws.yC2 = 0.0f; ws.lAy = 1.0f;
+  } else {
+    const Herm h = herm(I.y, __ldg(T.YY + iy0), __ldg(T.YY + iy1));
+    ws.yA = d2f_round(h.A * h.D); ws.yB = d2f_round(h.B * h.D); ws.yC1 = d2f_round(h.C1 * h.D);
+    ws.yC2 = d2f_round(h.C2 * h.D); ws.lAy = d2f_round(h.lA);
+  }
+  ws.dd = (I.flag2 && !flag_hy && iy0 + 1 < T.nstpy - 1) ? 1.0f : 0.0f;
+  const int NK = T.NK;
+  const int Ktop = max(__ldg(T.nfx + ix0), __ldg(T.nfx + ix1)) + 2;
+  const float twox = d2f_round(2.0 * I.cb);
+  float Ws[39];
+  if (colx) {
+    interp_column<float>(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, ws,
+                         twox, Ws);
+  } else {
+    const float *node = T.node32;
+    interp_generic<float>(node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow,
+                          node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow,
+                          node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow,
+                          node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, ws, twox, Ws);
+  }
+  fill_record_f32(R, xv, yv, I, Ws, T.ystp);
+  return K_GEN;
+}
+
 /* ------------------------------------------------ phases B and C (warp) */
 
 /* 200 STV components of one generic pair into stv[] (lane-parallel):
@@ -1555,6 +1611,28 @@ __device__ __forceinline__ const LatticeArgs &job_of(const LatticeArgs &A,
 /* records of the pairs of lattice units u0 + uu, uu < nu; unit u of a
    lattice is (x_k, sites t*kTile .. t*kTile + kTile - 1), k = u' / tiles,
    t = u' % tiles, u' = u - u_begin; record r = uu * kTile + j */
+/* one lattice record r of a chunk starting at unit u0: the pair's job,
+   (x, site) indices, and whether it is a real pair (the last tile of a
+   lattice can be partial) */
+template <bool BATCH>
+__device__ __forceinline__ bool record_pair(const LatticeArgs &A, const LatticeArgs *jobs,
+                                            int njobs, size_t u0, size_t r,
+                                            const LatticeArgs *&Jp, size_t &k, size_t &n)
+{
+  const size_t u = u0 + r / kTile;
+  const LatticeArgs &J = BATCH ? job_of(A, jobs, njobs, u) : A;
+  const size_t ul = u - J.u_begin;
+  k = ul / J.tiles;
+  n = (ul % J.tiles) * kTile + r % kTile;
+  Jp = &J;
+  return n < J.ny;
+}
+
+/* records of the pairs of lattice units u0 + uu, uu < nu; unit u of a
+   lattice is (x_k, sites t*kTile .. t*kTile + kTile - 1), k = u' / tiles,
+   t = u' % tiles, u' = u - u_begin; record r = uu * kTile + j.  With
+   A.list, only the records A.list[0 .. *A.count) (the pairs the lean float
+   pass left). */
 template <typename SI, bool BATCH>
 __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __grid_constant__ LatticeArgs A,
                                                          const LatticeArgs *jobs, int njobs,
@@ -1562,13 +1640,14 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
                                                          double near2, double orig2, int chnr32)
 {
   const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
-  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nu * kTile;
-       r += (size_t)gridDim.x * blockDim.x) {
-    const size_t u = u0 + r / kTile;
-    const LatticeArgs &J = BATCH ? job_of(A, jobs, njobs, u) : A;
-    const size_t ul = u - J.u_begin;
-    const size_t k = ul / J.tiles, n = (ul % J.tiles) * kTile + r % kTile;
-    if (n >= J.ny) continue;
+  const size_t total = A.list ? (size_t)*A.count : nu * kTile;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = A.list ? (size_t)A.list[i] : i;
+    const LatticeArgs *Jp;
+    size_t k, n;
+    if (!record_pair<BATCH>(A, jobs, njobs, u0, r, Jp, k, n)) continue;
+    const LatticeArgs &J = *Jp;
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
     const bool f64 = mixed && fp64_assembly(xv, yv, near2, orig2);
@@ -1580,6 +1659,41 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
     const int kind = phase_a<SI>(T, xv, yv, sk, status, col ? col + k * per_x : nullptr,
                                  J.col ? J.col + k * per_x : nullptr, f64, chnr32 != 0);
     A.code[r] = pair_code(kind, f64, status);
+    if (!J.pi) A.env[r] = pi_envelope(xv, yv);
+  }
+}
+
+/* The mixed form's lean record kernel: the float pairs through
+   phase_a_lean; every other pair's record index is appended to A.list for
+   lattice_rec_kernel (order of the list is irrelevant: records are indexed) */
+template <bool BATCH>
+__global__ void __launch_bounds__(64) lattice_rec_lean_kernel(DevTables T,
+                                                              const __grid_constant__ LatticeArgs A,
+                                                              const LatticeArgs *jobs, int njobs,
+                                                              size_t u0, size_t nu, double near2,
+                                                              double orig2)
+{
+  const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nu * kTile;
+       r += (size_t)gridDim.x * blockDim.x) {
+    const LatticeArgs *Jp;
+    size_t k, n;
+    if (!record_pair<BATCH>(A, jobs, njobs, u0, r, Jp, k, n)) continue;
+    const LatticeArgs &J = *Jp;
+    double xv[4], yv[4];
+    for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
+    int kind = -1, status = 0;
+    if (!fp64_assembly(xv, yv, near2, orig2)) {
+      Sink sk;
+      sk.f = nullptr;
+      sk.d = A.rec + r * REC;
+      kind = phase_a_lean(T, xv, yv, sk, status, J.col32 ? J.col32 + k * per_x : nullptr);
+    }
+    if (kind < 0) {
+      A.list[atomicAdd(A.count, 1u)] = (uint32_t)r;
+      continue;
+    }
+    A.code[r] = pair_code(kind, false, status);
     if (!J.pi) A.env[r] = pi_envelope(xv, yv);
   }
 }
@@ -2142,14 +2256,32 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
   const size_t ablocks0 = grid_blocks(afn, wpb * 32, smem);
   const int mixed = sizeof(S) == 4;
   const size_t cu = a.rec_cap / kTile;
+  /* the mixed form runs the lean float record pass first and the full
+     record kernel over the pairs it left */
+  const bool lean = mixed && a.list && a.count;
   for (size_t u0 = 0; u0 < units; u0 += cu) {
     const size_t nu = std::min(cu, units - u0);
+    LatticeArgs al = a;
+    if (lean) {
+      if ((e = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+      if (njobs)
+        lattice_rec_lean_kernel<true><<<rec_grid(lattice_rec_lean_kernel<true>, nu * kTile), 64, 0,
+                                        s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
+                                             orig2_of(cfg));
+      else
+        lattice_rec_lean_kernel<false><<<rec_grid(lattice_rec_lean_kernel<false>, nu * kTile), 64, 0,
+                                         s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
+                                              orig2_of(cfg));
+      g_launches++;
+    } else {
+      al.list = nullptr;
+    }
     if (njobs)
       lattice_rec_kernel<SI, true><<<rec_grid(lattice_rec_kernel<SI, true>, nu * kTile), 64, 0, s>>>(
-          T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg), cfg.chnr32);
+          T, al, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg), cfg.chnr32);
     else
       lattice_rec_kernel<SI, false><<<rec_grid(lattice_rec_kernel<SI, false>, nu * kTile), 64, 0,
-                                      s>>>(T, a, jobs, njobs, u0, nu, mixed, near2_of(cfg),
+                                      s>>>(T, al, jobs, njobs, u0, nu, mixed, near2_of(cfg),
                                            orig2_of(cfg), cfg.chnr32);
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;

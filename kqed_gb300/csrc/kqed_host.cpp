@@ -576,17 +576,21 @@ static int check_variant_precision(int variant, int precision)
 static thread_local int tl_precision = KQED_FP64;
 
 /* record scratch for n pairs (capped at kRecPairs; launches are chunked):
-   records [cap][kRec], Pi envelopes [cap], codes [cap] bytes */
+   records [cap][kRec], Pi envelopes [cap], the mixed form's deferred-record
+   list [cap] + its count, codes [cap] bytes */
 static int rec_scratch(ThreadStage &st, size_t n, double **rec, uint8_t **code, size_t *cap,
-                       double **env = nullptr)
+                       double **env = nullptr, uint32_t **list = nullptr,
+                       unsigned **count = nullptr)
 {
   size_t c = std::min(std::max(n, (size_t)kTile), kRecPairs);
   c = (c + kTile - 1) / kTile * kTile;
-  double *b = st.d_rec.get(c * kRec + c + c / 8 + 1);
+  double *b = st.d_rec.get(c * kRec + c + c / 2 + 1 + c / 8 + 1);
   if (!b) return fail("out of device memory for %zu pair records", c);
   *rec = b;
   if (env) *env = b + c * kRec;
-  *code = reinterpret_cast<uint8_t *>(b + c * kRec + c);
+  if (list) *list = reinterpret_cast<uint32_t *>(b + c * kRec + c);
+  if (count) *count = reinterpret_cast<unsigned *>(b + c * kRec + c + c / 2);
+  *code = reinterpret_cast<uint8_t *>(b + c * kRec + c + c / 2 + 1);
   *cap = c;
   return 0;
 }
@@ -850,6 +854,8 @@ struct LatticeRun {
   const double *d_x, *d_y;
   size_t nx, ny;
   double *Ky, *Bx, *partial, *col, *rec, *env;
+  uint32_t *list;
+  unsigned *count;
   float2 *Ky2, *Bx2;
   float *col32;
   uint8_t *code;
@@ -874,7 +880,8 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.col = nullptr;
   R.tiles = (int)((ny + kTile - 1) / kTile);
   /* records first: the kernel-term launches below reuse the same scratch */
-  if (rec_scratch(st, nx * (size_t)R.tiles * kTile, &R.rec, &R.code, &R.rec_cap, &R.env))
+  if (rec_scratch(st, nx * (size_t)R.tiles * kTile, &R.rec, &R.code, &R.rec_cap, &R.env,
+                  &R.list, &R.count))
     return 1;
   if (lattice_terms(c, variant, d_x, nx, d_y, ny, &R.Ky, &R.Bx, s, st)) return 1;
   R.partial = st.d_tmp.get(nx * (size_t)std::max(R.tiles, 1) * 2);
@@ -916,13 +923,30 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
 {
   const size_t per_x = (size_t)R.c->T.nstpy * R.c->T.NK * kRow;
   const bool mixed = R.precision == KQED_FP32_MIXED;
-  LatticeArgs a{R.d_x + 4 * x0, R.d_y, nxc, R.ny, d_pi,
-                R.Ky, R.Bx ? R.Bx + 384 * x0 : nullptr,
-                R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1), R.tiles,
-                R.col ? R.col + per_x * x0 : nullptr,
-                R.Ky2, R.Bx2 ? R.Bx2 + 384 * x0 : nullptr,
-                R.col32 ? R.col32 + per_x * x0 : nullptr, R.rec, R.code, R.rec_cap, R.env,
-                R.pi_seed, R.pi_stream, R.x_offset + x0, R.y_offset};
+  LatticeArgs a{};
+  a.x = R.d_x + 4 * x0;
+  a.y = R.d_y;
+  a.nx = nxc;
+  a.ny = R.ny;
+  a.pi = d_pi;
+  a.Ky = R.Ky;
+  a.Bx = R.Bx ? R.Bx + 384 * x0 : nullptr;
+  a.partial = R.partial + 2 * x0 * (size_t)std::max(R.tiles, 1);
+  a.tiles = R.tiles;
+  a.col = R.col ? R.col + per_x * x0 : nullptr;
+  a.Ky2 = R.Ky2;
+  a.Bx2 = R.Bx2 ? R.Bx2 + 384 * x0 : nullptr;
+  a.col32 = R.col32 ? R.col32 + per_x * x0 : nullptr;
+  a.rec = R.rec;
+  a.code = R.code;
+  a.rec_cap = R.rec_cap;
+  a.env = R.env;
+  a.list = R.list;
+  a.count = R.count;
+  a.pi_seed = R.pi_seed;
+  a.pi_stream = R.pi_stream;
+  a.k0 = R.x_offset + x0;
+  a.n0 = R.y_offset;
   TimedLaunch tl;
   prof_begin(s, tl);
   if (mixed) CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s));
@@ -1342,11 +1366,13 @@ extern "C" int kqed_batch_plan_create(const struct QED_kernel_temps *t, int njob
   size_t cap = std::min(std::max(total_pairs, zmax), kRecPairs);
   cap = (cap + kTile - 1) / kTile * kTile;
   double *rb = nullptr;
-  if (plan_alloc(p, &rb, cap * kRec + cap + cap / 8 + 1)) return 1;
-  p->rs = {rb, reinterpret_cast<uint8_t *>(rb + cap * kRec + cap), cap};
+  if (plan_alloc(p, &rb, cap * kRec + cap + cap / 2 + 1 + cap / 8 + 1)) return 1;
+  p->rs = {rb, reinterpret_cast<uint8_t *>(rb + cap * kRec + cap + cap / 2 + 1), cap};
   p->shared = LatticeArgs{};
   p->shared.rec = rb;
   p->shared.env = rb + cap * kRec;
+  p->shared.list = reinterpret_cast<uint32_t *>(rb + cap * kRec + cap);
+  p->shared.count = reinterpret_cast<unsigned *>(rb + cap * kRec + cap + cap / 2);
   p->shared.code = p->rs.code;
   p->shared.rec_cap = cap;
   if (plan_alloc(p, &p->d_jobs, njobs)) return 1;

@@ -113,6 +113,8 @@ struct LatticeArgs {
   uint8_t *code;        /* [rec_cap] */
   size_t rec_cap;       /* pairs per record kernel launch (a multiple of kTile) */
   double *env;          /* [rec_cap] Pi envelope per record (generated Pi) */
+  uint32_t *list;       /* [rec_cap] mixed form: records left by the lean float pass */
+  unsigned *count;      /* entries in list */
   uint64_t pi_seed;     /* generated Pi: Philox key */
   uint32_t pi_stream;   /* generated Pi: fourth counter word */
   size_t k0;            /* generated Pi: global index of x[0] */
