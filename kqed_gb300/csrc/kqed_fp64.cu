@@ -1444,13 +1444,22 @@ __device__ __forceinline__ void apply_map_warp_df(const uint16_t *ent, const uin
   for (int r = 0; r < kMapRounds; r++) {
     const uint16_t *e = ent + M.off[r] + lane;
     const int len = M.len[r];
-    df acc(0.0f, 0.0f);
+    /* a row has at most ~20 terms: TwoSum of the high parts, the rounding
+       errors and low parts gathered in one float, one renormalisation at
+       the end */
+    float sh = 0.0f, sl = 0.0f;
 #pragma unroll 4
     for (int q = 0; q < len; q++) {
       const uint16_t v = e[q * 32];
-      acc += scale_exact(stv[v & 0xff], coef[v >> 8]);
+      const df t = scale_exact(stv[v & 0xff], coef[v >> 8]);
+      float hs, he;
+      two_sum(sh, t.hi, hs, he);
+      sh = hs;
+      sl += he + t.lo;
     }
-    tbuf[rows[r * 32 + lane]] = acc;
+    float h, l;
+    fast_two_sum(sh, sl, h, l);
+    tbuf[rows[r * 32 + lane]] = df(h, l);
   }
 }
 
