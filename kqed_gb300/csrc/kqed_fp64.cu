@@ -1463,15 +1463,17 @@ __device__ __forceinline__ void apply_map_warp_df(const uint16_t *ent, const uin
   }
 }
 
-/* double -> double-float (hi = v rounded to float, lo = the rest rounded):
-   integer conversions and one exact FP64 subtraction */
+/* double -> double-float (hi = v rounded to float, lo = the rest rounded;
+   v - hi is exact) and back.  Hardware conversions: in the double-float
+   assembly the FP64 pipe has room and the issue slots do not (measured 2.6%
+   faster than the integer conversions the float contraction uses). */
 __device__ __forceinline__ df split_d(double v)
 {
-  const float h = d2f_round(v);
-  return df(h, d2f_round(v - f2d_exact(h)));
+  const float h = __double2float_rn(v);
+  return df(h, __double2float_rn(v - (double)h));
 }
 
-__device__ __forceinline__ double df_to_d(df a) { return f2d_exact(a.hi) + f2d_exact(a.lo); }
+__device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
 
 __device__ __forceinline__ int mulam(int i)
 {
