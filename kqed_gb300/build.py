@@ -90,7 +90,6 @@ def build_lib(verbose=False):
     o_crc = os.path.join(OUT, "kqed_crc32c.o")
     jobs = [
         [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "--split-compile", "0",
                          "-Xptxas", "-v" if verbose else "-O3", "-c", cu, "-o", o_cu],
         ["g++"] + HOST_FLAGS + [lib_default, "-I" + os.path.join(CUDA_HOME, "include"),
                                 "-c", host, "-o", o_host],

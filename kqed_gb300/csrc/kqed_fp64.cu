@@ -1625,13 +1625,12 @@ __device__ __forceinline__ const LatticeArgs &job_of(const LatticeArgs &A,
 /* one lattice record r of a chunk starting at unit u0: the pair's job,
    (x, site) indices, and whether it is a real pair (the last tile of a
    lattice can be partial) */
-template <bool BATCH>
 __device__ __forceinline__ bool record_pair(const LatticeArgs &A, const LatticeArgs *jobs,
                                             int njobs, size_t u0, size_t r,
                                             const LatticeArgs *&Jp, size_t &k, size_t &n)
 {
   const size_t u = u0 + r / kTile;
-  const LatticeArgs &J = BATCH ? job_of(A, jobs, njobs, u) : A;
+  const LatticeArgs &J = job_of(A, jobs, njobs, u);
   const size_t ul = u - J.u_begin;
   k = ul / J.tiles;
   n = (ul % J.tiles) * kTile + r % kTile;
@@ -1644,7 +1643,7 @@ __device__ __forceinline__ bool record_pair(const LatticeArgs &A, const LatticeA
    t = u' % tiles, u' = u - u_begin; record r = uu * kTile + j.  With
    A.list, only the records A.list[0 .. *A.count) (the pairs the lean float
    pass left). */
-template <typename SI, bool BATCH>
+template <typename SI>
 __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __grid_constant__ LatticeArgs A,
                                                          const LatticeArgs *jobs, int njobs,
                                                          size_t u0, size_t nu, int mixed,
@@ -1657,7 +1656,7 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
     const size_t r = A.list ? (size_t)A.list[i] : i;
     const LatticeArgs *Jp;
     size_t k, n;
-    if (!record_pair<BATCH>(A, jobs, njobs, u0, r, Jp, k, n)) continue;
+    if (!record_pair(A, jobs, njobs, u0, r, Jp, k, n)) continue;
     const LatticeArgs &J = *Jp;
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
@@ -1677,7 +1676,6 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
 /* The mixed form's lean record kernel: the float pairs through
    phase_a_lean; every other pair's record index is appended to A.list for
    lattice_rec_kernel (order of the list is irrelevant: records are indexed) */
-template <bool BATCH>
 __global__ void __launch_bounds__(64) lattice_rec_lean_kernel(DevTables T,
                                                               const __grid_constant__ LatticeArgs A,
                                                               const LatticeArgs *jobs, int njobs,
@@ -1689,7 +1687,7 @@ __global__ void __launch_bounds__(64) lattice_rec_lean_kernel(DevTables T,
        r += (size_t)gridDim.x * blockDim.x) {
     const LatticeArgs *Jp;
     size_t k, n;
-    if (!record_pair<BATCH>(A, jobs, njobs, u0, r, Jp, k, n)) continue;
+    if (!record_pair(A, jobs, njobs, u0, r, Jp, k, n)) continue;
     const LatticeArgs &J = *Jp;
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
@@ -2275,25 +2273,14 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
     LatticeArgs al = a;
     if (lean) {
       if ((e = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
-      if (njobs)
-        lattice_rec_lean_kernel<true><<<rec_grid(lattice_rec_lean_kernel<true>, nu * kTile), 64, 0,
-                                        s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
-                                             orig2_of(cfg));
-      else
-        lattice_rec_lean_kernel<false><<<rec_grid(lattice_rec_lean_kernel<false>, nu * kTile), 64, 0,
-                                         s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
-                                              orig2_of(cfg));
+      lattice_rec_lean_kernel<<<rec_grid(lattice_rec_lean_kernel, nu * kTile), 64, 0, s>>>(
+          T, a, jobs, njobs, u0, nu, near2_of(cfg), orig2_of(cfg));
       g_launches++;
     } else {
       al.list = nullptr;
     }
-    if (njobs)
-      lattice_rec_kernel<SI, true><<<rec_grid(lattice_rec_kernel<SI, true>, nu * kTile), 64, 0, s>>>(
-          T, al, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg), cfg.chnr32);
-    else
-      lattice_rec_kernel<SI, false><<<rec_grid(lattice_rec_kernel<SI, false>, nu * kTile), 64, 0,
-                                      s>>>(T, al, jobs, njobs, u0, nu, mixed, near2_of(cfg),
-                                           orig2_of(cfg), cfg.chnr32);
+    lattice_rec_kernel<SI><<<rec_grid(lattice_rec_kernel<SI>, nu * kTile), 64, 0, s>>>(
+        T, al, jobs, njobs, u0, nu, mixed, near2_of(cfg), orig2_of(cfg), cfg.chnr32);
     g_launches++;
     size_t blocks = cfg.blocks > 0 ? (size_t)cfg.blocks : ablocks0;
     blocks = std::min(blocks, nu);
