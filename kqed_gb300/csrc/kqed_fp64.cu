@@ -1464,16 +1464,27 @@ __device__ __forceinline__ void apply_map_warp_df(const uint16_t *ent, const uin
 }
 
 /* double -> double-float (hi = v rounded to float, lo = the rest rounded;
-   v - hi is exact) and back.  Hardware conversions: in the double-float
-   assembly the FP64 pipe has room and the issue slots do not (measured 2.6%
-   faster than the integer conversions the float contraction uses). */
+   v - hi is exact) and back.  In the FP64 form's assembly kernel (HW) the
+   FP64 pipe has room and the issue slots do not, so hardware conversions
+   (2.6% faster there); in the mixed form's kernel the FP64 pipe is the
+   busier one, so conversions by integer bit manipulation. */
+template <bool HW = true>
 __device__ __forceinline__ df split_d(double v)
 {
-  const float h = __double2float_rn(v);
-  return df(h, __double2float_rn(v - (double)h));
+  if (HW) {
+    const float h = __double2float_rn(v);
+    return df(h, __double2float_rn(v - (double)h));
+  }
+  const float h = d2f_round(v);
+  return df(h, d2f_round(v - f2d_exact(h)));
 }
 
-__device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
+template <bool HW = true>
+__device__ __forceinline__ double df_to_d(df a)
+{
+  if (HW) return (double)a.hi + (double)a.lo;
+  return f2d_exact(a.hi) + f2d_exact(a.lo);
+}
 
 __device__ __forceinline__ int mulam(int i)
 {
@@ -1625,12 +1636,13 @@ __device__ __forceinline__ const LatticeArgs &job_of(const LatticeArgs &A,
 /* one lattice record r of a chunk starting at unit u0: the pair's job,
    (x, site) indices, and whether it is a real pair (the last tile of a
    lattice can be partial) */
+template <bool BATCH = true>
 __device__ __forceinline__ bool record_pair(const LatticeArgs &A, const LatticeArgs *jobs,
                                             int njobs, size_t u0, size_t r,
                                             const LatticeArgs *&Jp, size_t &k, size_t &n)
 {
   const size_t u = u0 + r / kTile;
-  const LatticeArgs &J = job_of(A, jobs, njobs, u);
+  const LatticeArgs &J = BATCH ? job_of(A, jobs, njobs, u) : A;
   const size_t ul = u - J.u_begin;
   k = ul / J.tiles;
   n = (ul % J.tiles) * kTile + r % kTile;
@@ -1676,6 +1688,7 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
 /* The mixed form's lean record kernel: the float pairs through
    phase_a_lean; every other pair's record index is appended to A.list for
    lattice_rec_kernel (order of the list is irrelevant: records are indexed) */
+template <bool BATCH>
 __global__ void __launch_bounds__(64) lattice_rec_lean_kernel(DevTables T,
                                                               const __grid_constant__ LatticeArgs A,
                                                               const LatticeArgs *jobs, int njobs,
@@ -1687,7 +1700,7 @@ __global__ void __launch_bounds__(64) lattice_rec_lean_kernel(DevTables T,
        r += (size_t)gridDim.x * blockDim.x) {
     const LatticeArgs *Jp;
     size_t k, n;
-    if (!record_pair(A, jobs, njobs, u0, r, Jp, k, n)) continue;
+    if (!record_pair<BATCH>(A, jobs, njobs, u0, r, Jp, k, n)) continue;
     const LatticeArgs &J = *Jp;
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
@@ -1826,7 +1839,7 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
   if (t64) {
     /* FP64 records assembled in double-float on the FP32 pipe */
     df *rd = reinterpret_cast<df *>(L.rec);
-    for (int i = lane; i < REC; i += 32) rd[i] = split_d(__ldg(grec + i));
+    for (int i = lane; i < REC; i += 32) rd[i] = split_d<sizeof(S) == 8>(__ldg(grec + i));
     __syncwarp();
     assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), reinterpret_cast<df *>(L.tbuf),
                 lane);
@@ -1927,7 +1940,7 @@ template <> struct PiSrc<true> {
    where L1..L3's near-cancelling terms subtract exactly, and each component
    enters an FP64 product with Pi, so neither Pi nor the sum is rounded to
    float; the lo parts go through a float accumulator. */
-template <bool GEN>
+template <bool GEN, bool HW>
 __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm, bool t64,
                                          const PiSrc<GEN> &P, const double *ky, const double *bx,
                                          const float2 *ky2, const float2 *bx2, int lane,
@@ -1944,12 +1957,12 @@ __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm,
       const int i = r * 32 + lane;
       df kv = live ? kcomp_df(L, perm, i) : df(0.0f, 0.0f);
       if (ky2) { const float2 q = __ldg(ky2 + i); kv += df(q.x, q.y); }
-      else if (ky) kv += split_d(__ldg(ky + i));
+      else if (ky) kv += split_d<HW>(__ldg(ky + i));
       if (bx2) { const float2 q = __ldg(bx2 + i); kv += df(q.x, q.y); }
-      else if (bx) kv += split_d(__ldg(bx + i));
-      pacc += kv * split_d(P.get(r, pg, lane));
+      else if (bx) kv += split_d<HW>(__ldg(bx + i));
+      pacc += kv * split_d<HW>(P.get(r, pg, lane));
     }
-    acc[0] += df_to_d(pacc);
+    acc[0] += df_to_d<HW>(pacc);
     return;
   }
   const float *tb = reinterpret_cast<const float *>(L.tbuf);
@@ -2016,10 +2029,10 @@ __global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __
       const float2 *bx2 = J.Bx2 ? J.Bx2 + k * 384 : nullptr;
       if (J.pi) {
         const PiSrc<false> P{J.pi + (k * J.ny + n) * 384};
-        contract<false>(L, live, perm, t64, P, ky, bx, ky2, bx2, lane, acc);
+        contract<false, sizeof(S) == 8>(L, live, perm, t64, P, ky, bx, ky2, bx2, lane, acc);
       } else {
         const PiSrc<true> P{J.pi_seed, J.pi_stream, J.k0 + k, J.n0 + n, A.env[r]};
-        contract<true>(L, live, perm, t64, P, ky, bx, ky2, bx2, lane, acc);
+        contract<true, sizeof(S) == 8>(L, live, perm, t64, P, ky, bx, ky2, bx2, lane, acc);
       }
       __syncwarp();
     }
@@ -2273,8 +2286,14 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
     LatticeArgs al = a;
     if (lean) {
       if ((e = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
-      lattice_rec_lean_kernel<<<rec_grid(lattice_rec_lean_kernel, nu * kTile), 64, 0, s>>>(
-          T, a, jobs, njobs, u0, nu, near2_of(cfg), orig2_of(cfg));
+      if (njobs)
+        lattice_rec_lean_kernel<true><<<rec_grid(lattice_rec_lean_kernel<true>, nu * kTile), 64, 0,
+                                        s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
+                                             orig2_of(cfg));
+      else
+        lattice_rec_lean_kernel<false><<<rec_grid(lattice_rec_lean_kernel<false>, nu * kTile), 64, 0,
+                                         s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
+                                              orig2_of(cfg));
       g_launches++;
     } else {
       al.list = nullptr;
