@@ -1837,9 +1837,11 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
   t64 = sizeof(S) == 8 || (code & 8);
   if (kind == K_NONE) return false;
   if (t64) {
-    /* FP64 records assembled in double-float on the FP32 pipe */
+    /* FP64 records assembled in double-float on the FP32 pipe; the same
+       (hardware) split in both forms, so that the mixed form's FP64 pairs
+       come out bit-identical to the FP64 form's */
     df *rd = reinterpret_cast<df *>(L.rec);
-    for (int i = lane; i < REC; i += 32) rd[i] = split_d<sizeof(S) == 8>(__ldg(grec + i));
+    for (int i = lane; i < REC; i += 32) rd[i] = split_d(__ldg(grec + i));
     __syncwarp();
     assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), reinterpret_cast<df *>(L.tbuf),
                 lane);
