@@ -423,7 +423,8 @@ def run_gb300(args):
                          "traffic_source": F.table().get("traffic_source"),
                          "kernel": "lattice_rec_kernel<double> + lattice_asm_kernel<double>"
                                    if args.precision == "fp64" else
-                                   "lattice_rec_kernel<float> + lattice_asm_kernel<float>",
+                                   "lattice_rec_lean_kernel + lattice_rec_kernel<float> + "
+                                   "lattice_asm_kernel<float>",
                          "kernel_ms": kavg_ms,
                          "flops_per_launch": flops_launch,
                          "flops_source": F.table().get("source"),
