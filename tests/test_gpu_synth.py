@@ -87,3 +87,23 @@ def test_site_slabs_with_offsets_reproduce_the_full_sum(temps):
         parts.append(_gpu_local_sum(temps, 2, xs, ys[lo:hi], lo, None, 17, 4, K().KQED_FP64))
     got = combine_rank_order(parts)
     assert np.abs(got - full).max() <= 1e-13 * np.abs(full).max()
+
+
+def test_synth_lattice_workload_runs_small():
+    """the large-lattice workload (generated Pi, both forms) on an 8^4
+    lattice: one JSON line, FP64 checksum finite, mixed error within the
+    1e-6 integrand bound at this size"""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-m", "kqed_gb300.synth_lattice_workload", "--L", "8",
+                        "--nx", "4", "--steps", "1", "--warmup", "1"], cwd=root,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["evals_per_step"] == 4 * 8 ** 4
+    assert np.isfinite(d["checksum_fp64"])
+    assert d["fp32_mixed"]["err_vs_fp64"]["max"] <= 1e-6
+    assert len(d["fp32_mixed"]["err_vs_fp64"]["per_x"]) == 4
