@@ -86,6 +86,24 @@ KQED_HD df operator*(df a, df b)
   return df(h, l);
 }
 
+/* a * b + c with one renormalisation: the product's high part and c.hi
+   added by TwoSum, the low terms (product error, cross terms, c.lo) in
+   float.  Generic code calls fma(a, b, c) for double, float and df alike. */
+using ::fma;
+KQED_HD df fma(df a, df b, df c)
+{
+  const float p = a.hi * b.hi;
+  float e = df_fma(a.hi, b.hi, -p);
+  e = df_fma(a.hi, b.lo, e);
+  e = df_fma(a.lo, b.hi, e);
+  float s, t;
+  two_sum(p, c.hi, s, t);
+  t += e + c.lo;
+  float h, l;
+  fast_two_sum(s, t, h, l);
+  return df(h, l);
+}
+
 /* multiplication by a power of two or its negative (exact) */
 KQED_HD df scale_exact(df a, float c) { return df(a.hi * c, a.lo * c); }
 

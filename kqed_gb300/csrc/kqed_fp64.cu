@@ -48,6 +48,8 @@ __constant__ double cRa[4][kNKMax];
 __constant__ double cRb[4][kNKMax];
 __constant__ float cRaf[4][kNKMax];
 __constant__ float cRbf[4][kNKMax];
+__constant__ float2 cRadf[4][kNKMax];   /* the FP64 constants as (hi, lo) floats */
+__constant__ float2 cRbdf[4][kNKMax];
 
 int upload_map_constants()
 {
@@ -64,6 +66,15 @@ int upload_map_constants()
     for (int j = 0; j < kNKMax; j++) { raf[o][j] = (float)ra[o][j]; rbf[o][j] = (float)rb[o][j]; }
   if (cudaMemcpyToSymbol(cRaf, raf, sizeof(raf)) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(cRbf, rbf, sizeof(rbf)) != cudaSuccess) return 1;
+  float2 radf[4][kNKMax], rbdf[4][kNKMax];
+  for (int o = 0; o < 4; o++)
+    for (int j = 0; j < kNKMax; j++) {
+      const df a(ra[o][j]), b(rb[o][j]);
+      radf[o][j] = make_float2(a.hi, a.lo);
+      rbdf[o][j] = make_float2(b.hi, b.lo);
+    }
+  if (cudaMemcpyToSymbol(cRadf, radf, sizeof(radf)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(cRbdf, rbdf, sizeof(rbdf)) != cudaSuccess) return 1;
   return 0;
 }
 
@@ -153,9 +164,17 @@ template <typename S> __device__ __forceinline__ S fin0(const Rc<S> &r, S twox, 
 template <typename S> struct V2T;
 template <> struct V2T<double> { typedef double2 t; };
 template <> struct V2T<float> { typedef float2 t; };
+struct df2 { df x, y; };
+template <> struct V2T<df> { typedef df2 t; };
 template <typename S> __device__ __forceinline__ typename V2T<S>::t ld2(const S *p)
 {
   return __ldg(reinterpret_cast<const typename V2T<S>::t *>(p));
+}
+/* a (value, y-derivative) pair of a double-float column: one 16-byte load */
+template <> __device__ __forceinline__ df2 ld2<df>(const df *p)
+{
+  const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+  return df2{df(v.x, v.y), df(v.z, v.w)};
 }
 
 /* Clenshaw ratio constants in the arithmetic type */
@@ -165,6 +184,16 @@ template <> __device__ __forceinline__ double cra<double>(int o, int K) { return
 template <> __device__ __forceinline__ double crb<double>(int o, int K) { return cRb[o][K]; }
 template <> __device__ __forceinline__ float cra<float>(int o, int K) { return cRaf[o][K]; }
 template <> __device__ __forceinline__ float crb<float>(int o, int K) { return cRbf[o][K]; }
+template <> __device__ __forceinline__ df cra<df>(int o, int K)
+{
+  const float2 v = cRadf[o][K];
+  return df(v.x, v.y);
+}
+template <> __device__ __forceinline__ df crb<df>(int o, int K)
+{
+  const float2 v = cRbdf[o][K];
+  return df(v.x, v.y);
+}
 
 /* node table in the arithmetic type */
 template <typename S> __device__ __forceinline__ const S *node_table(const DevTables &T);
@@ -321,11 +350,11 @@ __device__ __noinline__ void interp_column(const S *__restrict__ r0,
                                            S twox, S *W)
 {
   {
-    Rc<S> A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
-    Rc<S> B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
-    Rc<S> C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
-    Rc<S> D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
-    S fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
+    Rc<S> A3o0 = {S(0), S(0)}, A3o1 = {S(0), S(0)}, A2o0 = {S(0), S(0)}, A1o0 = {S(0), S(0)};
+    Rc<S> B3o2 = {S(0), S(0)}, B3o3 = {S(0), S(0)}, B2o2 = {S(0), S(0)}, B1o2 = {S(0), S(0)};
+    Rc<S> C3o1 = {S(0), S(0)}, C3o2 = {S(0), S(0)}, C2o1 = {S(0), S(0)}, C1o1 = {S(0), S(0)};
+    Rc<S> D3o0 = {S(0), S(0)}, D3o1 = {S(0), S(0)}, D2o0 = {S(0), S(0)}, D1o0 = {S(0), S(0)};
+    S fA3 = S(0), fA2 = S(0), fA1 = S(0), fD3 = S(0), fD2 = S(0), fD1 = S(0);
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
@@ -358,11 +387,11 @@ __device__ __noinline__ void interp_column(const S *__restrict__ r0,
     W[12] = S(2) * D3o1.b; W[13] = fD1; W[14] = fD2; W[15] = fD3;
   }
   {
-    Rc<S> E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
-    Rc<S> F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
-    Rc<S> G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
-    Rc<S> H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
-    S fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
+    Rc<S> E3o1 = {S(0), S(0)}, E3o2 = {S(0), S(0)}, E3o3 = {S(0), S(0)}, E2o1 = {S(0), S(0)}, E2o2 = {S(0), S(0)}, Edo1 = {S(0), S(0)};
+    Rc<S> F3o1 = {S(0), S(0)}, F3o2 = {S(0), S(0)}, F2o1 = {S(0), S(0)}, F1o1 = {S(0), S(0)};
+    Rc<S> G3o0 = {S(0), S(0)}, G3o1 = {S(0), S(0)}, G2o0 = {S(0), S(0)}, G1o0 = {S(0), S(0)};
+    Rc<S> H3o1 = {S(0), S(0)}, H3o2 = {S(0), S(0)}, H2o0 = {S(0), S(0)}, H2o1 = {S(0), S(0)}, Hdo0 = {S(0), S(0)};
+    S fG3 = S(0), fG2 = S(0), fG1 = S(0), fH2 = S(0), fHd = S(0);
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
@@ -1066,6 +1095,12 @@ __device__ __forceinline__ bool is_zero4(const double *v)
 __device__ __forceinline__ double to_double(double v) { return v; }
 __device__ __forceinline__ double to_double(float v) { return f2d_exact(v); }
 __device__ __forceinline__ float d2f_round(double v);
+/* double -> (hi, lo) floats by integer conversions */
+__device__ __forceinline__ df split_int(double v)
+{
+  const float h = d2f_round(v);
+  return df(h, d2f_round(v - f2d_exact(h)));
+}
 
 /* the chain rule of a generic pair in float (mixed form), from the float
    weight functions; FP64 invariants rounded to float */
@@ -1097,7 +1132,7 @@ __device__ __noinline__ void fill_record_f32(const Sink &R, const double *xv, co
 template <typename S>
 __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, const Sink &R,
                        int &status, const S *colx, const double *col64, bool f64pair,
-                       bool chnr32 = false)
+                       bool chnr32 = false, const float2 *coldf = nullptr)
 {
   status = 0;
   /* non-finite input: the reference's grid search would run off the tables;
@@ -1188,6 +1223,22 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
                              node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow,
                              node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow,
                              node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, w, 2.0 * I.cb, Wd);
+    } else if (sizeof(S) == 8 && coldf && fabs(I.cb) <= 0.99) {
+      /* the FP64 form's Chebyshev sums in double-float on the FP32 pipe,
+         from the (hi, lo) copy of the FP64 columns; FP64 near cb = +-1.
+         Conversions by integer bit manipulation: this kernel's FP64 pipe is
+         its busy one. */
+      Wts<df> wf;
+      wf.xA = split_int(w.xA); wf.xB = split_int(w.xB); wf.xC1 = split_int(w.xC1);
+      wf.xC2 = split_int(w.xC2); wf.lAx = split_int(w.lAx);
+      wf.yA = split_int(w.yA); wf.yB = split_int(w.yB); wf.yC1 = split_int(w.yC1);
+      wf.yC2 = split_int(w.yC2); wf.lAy = split_int(w.lAy);
+      wf.dd = split_int(w.dd);
+      const df *cd = reinterpret_cast<const df *>(coldf);
+      df Wf[39];
+      interp_column<df>(cd + (size_t)iy0 * NK * kRow, cd + (size_t)iy1 * NK * kRow, Ktop, wf,
+                        split_int(2.0 * I.cb), Wf);
+      for (int i = 0; i < 39; i++) Wd[i] = f2d_exact(Wf[i].hi) + f2d_exact(Wf[i].lo);
     } else {
       if (colx) {
         interp_column<S>(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, ws,
@@ -1679,7 +1730,8 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
     int status;
     const SI *col = column_of<SI>(J);
     const int kind = phase_a<SI>(T, xv, yv, sk, status, col ? col + k * per_x : nullptr,
-                                 J.col ? J.col + k * per_x : nullptr, f64, chnr32 != 0);
+                                 J.col ? J.col + k * per_x : nullptr, f64, chnr32 != 0,
+                                 J.coldf ? J.coldf + k * per_x : nullptr);
     A.code[r] = pair_code(kind, f64, status);
     if (!J.pi) A.env[r] = pi_envelope(xv, yv);
   }

@@ -858,6 +858,7 @@ struct LatticeRun {
   unsigned *count;
   float2 *Ky2, *Bx2;
   float *col32;
+  float2 *coldf;
   uint8_t *code;
   size_t rec_cap;
   int tiles, precision, variant;
@@ -877,6 +878,7 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.x_offset = R.y_offset = 0;
   R.Ky2 = R.Bx2 = nullptr;
   R.col32 = nullptr;
+  R.coldf = nullptr;
   R.col = nullptr;
   R.tiles = (int)((ny + kTile - 1) / kTile);
   /* records first: the kernel-term launches below reuse the same scratch */
@@ -894,18 +896,24 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.col = st.d_col.get(ncol);
   if (!R.col) return fail("out of device memory for x-column tables");
   CUDA_OK(launch_build_columns(c->T, d_x, nx, R.col, s));
-  if (mixed || R.Ky) {
-    /* (mixed form) ncol floats, an even count (kRow = 28 per row); then the
-       per-site / per-x terms as float2 (both forms: the FP64 form contracts
-       in double-float) */
-    const size_t n32 = (mixed ? ncol : 0) + (R.Ky ? (ny + nx) * 384 * 2 : 0);
+  {
+    /* float tables: the mixed form's float columns (ncol floats) or the FP64
+       form's (hi, lo) copy of its columns (ncol float2), an even count of
+       floats (kRow = 28 per row) so the float2 tables after them stay
+       8-byte aligned; then the per-site / per-x terms as float2 (both forms:
+       the FP64 form contracts in double-float) */
+    const size_t ncf = mixed ? ncol : 2 * ncol;
+    const size_t n32 = ncf + (R.Ky ? (ny + nx) * 384 * 2 : 0);
     float *b32 = reinterpret_cast<float *>(st.d_col32.get(n32 / 2 + 2));
     if (!b32) return fail("out of device memory for float tables");
     if (mixed) {
       R.col32 = b32;
-      b32 += ncol;
       CUDA_OK(launch_build_columns32(c->T, d_x, nx, R.col32, s));
+    } else {
+      R.coldf = reinterpret_cast<float2 *>(b32);
+      CUDA_OK(launch_to_float2(R.col, R.coldf, ncol, s));
     }
+    b32 += ncf;
     if (R.Ky) {
       /* the FP64-evaluated per-site / per-x terms, as float (hi, lo) pairs */
       R.Ky2 = reinterpret_cast<float2 *>(b32);
@@ -937,6 +945,7 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
   a.Ky2 = R.Ky2;
   a.Bx2 = R.Bx2 ? R.Bx2 + 384 * x0 : nullptr;
   a.col32 = R.col32 ? R.col32 + per_x * x0 : nullptr;
+  a.coldf = R.coldf ? R.coldf + per_x * x0 : nullptr;
   a.rec = R.rec;
   a.code = R.code;
   a.rec_cap = R.rec_cap;
@@ -1194,6 +1203,9 @@ int plan_enqueue(kqed_batch_plan *p, cudaStream_t s)
     CUDA_OK(launch_build_columns(p->c->T, J.d_x, J.nx, const_cast<double *>(p->hj[j].col), s));
     if (mixed)
       CUDA_OK(launch_build_columns32(p->c->T, J.d_x, J.nx, const_cast<float *>(p->hj[j].col32), s));
+    else
+      CUDA_OK(launch_to_float2(p->hj[j].col, const_cast<float2 *>(p->hj[j].coldf),
+                               J.nx * (size_t)p->c->T.nstpy * p->c->T.NK * kRow, s));
   }
   if (plan_enqueue_terms(p, s)) return 1;
   if (plan_enqueue_kernels(p, p->cfg, s)) return 1;
@@ -1340,6 +1352,10 @@ extern "C" int kqed_batch_plan_create(const struct QED_kernel_temps *t, int njob
       float *c32 = nullptr;
       if (plan_alloc(p, &c32, J.nx * per_x)) return 1;
       A.col32 = c32;
+    } else {
+      float2 *cdf = nullptr;
+      if (plan_alloc(p, &cdf, J.nx * per_x)) return 1;
+      A.coldf = cdf;
     }
     if (J.variant) {
       /* per-site term, shared with earlier jobs on the same sites */

@@ -109,6 +109,8 @@ struct LatticeArgs {
   const double *col;    /* per-x column tables [nx][nstpy][NK][kRow] or NULL */
   const float2 *Ky2, *Bx2;   /* Ky, Bx as float (hi, lo) pairs, for the mixed form */
   const float *col32;        /* column tables in float, for the mixed form */
+  const float2 *coldf;       /* the FP64 column tables as (hi, lo) floats, for the FP64 form's
+                                double-float Chebyshev sums, or NULL */
   double *rec;          /* record scratch [rec_cap][kRec] */
   uint8_t *code;        /* [rec_cap] */
   size_t rec_cap;       /* pairs per record kernel launch (a multiple of kTile) */

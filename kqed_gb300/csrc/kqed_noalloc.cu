@@ -161,8 +161,19 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
     }
     if (bad) return kqed::set_error("kqed_lattice_sum_noalloc: kernel-term launch failed");
   }
-  kqed::LatticeArgs a{d_x, d_y, nx, ny, d_pi, Ky, Bx, partial, (int)tiles, nullptr,
-                      nullptr, nullptr, nullptr, RC.rec, RC.code, RC.cap};
+  kqed::LatticeArgs a{};
+  a.x = d_x;
+  a.y = d_y;
+  a.nx = nx;
+  a.ny = ny;
+  a.pi = d_pi;
+  a.Ky = Ky;
+  a.Bx = Bx;
+  a.partial = partial;
+  a.tiles = (int)tiles;
+  a.rec = RC.rec;
+  a.code = RC.code;
+  a.rec_cap = RC.cap;
   if (kqed::launch_lattice_fp64(T, M, a, cfg, s) != cudaSuccess ||
       kqed::launch_reduce_partials(partial, nx, (int)tiles, d_sums, s) != cudaSuccess)
     return kqed::set_error("kqed_lattice_sum_noalloc: lattice kernel launch failed");
