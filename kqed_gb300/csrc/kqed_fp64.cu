@@ -230,11 +230,11 @@ __device__ __noinline__ void interp_generic(const S *__restrict__ b00,
 {
   /* ---- pass 1: (QG0,dxQG0) (QL2,dxQL2) (QL4,dxQL4) (QG1,dxQG1) ---- */
   {
-    Rc<S> A3o0 = {0, 0}, A3o1 = {0, 0}, A2o0 = {0, 0}, A1o0 = {0, 0};
-    Rc<S> B3o2 = {0, 0}, B3o3 = {0, 0}, B2o2 = {0, 0}, B1o2 = {0, 0};
-    Rc<S> C3o1 = {0, 0}, C3o2 = {0, 0}, C2o1 = {0, 0}, C1o1 = {0, 0};
-    Rc<S> D3o0 = {0, 0}, D3o1 = {0, 0}, D2o0 = {0, 0}, D1o0 = {0, 0};
-    S fA3 = 0, fA2 = 0, fA1 = 0, fD3 = 0, fD2 = 0, fD1 = 0;
+    Rc<S> A3o0 = {S(0), S(0)}, A3o1 = {S(0), S(0)}, A2o0 = {S(0), S(0)}, A1o0 = {S(0), S(0)};
+    Rc<S> B3o2 = {S(0), S(0)}, B3o3 = {S(0), S(0)}, B2o2 = {S(0), S(0)}, B1o2 = {S(0), S(0)};
+    Rc<S> C3o1 = {S(0), S(0)}, C3o2 = {S(0), S(0)}, C2o1 = {S(0), S(0)}, C1o1 = {S(0), S(0)};
+    Rc<S> D3o0 = {S(0), S(0)}, D3o1 = {S(0), S(0)}, D2o0 = {S(0), S(0)}, D1o0 = {S(0), S(0)};
+    S fA3 = S(0), fA2 = S(0), fA1 = S(0), fD3 = S(0), fD2 = S(0), fD1 = S(0);
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
@@ -277,11 +277,11 @@ __device__ __noinline__ void interp_generic(const S *__restrict__ b00,
   }
   /* ---- pass 2: QG2 (8), dxQG2 (9), d2xQG2 (10), QG3 (11), dxQG3 (12), d2xQG3 (13) ---- */
   {
-    Rc<S> E3o1 = {0, 0}, E3o2 = {0, 0}, E3o3 = {0, 0}, E2o1 = {0, 0}, E2o2 = {0, 0}, Edo1 = {0, 0};
-    Rc<S> F3o1 = {0, 0}, F3o2 = {0, 0}, F2o1 = {0, 0}, F1o1 = {0, 0};
-    Rc<S> G3o0 = {0, 0}, G3o1 = {0, 0}, G2o0 = {0, 0}, G1o0 = {0, 0};
-    Rc<S> H3o1 = {0, 0}, H3o2 = {0, 0}, H2o0 = {0, 0}, H2o1 = {0, 0}, Hdo0 = {0, 0};
-    S fG3 = 0, fG2 = 0, fG1 = 0, fH2 = 0, fHd = 0;
+    Rc<S> E3o1 = {S(0), S(0)}, E3o2 = {S(0), S(0)}, E3o3 = {S(0), S(0)}, E2o1 = {S(0), S(0)}, E2o2 = {S(0), S(0)}, Edo1 = {S(0), S(0)};
+    Rc<S> F3o1 = {S(0), S(0)}, F3o2 = {S(0), S(0)}, F2o1 = {S(0), S(0)}, F1o1 = {S(0), S(0)};
+    Rc<S> G3o0 = {S(0), S(0)}, G3o1 = {S(0), S(0)}, G2o0 = {S(0), S(0)}, G1o0 = {S(0), S(0)};
+    Rc<S> H3o1 = {S(0), S(0)}, H3o2 = {S(0), S(0)}, H2o0 = {S(0), S(0)}, H2o1 = {S(0), S(0)}, Hdo0 = {S(0), S(0)};
+    S fG3 = S(0), fG2 = S(0), fG1 = S(0), fH2 = S(0), fHd = S(0);
 #pragma unroll 1
     for (int K = Ktop - 1; K >= 0; --K) {
       const int o = K * kRow;
@@ -1213,7 +1213,36 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
        assembles in FP64 and near cb = +-1, where their derivatives lose
        digits in float */
     const bool cb64 = sizeof(S) == 4 && (f64pair || fabs(I.cb) > 0.99);
-    if (cb64 && col64) {
+    /* the FP64 form's Chebyshev sums, and those of the float form's pairs
+       assembled in FP64 (so that both forms give such pairs the same bits),
+       in double-float on the FP32 pipe, from the (hi, lo) copy of the FP64
+       columns (FP64-form lattice sums) or of the node table (pair batches);
+       FP64 near cb = +-1.  Conversions by integer bit manipulation: the
+       record kernels' FP64 pipe is their busy one. */
+    const bool dfsum = (sizeof(S) == 8 || f64pair) && fabs(I.cb) <= 0.99 &&
+                       (coldf || (!colx && T.nodedf));
+    if (dfsum) {
+      Wts<df> wf;
+      wf.xA = split_int(w.xA); wf.xB = split_int(w.xB); wf.xC1 = split_int(w.xC1);
+      wf.xC2 = split_int(w.xC2); wf.lAx = split_int(w.lAx);
+      wf.yA = split_int(w.yA); wf.yB = split_int(w.yB); wf.yC1 = split_int(w.yC1);
+      wf.yC2 = split_int(w.yC2); wf.lAy = split_int(w.lAy);
+      wf.dd = split_int(w.dd);
+      df Wf[39];
+      if (coldf) {
+        const df *cd = reinterpret_cast<const df *>(coldf);
+        interp_column<df>(cd + (size_t)iy0 * NK * kRow, cd + (size_t)iy1 * NK * kRow, Ktop, wf,
+                          split_int(2.0 * I.cb), Wf);
+      } else {
+        const df *nd = reinterpret_cast<const df *>(T.nodedf);
+        interp_generic<df>(nd + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow,
+                           nd + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow,
+                           nd + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow,
+                           nd + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, wf,
+                           split_int(2.0 * I.cb), Wf);
+      }
+      for (int i = 0; i < 39; i++) Wd[i] = f2d_exact(Wf[i].hi) + f2d_exact(Wf[i].lo);
+    } else if (cb64 && col64) {
       Wts<double> wd = w;
       interp_column<double>(col64 + (size_t)iy0 * NK * kRow, col64 + (size_t)iy1 * NK * kRow, Ktop,
                             wd, 2.0 * I.cb, Wd);
@@ -1223,22 +1252,6 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
                              node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow,
                              node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow,
                              node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, w, 2.0 * I.cb, Wd);
-    } else if (sizeof(S) == 8 && coldf && fabs(I.cb) <= 0.99) {
-      /* the FP64 form's Chebyshev sums in double-float on the FP32 pipe,
-         from the (hi, lo) copy of the FP64 columns; FP64 near cb = +-1.
-         Conversions by integer bit manipulation: this kernel's FP64 pipe is
-         its busy one. */
-      Wts<df> wf;
-      wf.xA = split_int(w.xA); wf.xB = split_int(w.xB); wf.xC1 = split_int(w.xC1);
-      wf.xC2 = split_int(w.xC2); wf.lAx = split_int(w.lAx);
-      wf.yA = split_int(w.yA); wf.yB = split_int(w.yB); wf.yC1 = split_int(w.yC1);
-      wf.yC2 = split_int(w.yC2); wf.lAy = split_int(w.lAy);
-      wf.dd = split_int(w.dd);
-      const df *cd = reinterpret_cast<const df *>(coldf);
-      df Wf[39];
-      interp_column<df>(cd + (size_t)iy0 * NK * kRow, cd + (size_t)iy1 * NK * kRow, Ktop, wf,
-                        split_int(2.0 * I.cb), Wf);
-      for (int i = 0; i < 39; i++) Wd[i] = f2d_exact(Wf[i].hi) + f2d_exact(Wf[i].lo);
     } else {
       if (colx) {
         interp_column<S>(colx + (size_t)iy0 * NK * kRow, colx + (size_t)iy1 * NK * kRow, Ktop, ws,

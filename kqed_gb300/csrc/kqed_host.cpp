@@ -452,8 +452,16 @@ static int setup_device(struct Grid_coeffs *G, Ctx *c)
     for (size_t i = 0; i < node.size(); i++) node32[i] = (float)node[i];
     T.node32 = (const float *)dev_upload(c, node32.data(), sizeof(float) * node32.size());
   }
+  {
+    std::vector<float2> nodedf(node.size());
+    for (size_t i = 0; i < node.size(); i++) {
+      const float hi = (float)node[i];
+      nodedf[i] = make_float2(hi, (float)(node[i] - (double)hi));
+    }
+    T.nodedf = (const float2 *)dev_upload(c, nodedf.data(), sizeof(float2) * nodedf.size());
+  }
   T.nfx = (const int *)dev_upload(c, G->nfx, sizeof(int) * G->nstpx);
-  if (!T.XX || !T.YY || !T.TX || !T.TY || !T.node || !T.node32 || !T.nfx)
+  if (!T.XX || !T.YY || !T.TX || !T.TY || !T.node || !T.node32 || !T.nodedf || !T.nfx)
     return fail("device table upload failed");
   T.nstpx = G->nstpx; T.nstpy = G->nstpy; T.ny_tay = G->NY_tay; T.nx_tay = G->NX_tay; T.NK = NK;
   T.ystp = G->ystp;

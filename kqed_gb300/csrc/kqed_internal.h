@@ -52,6 +52,8 @@ struct DevTables {
   const double *TY;      /* [14][nx_tay] TAYLORY */
   const double *node;
   const float *node32;   /* the same table rounded to float (mixed-precision form) */
+  const float2 *nodedf;  /* the same table as (hi, lo) floats (the FP64 form's double-float
+                            Chebyshev sums in pair batches) */
   const int *nfx;
   int nstpx, nstpy, ny_tay, nx_tay, NK;
   double ystp;
