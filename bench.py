@@ -132,7 +132,7 @@ def cpu_impl():
         try:
             os.environ["KQEDREF_PATH"] = os.path.join(ROOT, "kqed_gb300")
             L = ctypes.CDLL(ref)
-            if L.ref_init() == 0:
+            if L.ref_init_threads(os.cpu_count() or 1) == 0:
                 def contract(v, x, y, pi, nt):
                     dp = ctypes.POINTER(ctypes.c_double)
                     d = np.zeros(len(x))

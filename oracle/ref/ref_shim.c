@@ -18,14 +18,28 @@ const char *kqedref_lib_path(void)
 
 static struct QED_kernel_temps T;
 static int T_ready = 0;
+/* the reference sizes its per-thread scratch by omp_get_max_threads() at
+   initialise (src/LIBFILES/init.c:119,178) and indexes it by thread number
+   in the kernels (src/LIBFILES/QED_kernel.c:449): no call may run more
+   threads than this */
+static int T_threads = 0;
 
 int ref_init(void)
 {
   if (T_ready) return 0;
   memset(&T, 0, sizeof(T));
+  T_threads = omp_get_max_threads();
   if (initialise(&T)) return 1;
   T_ready = 1;
   return 0;
+}
+
+/* ref_init with the reference's scratch sized for nthreads threads
+   (whatever OMP_NUM_THREADS says); no effect once initialised */
+int ref_init_threads(int nthreads)
+{
+  if (!T_ready && nthreads > 0) omp_set_num_threads(nthreads);
+  return ref_init();
 }
 
 void ref_free(void)
@@ -67,7 +81,7 @@ int ref_kernel(int variant, long n, const double *x, const double *y, double *ou
 {
   kfun f = pick(variant);
   if (!T_ready || !f) return 1;
-  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  if (nthreads <= 0 || nthreads > T_threads) nthreads = T_threads;
   long i;
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
   for (i = 0; i < n; i++) {
@@ -86,7 +100,7 @@ int ref_contract(int variant, long n, const double *x, const double *y,
 {
   kfun f = pick(variant);
   if (!T_ready || !f) return 1;
-  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  if (nthreads <= 0 || nthreads > T_threads) nthreads = T_threads;
   long i;
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
   for (i = 0; i < n; i++) {
