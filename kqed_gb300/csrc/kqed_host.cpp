@@ -160,7 +160,12 @@ struct Scratch {
   }
 };
 
+std::atomic<uint64_t> g_ctx_ids{0};
+
 struct Ctx {
+  /* unique for the life of the process: a later context may reuse a freed
+     one's address (and sit on another device) */
+  uint64_t id = ++g_ctx_ids;
   int device = 0;
   DevTables T{};
   DevMaps M{};
@@ -170,7 +175,7 @@ struct Ctx {
 
 /* per-thread staging for the per-pair legacy calls and batched host calls */
 struct ThreadStage {
-  Ctx *owner = nullptr;
+  uint64_t owner = 0;       /* Ctx::id of the context the streams and buffers serve */
   cudaStream_t stream = nullptr, copy_stream = nullptr;
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double *h_pin = nullptr;   /* 8 + 384 doubles */
@@ -191,7 +196,7 @@ struct ThreadStage {
     d_rec.release(); d_sa.release(); d_sb.release();
     stream = nullptr;
     h_pin = nullptr;
-    owner = nullptr;
+    owner = 0;
   }
 };
 
@@ -200,9 +205,9 @@ thread_local ThreadStage tl_stage;
 static ThreadStage &stage_for(Ctx *c)
 {
   ThreadStage &st = tl_stage;
-  if (st.owner != c) {
+  if (st.owner != c->id) {
     st.reset();
-    st.owner = c;
+    st.owner = c->id;
   }
   return st;
 }
@@ -524,7 +529,7 @@ extern "C" void free_QED_temps(struct QED_kernel_temps *t)
   if (!t) return;
   Ctx *c = ctx_of(t);
   if (c) {
-    if (tl_stage.owner == c) tl_stage.reset();
+    if (tl_stage.owner == c->id) tl_stage.reset();
     for (void *p : c->allocs) cudaFree(p);
     delete c;
     free(t->Grid.PC);
