@@ -127,7 +127,8 @@ int kqed_kernel_batch_dev(const struct QED_kernel_temps *t, int variant, size_t 
      sums[k] = sum_n sum_c L<variant>_c(x_k, y_n) * pi[k][n][c]
    with pi laid out [nx][ny][384].  Accumulation is FP64 with compensated
    (Neumaier) summation and a fixed reduction order, so results are
-   reproducible.  Host buffers. */
+   reproducible.  An empty lattice (ny = 0) gives zero sums; its site and pi
+   pointers may then be NULL.  Host buffers. */
 int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, size_t nx, const double *x,
                      size_t ny, const double *y, const double *pi, double *sums, int precision);
 

@@ -985,8 +985,13 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
   if (!c) return fail("tables not initialised");
   if (check_variant_precision(variant, precision)) return 1;
   if (nx == 0) return 0;
-  if (!d_x || !d_y || !d_pi || !d_sums) return fail("null buffer");
+  if (!d_sums) return fail("null buffer");
   cudaStream_t s = (cudaStream_t)stream;
+  if (ny == 0) {   /* an empty lattice sums to zero (its site and Pi pointers may be NULL) */
+    CUDA_OK(cudaMemsetAsync(d_sums, 0, nx * sizeof(double), s));
+    return 0;
+  }
+  if (!d_x || !d_y || !d_pi) return fail("null buffer");
   ThreadStage &st = stage_for(c);
   LatticeRun R;
   if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R, precision)) return 1;
@@ -1005,8 +1010,13 @@ extern "C" int kqed_lattice_sum_synth(const struct QED_kernel_temps *t, int vari
   if (!c) return fail("tables not initialised");
   if (check_variant_precision(variant, precision)) return 1;
   if (nx == 0) return 0;
-  if (!d_x || !d_y || !d_sums) return fail("null buffer");
+  if (!d_sums) return fail("null buffer");
   cudaStream_t s = (cudaStream_t)stream;
+  if (ny == 0) {   /* an empty lattice sums to zero (its site pointer may be NULL) */
+    CUDA_OK(cudaMemsetAsync(d_sums, 0, nx * sizeof(double), s));
+    return 0;
+  }
+  if (!d_x || !d_y) return fail("null buffer");
   ThreadStage &st = stage_for(c);
   LatticeRun R;
   if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R, precision)) return 1;
@@ -1041,7 +1051,12 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
   if (!c) return fail("tables not initialised");
   if (check_variant_precision(variant, precision)) return 1;
   if (nx == 0) return 0;
-  if (!x || !y || !pi || !sums) return fail("null buffer");
+  if (!sums) return fail("null buffer");
+  if (ny == 0) {   /* an empty lattice sums to zero (its site and Pi pointers may be NULL) */
+    for (size_t k = 0; k < nx; k++) sums[k] = 0.0;
+    return 0;
+  }
+  if (!x || !y || !pi) return fail("null buffer");
   ThreadStage &st = stage_for(c);
   if (!st.stream) CUDA_OK(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking));
   if (!st.copy_stream) CUDA_OK(cudaStreamCreateWithFlags(&st.copy_stream, cudaStreamNonBlocking));

@@ -101,7 +101,14 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
   if (kqed::ctx_handles(t, &T, &M, &cfg)) return kqed::set_error("tables not initialised");
   if (variant < 0 || variant > 3) return kqed::set_error("variant not in 0..3");
   if (nx == 0) return 0;
-  if (!d_x || !d_y || !d_pi || !d_sums) return kqed::set_error("null buffer");
+  if (!d_sums) return kqed::set_error("null buffer");
+  if (ny == 0) {   /* an empty lattice sums to zero (its site and Pi pointers may be NULL) */
+    if (cudaMemsetAsync(d_sums, 0, nx * sizeof(double), static_cast<cudaStream_t>(stream)) !=
+        cudaSuccess)
+      return kqed::set_error("kqed_lattice_sum_noalloc: memset failed");
+    return 0;
+  }
+  if (!d_x || !d_y || !d_pi) return kqed::set_error("null buffer");
   const size_t tiles = (ny + kqed::kTile - 1) / kqed::kTile;
   const size_t n_partial = nx * (tiles ? tiles : 1) * 2;
   const size_t n_terms = variant ? ny * 384 + ny * 4 + nx * 384 * 2 + nx * 4 : 0;

@@ -107,3 +107,26 @@ def test_synth_lattice_workload_runs_small():
     assert np.isfinite(d["checksum_fp64"])
     assert d["fp32_mixed"]["err_vs_fp64"]["max"] <= 1e-6
     assert len(d["fp32_mixed"]["err_vs_fp64"]["per_x"]) == 4
+
+
+def test_empty_lattice_sums_to_zero(temps):
+    """an empty lattice (ny = 0; NULL site and Pi pointers) gives zero sums
+    through every lattice entry point, in both forms"""
+    import torch
+    xs, _ = _inputs()
+    nx = len(xs)
+    dx = torch.as_tensor(xs, device="cuda")
+    for prec in (K().KQED_FP64, K().KQED_FP32_MIXED):
+        for v in (0, 2):
+            out = torch.full((nx,), 7.0, dtype=torch.float64, device="cuda")
+            K().lattice_sum_dev(temps, v, dx.data_ptr(), nx, 0, 0, 0, out.data_ptr(), prec)
+            assert torch.count_nonzero(out).item() == 0
+            out.fill_(7.0)
+            K().lattice_sum_synth(temps, v, dx.data_ptr(), nx, 0, 0, 5, out.data_ptr(), prec)
+            assert torch.count_nonzero(out).item() == 0
+            h = K().lattice_sum(temps, v, xs, np.zeros((0, 4)), np.zeros((nx, 0, 384)), prec)
+            assert np.array_equal(h, np.zeros(nx))
+    out = torch.full((nx,), 7.0, dtype=torch.float64, device="cuda")
+    K().lattice_sum_noalloc(temps, 2, dx.data_ptr(), nx, 0, 0, 0, out.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.count_nonzero(out).item() == 0
