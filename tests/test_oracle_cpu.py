@@ -197,3 +197,54 @@ def test_synthetic_pi_generator_statistics():
     p0 = oracle_pi_synth(x, y2, seed=7)[0, 0]
     assert np.array_equal(p, p0)
     np.testing.assert_allclose(p / oracle_pi_synth(x, y2 * 0, seed=7)[0, 0], np.exp(-0.5), rtol=1e-15)
+
+
+def _edge_pairs(xlo, xhi, ylo, yhi):
+    """pairs on the branch and grid edges: y = c x (cb = +-1 exactly), x = -y,
+    |x| or |y| on the first / last grid node, cb one ulp-scale away from +-1,
+    tiny arguments, x = y + tiny, and lattice-diagonal pairs"""
+    rng = np.random.default_rng(11)
+    u = rng.normal(size=(16, 4))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    X, Y = [], []
+    for i, c in enumerate((0.5, 2.0, -0.5, -2.0, -1.0)):
+        X.append(u[i]); Y.append(c * u[i])
+    for i, (rx, ry) in enumerate(((xlo, 1.0), (xhi, 1.0), (1.0, ylo), (1.0, yhi), (xlo, ylo))):
+        X.append(rx * u[5 + i]); Y.append(ry * u[10 + i])
+    w = np.array([1.0, 0.0, 0.0, 0.0]); p = np.array([0.0, 1.0, 0.0, 0.0])
+    for eps in (1e-6, 1e-9):
+        X.append(1.3 * w); Y.append(0.7 * (w + eps * p))
+        X.append(1.3 * w); Y.append(-0.7 * (w + eps * p))
+    for s in (1e-8, 1e-5):
+        X.append(s * u[0]); Y.append(u[1])
+        X.append(u[2]); Y.append(s * u[3])
+    for d in (1e-10, 1e-6):
+        X.append(u[4]); Y.append(u[4] + d * u[5])
+    diag = np.ones(4) * 0.1
+    for k, m in ((1, 2), (3, 1), (2, -2), (5, 7), (4, -1)):
+        X.append(k * diag); Y.append(m * diag)
+    return np.array(X), np.array(Y)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference library not built here")
+def test_oracle_matches_live_reference_on_edge_pairs():
+    import ctypes
+    os.environ["KQEDREF_PATH"] = PKG
+    L = ctypes.CDLL(REF_SO)
+    assert L.ref_init() == 0
+    dp = ctypes.POINTER(ctypes.c_double)
+    O = oracle()
+    nstpx, nstpy = ctypes.c_int(), ctypes.c_int()
+    lim = [ctypes.c_double() for _ in range(4)]
+    assert O.oracle_grid(ctypes.byref(nstpx), ctypes.byref(nstpy),
+                         *[ctypes.byref(v) for v in lim]) == 0
+    x, y = _edge_pairs(*(v.value for v in lim))
+    n = len(x)
+    for v in range(4):
+        ref = np.zeros((n, 384))
+        L.ref_kernel(v, n, x.ctypes.data_as(dp), y.ctypes.data_as(dp), ref.ctypes.data_as(dp), 0)
+        got = oracle_kernel(v, x, y)
+        nz = np.abs(ref).max(1) > 0
+        assert np.array_equal(nz, np.abs(got).max(1) > 0), v
+        err = norm_rel(got[nz], ref[nz])
+        assert err.max() <= 1e-13, (v, err.max(), int(np.argmax(err)))
