@@ -43,6 +43,7 @@ def main():
     import torch
 
     import kqed_gb300 as K
+    from kqed_gb300.clocks import ClockSampler
     from kqed_gb300.workloads import diagonal_x, lattice_sites
     t = K.KernelTemps()
     specs = make_jobs(a.jobs, a.seed)
@@ -66,6 +67,8 @@ def main():
         e1.record()
         torch.cuda.synchronize()
         plan_ms = e0.elapsed_time(e1)
+        clk = ClockSampler(torch.cuda.current_device())
+        clk.start()
         plan.launch()
         torch.cuda.synchronize()
         e0.record()
@@ -73,6 +76,7 @@ def main():
             plan.launch()
         e1.record()
         torch.cuda.synchronize()
+        clocks = clk.stop()
         graph_ms = e0.elapsed_time(e1) / a.steps
         got = np.concatenate([s.cpu().numpy() for s in sums])
         # the same jobs, one call each
@@ -89,7 +93,7 @@ def main():
         out[name] = {"graph_ms_per_step": graph_ms, "evals_per_s": pairs / (graph_ms / 1e3),
                      "sequential_calls_ms": seq_ms,
                      "sequential_evals_per_s": pairs / (seq_ms / 1e3),
-                     "plan_create_ms": plan_ms,
+                     "plan_create_ms": plan_ms, "clocks": clocks,
                      "max_rel_diff_vs_sequential": float(np.abs(got - r).max() /
                                                          max(np.abs(r).max(), 1e-300)),
                      "launch": {k: info[k] for k in ("warps_per_block", "blocks",

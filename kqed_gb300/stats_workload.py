@@ -49,11 +49,15 @@ def main():
     import kqed_gb300 as K
     n = int(a.pairs)
     t = K.KernelTemps()
+    from kqed_gb300.clocks import ClockSampler
     x, y = make_pairs(n, a.seed, "cuda")
     torch.cuda.synchronize()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
     t0 = time.perf_counter()
     st = K.precision_stats(t, a.variant, x.data_ptr(), y.data_ptr(), n, a.floor)
     wall = time.perf_counter() - t0
+    clocks = clk.stop()
     cm, cr = st["comp_max"], st["comp_rms"]
     out = {"workload": "L%d, %d pairs, x,y ~ U[-4,4]^4, 1%% with |x| or |y| in [1e-4,1e-2)"
                        % (a.variant, n),
@@ -62,7 +66,7 @@ def main():
            "component_max": {"max": float(cm.max()), "median": float(np.median(cm)),
                              "argmax": int(np.argmax(cm))},
            "component_rms": {"max": float(cr.max()), "median": float(np.median(cr))},
-           "seconds": wall, "pairs_per_s_both_forms": n / wall}
+           "seconds": wall, "pairs_per_s_both_forms": n / wall, "clocks": clocks}
     print(json.dumps(out))
     t.free()
 

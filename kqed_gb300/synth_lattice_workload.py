@@ -35,6 +35,7 @@ def main():
     import torch
 
     import kqed_gb300 as K
+    from kqed_gb300.clocks import ClockSampler
     from kqed_gb300.workloads import diagonal_x, lattice_sites
     t = K.KernelTemps()
     xs = diagonal_x(a.nx, a.spacing)
@@ -50,6 +51,8 @@ def main():
         def step():
             K.lattice_sum_synth(t, a.variant, dx.data_ptr(), nx, dy.data_ptr(), ny, a.seed,
                                 out.data_ptr(), prec, stream=stream.cuda_stream)
+        clk = ClockSampler(torch.cuda.current_device())
+        clk.start()
         for _ in range(a.warmup):
             step()
         torch.cuda.synchronize()
@@ -60,9 +63,10 @@ def main():
             step()
         e1.record(stream)
         torch.cuda.synchronize()
+        clocks = clk.stop()
         ms = e0.elapsed_time(e1) / a.steps
         sums[name] = out.cpu().numpy()
-        res[name] = {"ms_per_step": ms, "evals_per_s": nx * ny / (ms / 1e3)}
+        res[name] = {"ms_per_step": ms, "evals_per_s": nx * ny / (ms / 1e3), "clocks": clocks}
     s64, s32 = sums["fp64"], sums["fp32_mixed"]
     rms = float(np.sqrt(np.mean(s64 ** 2)))
     err = np.abs(s32 - s64) / rms
