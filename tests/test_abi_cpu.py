@@ -175,3 +175,29 @@ int main(void){
     J, I = K.LatticeJob, K.BatchInfo
     assert got == [ctypes.sizeof(J), J.d_pi.offset, J.pi_stream.offset, J.d_sums.offset,
                    ctypes.sizeof(I), I.tuned_ms.offset]
+
+
+def test_c_program_links_every_entry_point(lib, tmp_path):
+    """a C caller (the reference's language) compiles against include/kqed.h,
+    links libkqed_gb300.so and resolves every declared entry point; it then
+    calls only kqed_last_error and kqed_launch_count (no GPU work)"""
+    names = declared_functions()
+    c = tmp_path / "link.c"
+    c.write_text(
+        "#include <stdio.h>\n#include \"kqed.h\"\n"
+        "typedef void (*fp)(void);\n"
+        "int main(void) {\n"
+        "  fp f[] = {" + ", ".join("(fp)%s" % n for n in names) + "};\n"
+        "  int n = 0;\n"
+        "  for (unsigned i = 0; i < sizeof(f) / sizeof(f[0]); i++) n += f[i] != 0;\n"
+        "  printf(\"%d %llu [%s]\\n\", n, (unsigned long long)kqed_launch_count(),"
+        " kqed_last_error());\n"
+        "  return 0;\n}\n")
+    libdir = os.path.dirname(lib._name)
+    exe = str(tmp_path / "link")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.dirname(HDR), "-o",
+                        exe, str(c), "-L" + libdir, "-lkqed_gb300", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert int(out[0]) == len(names) and int(out[1]) == 0
