@@ -1,6 +1,6 @@
 """Batched-lattice workload: many fused lattice sums in one CUDA graph.
 
-  python -m kqed_gb300.batch_workload [--jobs 64] [--seed 3] [--steps 3]
+  python -m benchmarks.batch_workload [--jobs 64] [--seed 3] [--steps 3]
 
 Jobs: lattice size L and kernel variant drawn (numpy default_rng(seed)) from
 {12, 16, 24, 32} x {L0, L1, L2, L3}; every job is a periodic L^4 lattice
@@ -43,7 +43,7 @@ def main():
     import torch
 
     import kqed_gb300 as K
-    from kqed_gb300.clocks import ClockSampler
+    from benchmarks.clocks import ClockSampler
     from kqed_gb300.workloads import diagonal_x, lattice_sites
     t = K.KernelTemps()
     specs = make_jobs(a.jobs, a.seed)

@@ -1,11 +1,11 @@
 """Calibration of the FP64 work model in flops.py.
 
-  python -m kqed_gb300.calibrate --run            launches one fused lattice sum (L2)
+  python -m benchmarks.calibrate --run            launches one fused lattice sum (L2)
                                                   per branch-uniform case (a record kernel
                                                   and an assembly kernel each); run it
                                                   under ncu with the FP64 instruction
                                                   counters
-  python -m kqed_gb300.calibrate --fit CSV        fits PER_K / FIXED / AXIS from the ncu CSV
+  python -m benchmarks.calibrate --fit CSV        fits PER_K / FIXED / AXIS from the ncu CSV
                                                   and writes flops_table.json
 
 Cases: one x point against 4096 sites of a shifted 8^4 lattice (no site is 0
@@ -112,7 +112,7 @@ def fit(path, cases_path):
     table = {"PER_K": float(per_k), "FIXED": float(fixed), "AXIS": float(axis), "CONTRACT": 0.0,
              "CONTRACT_EXTRA": 0.0,
              "source": "ncu executed FP64 ops of lattice_rec_kernel + lattice_asm_kernel "
-                       "(FP64 form), L2, kqed_gb300/calibrate.py",
+                       "(FP64 form), L2, benchmarks/calibrate.py",
              "cases": cases}
     with open(os.path.join(HERE, "flops_table.json"), "w") as f:
         json.dump(table, f, indent=1)

@@ -4,7 +4,7 @@ The figures are the FP64 operations the kernel performs per (x, y) pair
 (add/sub/mul = 1, fma = 2; divisions and square roots count as the FMA
 sequences they compile to), measured once per kernel version with ncu's
 executed-instruction counters on branch-uniform cases
-(`python -m kqed_gb300.calibrate`, summary in profiles/) and frozen here.
+(`python -m benchmarks.calibrate`, summary in profiles/) and frozen here.
 A generic pair costs PER_K * Ktop + FIXED, Ktop = max(nfx[ix], nfx[ix+1]) + 2
 being the number of Chebyshev steps of its x cell; an x=0 / y=0 / x=y pair
 costs AXIS.  CONTRACT is the per-pair contraction with Pi (and the per-site

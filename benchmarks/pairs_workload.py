@@ -1,6 +1,6 @@
 """Non-fused pair batches: L<variant>(x_i, y_i), 384 FP64 components each.
 
-  python -m kqed_gb300.pairs_workload [--variant 0] [--repeat 64] [--steps 5]
+  python -m benchmarks.pairs_workload [--variant 0] [--repeat 64] [--steps 5]
 
 Pairs: the 4160 pairs of workloads.config1_pairs (4096 with components
 U[-2,2], 64 with one side of norm 1e-6..1e-3), tiled `--repeat` times so

@@ -1,7 +1,7 @@
 """Error statistics of the mixed-precision form against the FP64 form on a
 large random pair set, accumulated on the device (kqed_precision_stats).
 
-  python -m kqed_gb300.stats_workload [--pairs 1e8] [--variant 3] [--seed 4]
+  python -m benchmarks.stats_workload [--pairs 1e8] [--variant 3] [--seed 4]
 
 Pairs: x, y uniform in [-4, 4]^4; 1% of them get a small side: |x| (half of
 them) or |y| (the other half) scaled into [1e-4, 1e-2) (log-uniform).  Both
@@ -49,7 +49,7 @@ def main():
     import kqed_gb300 as K
     n = int(a.pairs)
     t = K.KernelTemps()
-    from kqed_gb300.clocks import ClockSampler
+    from benchmarks.clocks import ClockSampler
     x, y = make_pairs(n, a.seed, "cuda")
     torch.cuda.synchronize()
     clk = ClockSampler(torch.cuda.current_device())

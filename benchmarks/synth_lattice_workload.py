@@ -3,7 +3,7 @@ over a periodic L^4 lattice, Pi generated inside the kernels (seeded Philox,
 the synthetic Pi of kqed_lattice_sum_synth), so that lattices whose stored
 Pi would not fit in HBM (48^4 x 16 x: 261 GB) run at full size.
 
-  python -m kqed_gb300.synth_lattice_workload [--L 48] [--nx 16] [--variant 2]
+  python -m benchmarks.synth_lattice_workload [--L 48] [--nx 16] [--variant 2]
 
 Default: 48^4 lattice, spacing 0.1, 16 diagonal x, kernel L2 -- 84,934,656
 evaluations per step.  Both precision forms on the same inputs, timed with
@@ -35,7 +35,7 @@ def main():
     import torch
 
     import kqed_gb300 as K
-    from kqed_gb300.clocks import ClockSampler
+    from benchmarks.clocks import ClockSampler
     from kqed_gb300.workloads import diagonal_x, lattice_sites
     t = K.KernelTemps()
     xs = diagonal_x(a.nx, a.spacing)

@@ -11,6 +11,18 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
 REF_SO = os.path.join(ROOT, "oracle", "_ref", "libkqedref_scalar.so")
 
+
+def reference_root():
+    """The reference checkout: the environment variable KQED_REFERENCE, else
+    the one the build recorded in oracle/_ref/REFERENCE; None when neither
+    names an existing directory (the tests that read it then skip)."""
+    cand = os.environ.get("KQED_REFERENCE")
+    if not cand:
+        rec = os.path.join(ROOT, "oracle", "_ref", "REFERENCE")
+        if os.path.exists(rec):
+            cand = open(rec).read().strip()
+    return cand if cand and os.path.isdir(os.path.join(cand, "src")) else None
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _oracle = None
 

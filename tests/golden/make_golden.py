@@ -22,7 +22,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("KQED_REFERENCE", "/root/reference")
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+from _helpers import reference_root  # noqa: E402
+
+REF = reference_root()
+if REF is None:
+    sys.exit("make_golden.py: set KQED_REFERENCE to the reference checkout")
 
 
 def parse_reg(path):

@@ -8,10 +8,12 @@ import shutil
 import subprocess
 
 import pytest
+from _helpers import reference_root
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HDR = os.path.join(ROOT, "include", "kqed.h")
-REF_HDR = "/root/reference/src/HEADERS/KQED.h"
+REF_ROOT = reference_root()
+REF_HDR = os.path.join(REF_ROOT, "src", "HEADERS", "KQED.h") if REF_ROOT else ""
 
 
 @pytest.fixture(scope="module")
@@ -74,7 +76,8 @@ def test_struct_layout_matches_ctypes(tmp_path):
     assert [int(v) for v in got] == want
 
 
-@pytest.mark.skipif(not os.path.exists(REF_HDR), reason="reference headers not present")
+@pytest.mark.skipif(not REF_HDR or not os.path.exists(REF_HDR),
+                    reason="reference headers not present (KQED_REFERENCE unset)")
 def test_struct_layout_matches_reference(tmp_path):
     """sizeof/offsets of struct QED_kernel_temps equal the reference's
     (src/HEADERS/KQED.h:69-93), so it can be passed by value unchanged"""

@@ -1,8 +1,8 @@
-"""The clock record of the benchmarks (`kqed_gb300/clocks.py`): median SM
+"""The clock record of the benchmarks (`benchmarks/clocks.py`): median SM
 clock, maximum clock and the throttle reasons seen active in any sample,
 from nvidia-smi's CSV lines; unparsable lines are skipped; without
 nvidia-smi the record says so."""
-from kqed_gb300.clocks import ClockSampler, summarize
+from benchmarks.clocks import ClockSampler, summarize
 
 
 def test_summary_of_samples():

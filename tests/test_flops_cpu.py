@@ -1,4 +1,4 @@
-"""The FP64 work model behind bench.py's roofline (`kqed_gb300/flops.py`):
+"""The FP64 work model behind bench.py's roofline (`benchmarks/flops.py`):
 its per-branch accounting of a lattice launch agrees with the oracle's own
 classification of every (x, y) pair -- x = 0 / y = 0 / x = y pairs at the
 axis cost, generic pairs (on or below the x grid, swapped or not) at
@@ -13,7 +13,7 @@ from _helpers import oracle, oracle_branch
 
 
 def test_lattice_work_model_matches_oracle_branches():
-    from kqed_gb300 import flops as F
+    from benchmarks import flops as F
     from kqed_gb300.workloads import diagonal_x, lattice_sites
     O = oracle()
     nstpx, nstpy = ctypes.c_int(), ctypes.c_int()

@@ -98,7 +98,7 @@ def test_synth_lattice_workload_runs_small():
     import subprocess
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    r = subprocess.run([sys.executable, "-m", "kqed_gb300.synth_lattice_workload", "--L", "8",
+    r = subprocess.run([sys.executable, "-m", "benchmarks.synth_lattice_workload", "--L", "8",
                         "--nx", "4", "--steps", "1", "--warmup", "1"], cwd=root,
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
