@@ -140,15 +140,19 @@ int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t n
 /* The fused lattice sum for callers that cannot allocate GPU memory (codes
    whose own pool owns the device; loops where cudaMalloc's implicit device
    synchronisation would stall other streams).  It has no counterpart in the
-   reference.  Same arguments and results as kqed_lattice_sum_dev, but its
+   reference.  Same arguments as kqed_lattice_sum_dev (FP64 form only), and
+   the same reduction order; results agree with it to about 1e-12 relative,
+   not bit for bit, because without room for per-x column tables the record
+   kernel interpolates from the node table, as the pair batches do.  Its
    scratch comes from a static 16 MiB device array compiled into the library
    (held by every GPU that loads it), so problems needing more scratch are
    rejected with an error: nx * ceil(ny / 64) * 2 doubles, plus, for L1..L3,
    388 * ny + 772 * nx doubles, plus one tile of pair records (64 * 88 + 8
-   doubles), must not exceed 2,097,152.  The first call on
-   a device looks up the array's device address; make it before any stream
-   capture.  Calls share the array: calls that overlap on the GPU race and
-   must be serialised by the caller.  Allocates nothing. */
+   doubles), must not exceed 2,097,152.  The first call in a CUDA context
+   (once per device, and again after cudaDeviceReset) looks up the array's
+   device address; make it before any stream capture.  Calls share the
+   array: calls that overlap on the GPU race and must be serialised by the
+   caller.  Allocates nothing. */
 int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int variant, size_t nx,
                              const double *d_x, size_t ny, const double *d_y, const double *d_pi,
                              double *d_sums, void *stream);

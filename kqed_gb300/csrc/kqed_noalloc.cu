@@ -15,10 +15,12 @@
  *     kNoallocDoubles doubles (16 MiB); every GPU that loads the library
  *     holds it until the process exits;
  *   - host code never uses the array's name as a device address (on the host
- *     it is only a stand-in symbol): the device address is obtained once per
- *     device with cudaGetSymbolAddress, with that device current, on the
- *     first call made on that device.  Make that first call before any
- *     stream capture;
+ *     it is only a stand-in symbol): the device address is obtained with
+ *     cudaGetSymbolAddress, with the device current, on the first call made
+ *     in each CUDA context -- once per device, and again after a
+ *     cudaDeviceReset has replaced the device's primary context (the cached
+ *     address is keyed by the context's unique id).  Make that first call
+ *     before any stream capture;
  *   - problems whose scratch does not fit are rejected with an error that
  *     states the need and the limit; nothing is allocated, here or in any
  *     library routine this function calls.  The per-pair records passed
@@ -32,8 +34,12 @@
  *     streams, or from different host threads -- race on the array and must
  *     be serialised by the caller.
  *
- * Results are those of kqed_lattice_sum_dev: the same kernels, the same
- * reduction order.
+ * Results agree with kqed_lattice_sum_dev's to about 1e-12 relative, not bit
+ * for bit: the reduction order is the same, but without room for the per-x
+ * column tables the record kernel interpolates from the node table (the
+ * path of the pair batches), and the contraction splits the FP64 per-site
+ * and per-x terms into (hi, lo) floats in the kernel instead of reading a
+ * prebuilt split.
  */
 #include <cuda_runtime.h>
 
@@ -50,18 +56,58 @@ constexpr size_t kNoallocDoubles = (size_t)2 << 20; /* 2,097,152 doubles = 16 Mi
 static __device__ __align__(256) double g_noalloc_scratch[kNoallocDoubles];
 
 constexpr int kMaxDevices = 64;
-double *g_scratch_addr[kMaxDevices] = {};
+struct ScratchSlot {
+  unsigned long long ctx_id; /* 0: not looked up yet */
+  double *addr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
-/* device address of the static scratch on the current device (set up once
-   per device with cudaGetSymbolAddress) */
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
+/* unique id of the calling thread's current CUDA context (0 if none); the
+   driver functions are reached through the runtime, so the library does not
+   link the driver library itself */
+unsigned long long current_ctx_id()
+{
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  if (!get_current || !get_id) return 0;
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+/* device address of the static scratch in the current context (looked up
+   with cudaGetSymbolAddress on the first call in each context) */
 int scratch_on_current_device(double **out)
 {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return kqed::set_error("kqed_lattice_sum_noalloc: no usable current CUDA device");
+  unsigned long long id = current_ctx_id();
+  if (id == 0) {   /* no context yet on this thread: make the device's primary one current */
+    if (cudaSetDevice(dev) != cudaSuccess)
+      return kqed::set_error("kqed_lattice_sum_noalloc: cannot make the device current");
+    id = current_ctx_id();
+  }
   std::lock_guard<std::mutex> g(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
+  ScratchSlot &sl = g_scratch[dev];
+  if (!sl.addr || id == 0 || sl.ctx_id != id) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -70,9 +116,10 @@ int scratch_on_current_device(double **out)
                cudaGetErrorString(e));
       return kqed::set_error(msg);
     }
-    g_scratch_addr[dev] = static_cast<double *>(p);
+    sl.addr = static_cast<double *>(p);
+    sl.ctx_id = id;
   }
-  *out = g_scratch_addr[dev];
+  *out = sl.addr;
   return 0;
 }
 
@@ -109,6 +156,15 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
     return 0;
   }
   if (!d_x || !d_y || !d_pi) return kqed::set_error("null buffer");
+  if (nx > kNoallocDoubles || ny > kNoallocDoubles) {
+    /* bounded first, so that the scratch arithmetic below cannot wrap */
+    char msg[256];
+    snprintf(msg, sizeof(msg),
+             "kqed_lattice_sum_noalloc: %zu x points x %zu sites exceed the static limit of "
+             "%zu doubles of scratch (16 MiB). Use kqed_lattice_sum_dev.", nx, ny,
+             kNoallocDoubles);
+    return kqed::set_error(msg);
+  }
   const size_t tiles = (ny + kqed::kTile - 1) / kqed::kTile;
   const size_t n_partial = nx * (tiles ? tiles : 1) * 2;
   const size_t n_terms = variant ? ny * 384 + ny * 4 + nx * 384 * 2 + nx * 4 : 0;

@@ -35,7 +35,7 @@ def _inputs(torch, L, a, nx, seed):
             torch.as_tensor(pi, device=dev))
 
 
-@pytest.mark.parametrize("variant", [0, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_noalloc_matches_device_entry_point_twice(setup, variant):
     K, t, torch = setup
     xs, ys, dx, dy, dpi = _inputs(torch, 6, 0.25, 4, seed=21 + variant)
@@ -71,6 +71,28 @@ def test_noalloc_second_call_with_other_inputs(setup):
         assert np.all(np.abs(g - r) <= TOL * np.maximum(np.abs(r), 1e-300) + 1e-300)
 
 
+def test_noalloc_allocates_nothing(setup):
+    """after a warm-up call (which loads the kernels' code), a call on a new
+    problem size leaves the device's free memory unchanged"""
+    K, t, torch = setup
+    stream = torch.cuda.current_stream().cuda_stream
+    xs, ys, dx, dy, dpi = _inputs(torch, 6, 0.25, 4, seed=41)
+    got = torch.zeros(len(xs), dtype=torch.float64, device="cuda")
+    K.lattice_sum_noalloc(t, 3, dx.data_ptr(), len(xs), dy.data_ptr(), len(ys), dpi.data_ptr(),
+                          got.data_ptr(), stream=stream)
+    torch.cuda.synchronize()
+    xs2, ys2, dx2, dy2, dpi2 = _inputs(torch, 5, 0.3, 3, seed=42)
+    got2 = torch.zeros(len(xs2), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    K.lattice_sum_noalloc(t, 3, dx2.data_ptr(), len(xs2), dy2.data_ptr(), len(ys2),
+                          dpi2.data_ptr(), got2.data_ptr(), stream=stream)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert np.all(np.isfinite(got2.cpu().numpy()))
+
+
 def test_noalloc_rejects_oversized_problem(setup):
     K, t, torch = setup
     ny = 20000   # L2 needs 388 * ny doubles of per-site terms: beyond 16 MiB
@@ -81,3 +103,7 @@ def test_noalloc_rejects_oversized_problem(setup):
     with pytest.raises(K.KQEDError, match="static limit"):
         K.lattice_sum_noalloc(t, 2, dx.data_ptr(), 2, dy.data_ptr(), ny, dpi.data_ptr(),
                               sums.data_ptr())
+    # sizes whose scratch arithmetic would wrap are rejected before it is done
+    with pytest.raises(K.KQEDError, match="static limit"):
+        K.lattice_sum_noalloc(t, 2, dx.data_ptr(), 2, dy.data_ptr(), (1 << 62) + 1,
+                              dpi.data_ptr(), sums.data_ptr())
