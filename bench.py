@@ -23,6 +23,7 @@ restatement under oracle/).
 import argparse
 import ctypes
 import json
+import math
 import os
 import sys
 import time
@@ -32,7 +33,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from kqed_gb300.clocks import ClockSampler  # noqa: E402
+from benchmarks.clocks import ClockSampler  # noqa: E402
 
 METRIC = ("(x,y) kernel evals/s on 1 GB300: plain FP64 vs FP32/surrogate at "
           "≤1e-6 rel err")
@@ -100,25 +101,45 @@ def cpu_impl():
 
 def cpu_sample(args, xs, ys, pi_host_fn, steps=1):
     """Time the CPU implementation on a bounded sample of the workload: a few
-    x points against all sites.  Returns (evals/s, cores, kind, sample)."""
+    x points against all sites.  Returns (evals/s, cores, kind, sample,
+    checked), checked = {k: (sum_y L.Pi, sum_y |L.Pi|)} of the sampled x
+    points, the CPU's lattice sums for the parity check of the GPU's."""
     contract, kind = cpu_impl()
     cores = os.cpu_count() or 1
     ks = [len(xs) // 4, len(xs) // 2, (3 * len(xs)) // 4] if len(xs) >= 4 else [0]
     best = None
+    checked = {}
     for _ in range(steps):
         t_tot, n_tot = 0.0, 0
         for k in ks:
             pik = pi_host_fn(k)
             X = np.ascontiguousarray(np.repeat(xs[k:k + 1], len(ys), 0))
             t0 = time.perf_counter()
-            contract(args.variant, X, ys, pik, cores)
+            d = contract(args.variant, X, ys, pik, cores)
             t_tot += time.perf_counter() - t0
             n_tot += len(ys)
+            checked[k] = (math.fsum(d), math.fsum(np.abs(d)))
         rate = n_tot / t_tot
         best = rate if best is None else max(best, rate)
     sample = "%d x points (k=%s) x %d sites, L%d contraction, %d threads" % (
         len(ks), ",".join(str(k) for k in ks), len(ys), args.variant, cores)
-    return best, cores, kind, sample
+    return best, cores, kind, sample, checked
+
+
+PARITY_TOL = 1e-12
+
+
+def parity_of(gpu_sums, checked):
+    """The GPU's FP64 lattice sums against the CPU implementation's on the
+    sampled x points: |S_gpu - S_cpu| / sum_y |L.Pi| (the sum's condition
+    scale; the tests use the same bound)."""
+    if not checked:
+        return None
+    rel = {k: abs(float(gpu_sums[k]) - s) / max(a, 1e-300) for k, (s, a) in checked.items()}
+    worst = max(rel.values())
+    return {"max_rel": worst, "tol": PARITY_TOL, "ok": bool(worst <= PARITY_TOL),
+            "x_checked": sorted(int(k) for k in checked),
+            "definition": "|S_gpu - S_cpu| / sum_y |L.Pi| per checked x, FP64 form"}
 
 
 def run_reference(args):
@@ -149,7 +170,7 @@ def run_reference(args):
     rates = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r, cores, kind, sample = cpu_sample(args, xs, ys, pi_cached, steps=1)
+        r, cores, kind, sample, _ = cpu_sample(args, xs, ys, pi_cached, steps=1)
         rates.append(r)
     wall = time.perf_counter() - t0
     value = float(np.median(rates))
@@ -179,7 +200,7 @@ def run_gb300(args):
     import torch
 
     import kqed_gb300 as K
-    from kqed_gb300 import flops as F
+    from benchmarks import flops as F
     from kqed_gb300.workloads import diagonal_x, lattice_sites, pi_synth_torch
 
     rank, world, local = dist_env()
@@ -347,11 +368,14 @@ def run_gb300(args):
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         def pi_k(k):
             return pi_host[k].numpy()
-        r, cores, kind, sample = cpu_sample(args, xs, ys, pi_k, steps=1)
+        r, cores, kind, sample, checked = cpu_sample(args, xs, ys, pi_k, steps=1)
         cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+        parity = parity_of(fsums["fp64"], checked)
+        parity["against"] = kind
 
     if rank == 0:
         line = {
@@ -383,6 +407,7 @@ def run_gb300(args):
                          "peak_source": "FP64 FMA-chain probe run by this bench (not in "
                                         "MEASURED_PEAKS.json)"},
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clk,
             "checksum": [float(v) for v in fsums["fp64"][:4]],
         }

@@ -91,7 +91,8 @@ enum { alpha0dx_0p = 0, alpha0_1p, alpha3_0p, beta2_1p, alpha3_1p, alpha1_0p, be
 
 /* ------------------------------------------------------------ records */
 
-enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4 };
+/* K_GEN64: a generic pair assembled in FP64 proper (near-parallel x, y) */
+enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4, K_GEN64 = 5 };
 
 /* generic record (doubles) */
 enum {
@@ -117,6 +118,21 @@ enum {
 /* ------------------------------------------------------------ helpers */
 
 __device__ __forceinline__ double lerp(double a, double t1, double t2) { return a * t1 + (1.0 - a) * t2; }
+
+/* a[0]b[0] + a[1]b[1] + a[2]b[2] + a[3]b[3] rounded after every operation,
+   left to right, with no multiply-add contraction: the reference's portable
+   SCALPROD (src/HEADERS/getff-new.h:49-53) and is_zero (kernels.c:14-17) as
+   its scalar build and the oracle evaluate them.  Every branch and grid
+   decision (zero / axis tests, |x| beyond the last node, the grid search,
+   the x <-> (x-y) swap test) is taken on these values, so a pair within an
+   ulp of a decision boundary goes the same way as in the reference. */
+__device__ __forceinline__ double dot4_rn(const double *a, const double *b)
+{
+  double s = __dmul_rn(a[0], b[0]);
+  s = __dadd_rn(s, __dmul_rn(a[1], b[1]));
+  s = __dadd_rn(s, __dmul_rn(a[2], b[2]));
+  return __dadd_rn(s, __dmul_rn(a[3], b[3]));
+}
 
 /* bsrch, src/LIBFILES/getff-new.c:199-210 */
 __device__ __forceinline__ int bsrch(const double *__restrict__ arr, double t, int lo, int hi)
@@ -446,7 +462,7 @@ __global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs,
     const int iy = rem / T.NK, K = rem % T.NK;
     S *out = col + u * kRow;
     const double *xv = xs + 4 * k;
-    double xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
+    double xsq = dot4_rn(xv, xv);   /* the same |x| as the pairs' invariants */
     xsq = xsq < 1E-7 ? 1E-7 : xsq;
     const double X = sqrt(fabs(xsq));
     const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
@@ -547,23 +563,23 @@ __device__ __forceinline__ void invariants(const DevTables &T, const double *xv,
                                            Inv &I)
 {
   const double EPSIN = 1E-7;
-  I.xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
+  I.xsq = dot4_rn(xv, xv);
   I.xsq = I.xsq < EPSIN ? EPSIN : I.xsq;
   I.x = sqrt(fabs(I.xsq));
-  I.ysq = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
+  I.ysq = dot4_rn(yv, yv);
   I.ysq = I.ysq < EPSIN ? EPSIN : I.ysq;
   I.y = sqrt(fabs(I.ysq));
-  I.xdoty = xv[0] * yv[0] + xv[1] * yv[1] + xv[2] * yv[2] + xv[3] * yv[3];
-  I.cb = I.xdoty / (I.x * I.y);
+  I.xdoty = dot4_rn(xv, yv);
+  I.cb = I.xdoty / __dmul_rn(I.x, I.y);
   I.cborig = I.cb;
   I.yorig = I.y;
-  I.xmysq = (I.xsq + I.ysq) * (1.00000000000001) - 2.0 * I.xdoty;
+  I.xmysq = __dsub_rn(__dmul_rn(__dadd_rn(I.xsq, I.ysq), 1.00000000000001), __dmul_rn(2.0, I.xdoty));
   I.xmy = sqrt(fabs(I.xmysq));
   I.flag2 = 0;
   const double rx = (I.x > I.xmy ? I.xmy / I.x : I.x / I.xmy);
   const double rxy = (I.x > I.y ? I.y / I.x : I.x / I.y);
   if (rx < rxy && I.xmy < __ldg(T.YY + T.nstpy - 1) && fabs(I.xmysq) > 1E-28) {
-    I.cb = (I.x - I.y * I.cb) / I.xmy;
+    I.cb = __dsub_rn(I.x, __dmul_rn(I.y, I.cb)) / I.xmy;
     I.y = I.xmy;
     I.flag2 = 1;
   }
@@ -992,7 +1008,7 @@ __device__ void fill_generic_record(const Sink &R, const double *xvd, const doub
    the TAYLORX grid (zero kernel) */
 __device__ int fill_x0_record(const DevTables &T, const Sink &R, const double *yv)
 {
-  const double ysq = yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2] + yv[3] * yv[3];
+  const double ysq = dot4_rn(yv, yv);
   const double y = sqrt(fabs(ysq));
   const int it = bsrch(T.TX, y, 0, T.ny_tay);
   if (it == T.ny_tay - 1) return 1;
@@ -1039,7 +1055,7 @@ __device__ int fill_x0_record(const DevTables &T, const Sink &R, const double *y
    beyond the grid (zero kernel) */
 __device__ int fill_y0_record(const DevTables &T, const Sink &R, const double *xv)
 {
-  const double xsq = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] + xv[3] * xv[3];
+  const double xsq = dot4_rn(xv, xv);
   const double x = sqrt(fabs(xsq));
   int ix = bsrch(T.XX, x, 0, T.nstpx);
   if (x > __ldg(T.XX + T.nstpx - 1)) return 1;
@@ -1089,7 +1105,7 @@ __device__ int fill_y0_record(const DevTables &T, const Sink &R, const double *x
 
 __device__ __forceinline__ bool is_zero4(const double *v)
 {
-  return (v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3]) < 1E-28;
+  return dot4_rn(v, v) < 1E-28;
 }
 
 __device__ __forceinline__ double to_double(double v) { return v; }
@@ -1286,7 +1302,9 @@ __device__ int phase_a(const DevTables &T, const double *xv, const double *yv, c
     V_swap(&D, k);
   }
   fill_generic_record(R, xv, yv, I, dg0dx, dg0dy, dg0dcb, Ts, D);
-  return K_GEN;
+  /* near-parallel pairs of the FP64 assembly: FP64 proper (see asm_pair) */
+  return ((sizeof(S) == 8 || f64pair) && fmax(fabs(I.cb), fabs(I.cborig)) > 0.99) ? K_GEN64
+                                                                                   : K_GEN;
 }
 
 /* The mixed form's lean phase A: only the pairs that are evaluated in float
@@ -1892,24 +1910,51 @@ __device__ __forceinline__ float d2f_round(double v)
 /* one pair by the warp, in the assembly precision S (the mixed form's
    flagged pairs in FP64): record from global memory to shared memory, then
    assemble.  Returns false for a zero kernel; t64 says whether the
-   components are doubles. */
+   components are double-float (else float).
+
+   Two kinds of pair leave the assembly with their components rounded
+   through FP64:
+   - near-parallel generic pairs (K_GEN64: max(|cb|, |cb'|) > 0.99, in the
+     FP64 form and among the mixed form's FP64-assembled pairs) are
+     assembled in FP64 proper and then split to double-float.  Their STV
+     components cancel strongly (the reference's own AVX2/FMA and portable
+     builds differ by up to 6e-13 there); in double-float, with 5 bits less
+     than FP64, the cancellation left errors up to 1.3e-11;
+   - the x = 0 / y = 0 / x = y forms are the kernels that the per-site and
+     per-x terms of L1..L3 repeat, and those terms are FP64 values of the
+     same double-float results (L2(0, y) = L0(0, y) - L0(0, y) - L0(0, 0) is
+     zero in the reference, src/LIBFILES/kernels.c:136-177): their components
+     are rounded to FP64 and split again, exactly as the terms were, so the
+     cancellation in the contraction is exact as in the reference. */
 template <typename S>
 __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, const double *grec,
                                          int code, int lane, bool &perm, bool &t64)
 {
-  const int kind = code & 7;
+  const int kind0 = code & 7;
+  const bool g64 = kind0 == K_GEN64;
+  const int kind = g64 ? K_GEN : kind0;
   perm = (kind == K_Y0PERM);
-  t64 = sizeof(S) == 8 || (code & 8);
+  t64 = sizeof(S) == 8 || (code & 8) || g64;
   if (kind == K_NONE) return false;
-  if (t64) {
+  df *tb = reinterpret_cast<df *>(L.tbuf);
+  if (g64) {
+    for (int i = lane; i < REC; i += 32) L.rec[i] = __ldg(grec + i);
+    __syncwarp();
+    assemble<double>(L, M, K_GEN, L.rec, L.stv, L.tbuf, L.coefd, lane);
+    for (int i = lane; i < 384; i += 32) tb[i] = split_d<true>(L.tbuf[i]);
+    __syncwarp();
+  } else if (t64) {
     /* FP64 records assembled in double-float on the FP32 pipe; the same
        (hardware) split in both forms, so that the mixed form's FP64 pairs
        come out bit-identical to the FP64 form's */
     df *rd = reinterpret_cast<df *>(L.rec);
     for (int i = lane; i < REC; i += 32) rd[i] = split_d(__ldg(grec + i));
     __syncwarp();
-    assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), reinterpret_cast<df *>(L.tbuf),
-                lane);
+    assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), tb, lane);
+    if (kind != K_GEN) {
+      for (int i = lane; i < 384; i += 32) tb[i] = split_d<true>(df_to_d<true>(tb[i]));
+      __syncwarp();
+    }
   } else {
     float *rf = reinterpret_cast<float *>(L.rec);
     for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));

@@ -95,3 +95,28 @@ def test_tuned_batch_plan(temps):
         g = k[2].cpu().numpy()
         assert np.abs(g - b).max() <= REL * np.abs(b).max()
     tuned.close()
+
+
+@pytest.mark.parametrize("precision", [0])
+def test_batch_jobs_match_oracle(temps, precision):
+    """jobs of the batch (stored and generated Pi, L0..L3) against the
+    oracle's contraction: |S - S_oracle| <= 1e-12 * sum_y |L.Pi|"""
+    import torch
+
+    from _helpers import oracle_contract, oracle_pi_synth
+    jobs, keep = _jobs(torch)
+    plan = K().BatchPlan(temps, jobs, precision=precision)
+    plan.launch()
+    torch.cuda.synchronize()
+    for j, (dx, dy, sums, pi) in list(zip(jobs, keep))[:4]:
+        xs, ys = dx.cpu().numpy(), dy.cpu().numpy()
+        if pi is None:
+            P = oracle_pi_synth(xs, ys, j["pi_seed"], j["pi_stream"])
+        else:
+            P = pi.cpu().numpy()
+        g = sums.cpu().numpy()
+        for k in range(len(xs)):
+            X = np.repeat(xs[k:k + 1], len(ys), 0)
+            terms = oracle_contract(j["variant"], X, ys, P[k])
+            assert abs(g[k] - np.sum(terms)) <= 1e-12 * np.sum(np.abs(terms)), (j["variant"], k)
+    plan.close()
