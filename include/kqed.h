@@ -250,6 +250,16 @@ int kqed_precision_stats(const struct QED_kernel_temps *t, int variant, size_t n
    stops and clears.  kqed_fp64_peak_gflops runs an FP64 FMA-chain probe on
    the current device and returns GFLOP/s.  No reference counterpart. */
 void kqed_profile(int enable);
+
+/* The BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory)
+   that trains and evaluates the learned surrogate, exposed for testing; no
+   reference counterpart.  d_c[z][m][n] = sum_{k in split z} A(m, k) B(n, k),
+   A(m, k) = d_a[m * sam + k * sak], B(n, k) = d_b[n * sbn + k * sbk] (bf16,
+   device), d_c fp32 with row stride ldc; split z of `splits` covers a
+   contiguous range of k.  Synchronises `stream`. */
+int kqed_bf16_gemm(const void *d_a, long long sam, long long sak, const void *d_b, long long sbn,
+                   long long sbk, int M, int N, int K, int splits, float *d_c, long long ldc,
+                   void *stream);
 int kqed_profile_read(double *total_ms, uint64_t *launches);
 int kqed_profile_read_copies(double *total_ms, uint64_t *copies);
 int kqed_fp64_peak_gflops(double *gflops);

@@ -140,6 +140,11 @@ def lib():
         L.kqed_batch_plan_info.restype = ctypes.c_int
         L.kqed_batch_plan_destroy.argtypes = [ctypes.c_void_p]
         L.kqed_batch_plan_destroy.restype = None
+        L.kqed_bf16_gemm.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
+                                     ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]
+        L.kqed_bf16_gemm.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
         L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
@@ -368,3 +373,10 @@ def fp64_peak_gflops():
     g = ctypes.c_double()
     _check(lib().kqed_fp64_peak_gflops(ctypes.byref(g)))
     return g.value
+
+
+def bf16_gemm(a_ptr, sam, sak, b_ptr, sbn, sbk, M, N, K, c_ptr, ldc, splits=1, stream=None):
+    """kqed_bf16_gemm: c[z][m][n] = sum_k A(m,k) B(n,k) on the tensor cores
+    (bf16 operands by strides, fp32 result); device pointers."""
+    _check(lib().kqed_bf16_gemm(a_ptr, sam, sak, b_ptr, sbn, sbk, M, N, K, splits, c_ptr, ldc,
+                                stream))

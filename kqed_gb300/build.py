@@ -77,17 +77,22 @@ def build_lib(verbose=False):
     so = os.path.join(OUT, "libkqed_gb300.so")
     cu = os.path.join(CSRC, "kqed_fp64.cu")
     cu2 = os.path.join(CSRC, "kqed_noalloc.cu")
+    cu3 = os.path.join(CSRC, "kqed_mlp_gemm.cu")
+    cu4 = os.path.join(CSRC, "kqed_mlp.cu")
     host = os.path.join(CSRC, "kqed_host.cpp")
     crc = os.path.join(CSRC, "kqed_crc32c.c")
     hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
     hdrs.append(os.path.join(ROOT, "include", "kqed.h"))
-    if _newer(so, [cu, cu2, host, crc] + hdrs):
+    srcs = [f for f in (cu, cu2, cu3, cu4, host, crc) if os.path.exists(f)]
+    if _newer(so, srcs + hdrs):
         return so
     lib_default = '-DKQED_DEFAULT_LIB_PATH="%s"' % HERE
     o_cu = os.path.join(OUT, "kqed_fp64.o")
     o_cu2 = os.path.join(OUT, "kqed_noalloc.o")
     o_host = os.path.join(OUT, "kqed_host.o")
     o_crc = os.path.join(OUT, "kqed_crc32c.o")
+    o_cu3 = os.path.join(OUT, "kqed_mlp_gemm.o")
+    o_cu4 = os.path.join(OUT, "kqed_mlp.o")
     jobs = [
         [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v" if verbose else "-O3", "-c", cu, "-o", o_cu],
@@ -96,12 +101,19 @@ def build_lib(verbose=False):
         ["gcc", "-O2", "-fPIC", "-std=gnu11", "-c", crc, "-o", o_crc],
         [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu2,
                          "-o", o_cu2],
+        [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu3,
+                         "-o", o_cu3],
     ]
-    with cf.ThreadPoolExecutor(4) as ex:
+    objs = [o_cu, o_cu2, o_cu3]
+    if os.path.exists(cu4):
+        jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                                     "-c", cu4, "-o", o_cu4])
+        objs.append(o_cu4)
+    with cf.ThreadPoolExecutor(len(jobs)) as ex:
         results = list(ex.map(_run, jobs))
     if verbose:
         sys.stderr.write(results[0].stderr)
-    _run([NVCC] + ARCH + ["-shared", "-o", so, o_cu, o_cu2, o_host, o_crc, "-lcudart"])
+    _run([NVCC] + ARCH + ["-shared", "-o", so] + objs + [o_host, o_crc, "-lcudart"])
     return so
 
 
