@@ -242,6 +242,60 @@ int kqed_precision_stats(const struct QED_kernel_temps *t, int variant, size_t n
                          const double *d_x, const double *d_y, double floor_abs, double *stats,
                          void *stream);
 
+/* The learned surrogate (precision KQED_SURROGATE; no reference
+   counterpart).  A 3 -> 256 -> 256 -> 256 -> 39 MLP (SiLU) maps a generic
+   pair's post-swap invariants (|x|, |y|, cb) to the 39 weight functions that
+   the reference interpolates from its form-factor grid (extractff2 / getff7,
+   src/LIBFILES/getff-new.c:262-312, src/LIBFILES/simd.c:488-612).  It is
+   trained on the GPU by this library's own BF16 tensor-core kernels (FP32
+   accumulation) on samples labelled by the FP64 interpolation, and attached
+   to the tables `t`; the lattice entry points with precision KQED_SURROGATE
+   then evaluate it wherever the held-out error bound of a pair's cell of
+   (ln|x|, ln|y|, cb) is <= tau, and fall back to the interpolation (the
+   mixed-precision form) everywhere else.  Errors are in units of each weight
+   function's local scale (a power law in |x|, |y| fitted to the labels). */
+struct kqed_surrogate_opts {
+  size_t samples;   /* training samples, |x|, |y| log-uniform on the grid, cb uniform */
+  size_t heldout;   /* held-out samples that set the per-cell error bounds */
+  int batch;        /* samples per step, a multiple of 128 */
+  int epochs;       /* passes over the training samples */
+  double lr;        /* peak Adam learning rate (warm-up, cosine decay) */
+  uint64_t seed;
+  double tau;       /* initial acceptance bound */
+};
+struct kqed_surrogate_report {
+  double loss_final;              /* mean-square training loss, last steps */
+  double heldout_rms, heldout_max;      /* trained network, held-out samples */
+  double untrained_rms, untrained_max;  /* the same network before training */
+  double train_seconds;           /* wall time of the training steps */
+  double steps;
+  double cells_accepted;          /* fraction of cells whose bound is <= tau */
+  double gemm_tflops;             /* tensor-core product rate during training */
+  double seconds_total;           /* labels, training and bounds */
+};
+/* opts NULL: 1e7 samples, 1e6 held out, batch 8192, 4 epochs, lr 2e-3, tau 1e-3 */
+int kqed_surrogate_train(const struct QED_kernel_temps *t, const struct kqed_surrogate_opts *opts,
+                         struct kqed_surrogate_report *report);
+int kqed_surrogate_set_tolerance(const struct QED_kernel_temps *t, double tau);
+/* fraction of the feature cells whose bound is <= tau */
+int kqed_surrogate_cells(const struct QED_kernel_temps *t, double tau, double *accepted_fraction);
+/* at post-swap invariants d_u[n][3] = (|x|, |y|, cb) (device): the network's
+   weight functions d_wnet[n][39] (float) and, if d_winterp != NULL, the FP64
+   interpolation's d_winterp[n][39]; synchronises `stream` */
+int kqed_surrogate_weights(const struct QED_kernel_temps *t, size_t n, const double *d_u,
+                           float *d_wnet, double *d_winterp, void *stream);
+/* the trained parameters (kqed_mlp_param_count() floats) and target scaling
+   (9 + 3 * 39 floats: ln-range lo[3], scale[3], unused[3], oa[39], ob[39],
+   os[39]); either may be NULL */
+int kqed_surrogate_export(const struct QED_kernel_temps *t, float *params, float *norm);
+size_t kqed_mlp_param_count(void);
+/* One forward and backward pass of the network through the GPU kernels, no
+   update, host buffers (for checking gradients): params as exported,
+   feat[n][3] network inputs, target[n][39]; y[n][39] outputs, grad[params]
+   of the mean-square loss, *loss.  n a multiple of 128. */
+int kqed_mlp_forward_backward(const float *params, size_t n, const float *feat,
+                              const float *target, float *y, float *grad, double *loss);
+
 /* Diagnostics.  kqed_profile(1) starts recording CUDA events on the
    launching stream around every main launch (the record + assembly kernel
    pair of the lattice sums and of the batched L0) and around every Pi chunk

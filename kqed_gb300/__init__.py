@@ -74,6 +74,20 @@ class BatchInfo(ctypes.Structure):
                 ("tuned_ms", ctypes.c_double)]
 
 
+class SurrogateOpts(ctypes.Structure):
+    """struct kqed_surrogate_opts of include/kqed.h"""
+    _fields_ = [("samples", ctypes.c_size_t), ("heldout", ctypes.c_size_t),
+                ("batch", ctypes.c_int), ("epochs", ctypes.c_int), ("lr", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("tau", ctypes.c_double)]
+
+
+class SurrogateReport(ctypes.Structure):
+    """struct kqed_surrogate_report of include/kqed.h"""
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("loss_final", "heldout_rms", "heldout_max", "untrained_rms", "untrained_max",
+                 "train_seconds", "steps", "cells_accepted", "gemm_tflops", "seconds_total")]
+
+
 def lib():
     """The loaded C-ABI library (raises if it has not been built)."""
     global _lib
@@ -145,6 +159,23 @@ def lib():
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]
         L.kqed_bf16_gemm.restype = ctypes.c_int
+        T_ = ctypes.POINTER(QED_kernel_temps)
+        L.kqed_surrogate_train.argtypes = [T_, ctypes.POINTER(SurrogateOpts),
+                                           ctypes.POINTER(SurrogateReport)]
+        L.kqed_surrogate_train.restype = ctypes.c_int
+        L.kqed_surrogate_set_tolerance.argtypes = [T_, ctypes.c_double]
+        L.kqed_surrogate_set_tolerance.restype = ctypes.c_int
+        L.kqed_surrogate_cells.argtypes = [T_, ctypes.c_double, dp]
+        L.kqed_surrogate_cells.restype = ctypes.c_int
+        L.kqed_surrogate_weights.argtypes = [T_, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p]
+        L.kqed_surrogate_weights.restype = ctypes.c_int
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.kqed_surrogate_export.argtypes = [T_, fp, fp]
+        L.kqed_surrogate_export.restype = ctypes.c_int
+        L.kqed_mlp_param_count.restype = ctypes.c_size_t
+        L.kqed_mlp_forward_backward.argtypes = [fp, ctypes.c_size_t, fp, fp, fp, fp, dp]
+        L.kqed_mlp_forward_backward.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
         L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
@@ -380,3 +411,60 @@ def bf16_gemm(a_ptr, sam, sak, b_ptr, sbn, sbk, M, N, K, c_ptr, ldc, splits=1, s
     (bf16 operands by strides, fp32 result); device pointers."""
     _check(lib().kqed_bf16_gemm(a_ptr, sam, sak, b_ptr, sbn, sbk, M, N, K, splits, c_ptr, ldc,
                                 stream))
+
+
+def surrogate_train(t, samples=10_000_000, heldout=1_000_000, batch=8192, epochs=4, lr=2e-3,
+                    seed=5, tau=1e-3):
+    """kqed_surrogate_train: train the weight-function network on the GPU and
+    attach it to the tables (precision KQED_SURROGATE); returns the report."""
+    o = SurrogateOpts(samples, heldout, batch, epochs, lr, seed, tau)
+    r = SurrogateReport()
+    _check(lib().kqed_surrogate_train(t.ptr, ctypes.byref(o), ctypes.byref(r)))
+    return {f: getattr(r, f) for f, _ in SurrogateReport._fields_}
+
+
+def surrogate_set_tolerance(t, tau):
+    _check(lib().kqed_surrogate_set_tolerance(t.ptr, tau))
+
+
+def surrogate_cells(t, tau):
+    """fraction of feature cells whose held-out error bound is <= tau"""
+    v = ctypes.c_double()
+    _check(lib().kqed_surrogate_cells(t.ptr, tau, ctypes.byref(v)))
+    return v.value
+
+
+def surrogate_weights(t, u_ptr, n, wnet_ptr, winterp_ptr=None, stream=None):
+    """network (float [n][39]) and FP64 interpolation ([n][39]) weight functions
+    at post-swap invariants u [n][3] = (|x|, |y|, cb); device pointers"""
+    _check(lib().kqed_surrogate_weights(t.ptr, n, u_ptr, wnet_ptr, winterp_ptr, stream))
+
+
+def mlp_param_count():
+    return int(lib().kqed_mlp_param_count())
+
+
+def surrogate_export(t):
+    """(params [P] float32, norm [126] float32) of the attached network"""
+    p = np.zeros(mlp_param_count(), dtype=np.float32)
+    nm = np.zeros(9 + 3 * 39, dtype=np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    _check(lib().kqed_surrogate_export(t.ptr, p.ctypes.data_as(fp), nm.ctypes.data_as(fp)))
+    return p, nm
+
+
+def mlp_forward_backward(params, feat, target):
+    """one forward/backward pass of the network on the GPU kernels: (y [n][39],
+    grad [P], loss)"""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    feat = np.ascontiguousarray(feat, dtype=np.float32)
+    target = np.ascontiguousarray(target, dtype=np.float32)
+    n = feat.shape[0]
+    y = np.zeros((n, 39), dtype=np.float32)
+    g = np.zeros(mlp_param_count(), dtype=np.float32)
+    loss = ctypes.c_double()
+    fp = ctypes.POINTER(ctypes.c_float)
+    _check(lib().kqed_mlp_forward_backward(params.ctypes.data_as(fp), n, feat.ctypes.data_as(fp),
+                                           target.ctypes.data_as(fp), y.ctypes.data_as(fp),
+                                           g.ctypes.data_as(fp), ctypes.byref(loss)))
+    return y, g, loss.value

@@ -2239,6 +2239,156 @@ __global__ void dfma_probe_kernel(double *out, int iters, double a, double b)
   out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+/* ------------------------------------------------- learned surrogate */
+
+/* weight functions of interp_generic at post-swap invariants (x, y, cb), FP64,
+   from the node table: the surrogate's labels and the judge of its error.
+   W[37], W[38] carry the flag2 y-derivative differences wherever they can be
+   live (not on the last y interval). */
+__global__ void weight_labels_kernel(DevTables T, const double *__restrict__ u, size_t n,
+                                     double *__restrict__ W)
+{
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double x = u[3 * i], y = u[3 * i + 1], cb = u[3 * i + 2];
+    double *w = W + kSurOut * i;
+    const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
+    const double ylo = __ldg(T.YY), yhi = __ldg(T.YY + T.nstpy - 1);
+    if (!(x >= xlo && x <= xhi && y >= ylo && y <= yhi && fabs(cb) <= 1.0)) {
+      for (int j = 0; j < kSurOut; j++) w[j] = 0.0;
+      continue;
+    }
+    const int flag_hx = (x >= xhi), flag_hy = (y >= yhi);
+    const int ix0 = bsrch(T.XX, x, 0, T.nstpx), iy0 = bsrch(T.YY, y, 0, T.nstpy);
+    const int ix1 = flag_hx ? ix0 : ix0 + 1, iy1 = flag_hy ? iy0 : iy0 + 1;
+    Wts<double> wt;
+    if (flag_hx) {
+      wt.xA = 1.0; wt.xB = 0.0; wt.xC1 = 0.0; wt.xC2 = 0.0; wt.lAx = 1.0;
+    } else {
+      const Herm h = herm(x, __ldg(T.XX + ix0), __ldg(T.XX + ix1));
+      wt.xA = h.A * h.D; wt.xB = h.B * h.D; wt.xC1 = h.C1 * h.D; wt.xC2 = h.C2 * h.D; wt.lAx = h.lA;
+    }
+    if (flag_hy) {
+      wt.yA = 1.0; wt.yB = 0.0; wt.yC1 = 0.0; wt.yC2 = 0.0; wt.lAy = 1.0;
+    } else {
+      const Herm h = herm(y, __ldg(T.YY + iy0), __ldg(T.YY + iy1));
+      wt.yA = h.A * h.D; wt.yB = h.B * h.D; wt.yC1 = h.C1 * h.D; wt.yC2 = h.C2 * h.D; wt.lAy = h.lA;
+    }
+    wt.dd = (!flag_hy && iy0 + 1 < T.nstpy - 1) ? 1.0 : 0.0;
+    const int NK = T.NK;
+    const int Ktop = max(__ldg(T.nfx + ix0), __ldg(T.nfx + ix1)) + 2;
+    double Wd[39];
+    interp_generic<double>(T.node + ((size_t)ix0 * T.nstpy + iy0) * NK * kRow,
+                           T.node + ((size_t)ix0 * T.nstpy + iy1) * NK * kRow,
+                           T.node + ((size_t)ix1 * T.nstpy + iy0) * NK * kRow,
+                           T.node + ((size_t)ix1 * T.nstpy + iy1) * NK * kRow, Ktop, wt, 2.0 * cb,
+                           Wd);
+    for (int j = 0; j < kSurOut; j++) w[j] = Wd[j];
+  }
+}
+
+/* features of post-swap invariants, and the cell of feature space they fall in */
+__device__ __forceinline__ int sur_features(const SurDev &S, double x, double y, double cb,
+                                            float4 &f)
+{
+  const float u0 = (float)log(x), u1 = (float)log(y), u2 = (float)cb;
+  f.x = (u0 - S.lo[0]) * S.sc[0] - 1.0f;
+  f.y = (u1 - S.lo[1]) * S.sc[1] - 1.0f;
+  f.z = (u2 - S.lo[2]) * S.sc[2] - 1.0f;
+  f.w = 0.0f;
+  const int c0 = min(S.nb[0] - 1, max(0, (int)((f.x + 1.0f) * 0.5f * S.nb[0])));
+  const int c1 = min(S.nb[1] - 1, max(0, (int)((f.y + 1.0f) * 0.5f * S.nb[1])));
+  const int c2 = min(S.nb[2] - 1, max(0, (int)((f.z + 1.0f) * 0.5f * S.nb[2])));
+  return (c0 * S.nb[1] + c1) * S.nb[2] + c2;
+}
+
+/* Surrogate form, step 1 of a chunk: every pair the mixed form's lean pass
+   would evaluate in float (generic, on the grid, not assembled in FP64,
+   |cb| <= 0.99) whose feature cell has an error bound <= tau is selected
+   for the network (features appended in selection order); every other pair
+   goes to A.list for the full record kernel -- the interpolation fallback. */
+template <bool BATCH>
+__global__ void __launch_bounds__(64) lattice_sur_select_kernel(DevTables T,
+                                                                const __grid_constant__ LatticeArgs A,
+                                                                const LatticeArgs *jobs, int njobs,
+                                                                size_t u0, size_t nu, double near2,
+                                                                double orig2, const SurDev *Sp)
+{
+  const SurDev &S = *Sp;
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < nu * kTile;
+       r += (size_t)gridDim.x * blockDim.x) {
+    const LatticeArgs *Jp;
+    size_t k, n;
+    if (!record_pair<BATCH>(A, jobs, njobs, u0, r, Jp, k, n)) continue;
+    const LatticeArgs &J = *Jp;
+    double xv[4], yv[4];
+    for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
+    bool take = false;
+    float4 f;
+    if (!fp64_assembly(xv, yv, near2, orig2) &&
+        isfinite(fabs(xv[0]) + fabs(xv[1]) + fabs(xv[2]) + fabs(xv[3]) + fabs(yv[0]) +
+                 fabs(yv[1]) + fabs(yv[2]) + fabs(yv[3]))) {
+      Inv I;
+      invariants(T, xv, yv, I);
+      const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
+      const double ylo = __ldg(T.YY), yhi = __ldg(T.YY + T.nstpy - 1);
+      if (I.x >= xlo && I.x <= xhi && I.y >= ylo && I.y < yhi && fabs(I.cb) <= 0.99) {
+        /* swapped pairs also use the two y-derivative differences: their
+           own bound, after the ncell bounds of the 37 others */
+        const int cell = sur_features(S, I.x, I.y, I.cb, f);
+        const int ncell = S.nb[0] * S.nb[1] * S.nb[2];
+        take = __ldg(S.cell + (I.flag2 ? ncell : 0) + cell) <= S.tau;
+      }
+    }
+    if (take) {
+      const unsigned slot = atomicAdd(S.ecount, 1u);
+      S.elist[slot] = (uint32_t)r;
+      S.feat[slot] = f;
+    } else {
+      A.list[atomicAdd(A.count, 1u)] = (uint32_t)r;
+    }
+  }
+}
+
+/* Surrogate form, step 3: records of the selected pairs from the network's
+   weight functions (the float chain rule and record of the mixed form's
+   float pairs) */
+template <bool BATCH>
+__global__ void __launch_bounds__(64) lattice_sur_record_kernel(DevTables T,
+                                                                const __grid_constant__ LatticeArgs A,
+                                                                const LatticeArgs *jobs, int njobs,
+                                                                size_t u0, const SurDev *Sp)
+{
+  const SurDev &S = *Sp;
+  const size_t ne = *S.ecount;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ne;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = S.elist[i];
+    const LatticeArgs *Jp;
+    size_t k, n;
+    record_pair<BATCH>(A, jobs, njobs, u0, r, Jp, k, n);
+    const LatticeArgs &J = *Jp;
+    double xv[4], yv[4];
+    for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
+    Inv I;
+    invariants(T, xv, yv, I);
+    const float lx = (float)log(I.x), ly = (float)log(I.y);
+    const float *y = S.Y + i * kSurOutPad;
+    float W[39];
+#pragma unroll
+    for (int j = 0; j < kSurOut; j++) W[j] = y[j] * S.os[j] * __expf(S.oa[j] * lx + S.ob[j] * ly);
+    const int flag_hy = (I.y >= __ldg(T.YY + T.nstpy - 1));
+    const bool dd = I.flag2 && !flag_hy && I.iy + 1 < T.nstpy - 1;
+    if (!dd) { W[37] = 0.0f; W[38] = 0.0f; }
+    Sink sk;
+    sk.f = nullptr;
+    sk.d = A.rec + r * REC;
+    fill_record_f32(sk, xv, yv, I, W, T.ystp);
+    A.code[r] = pair_code(K_GEN, false, I.flag2 ? 4 : 0);
+    if (!J.pi) A.env[r] = pi_envelope(xv, yv);
+  }
+}
+
 static int num_sms()
 {
   static int n = 0;
@@ -2377,7 +2527,8 @@ cudaError_t launch_l0_mixed(const DevTables &T, const DevMaps &M, const L0Args &
 template <typename SI, typename S>
 static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
                                     const LatticeArgs *jobs, int njobs, size_t units,
-                                    const LaunchCfg &cfg, cudaStream_t s)
+                                    const LaunchCfg &cfg, cudaStream_t s,
+                                    const SurHook *hook = nullptr)
 {
   if (units == 0) return cudaSuccess;
   if (!a.rec || !a.code || a.rec_cap < (size_t)kTile) return cudaErrorInvalidValue;
@@ -2396,7 +2547,29 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
   for (size_t u0 = 0; u0 < units; u0 += cu) {
     const size_t nu = std::min(cu, units - u0);
     LatticeArgs al = a;
-    if (lean) {
+    if (lean && hook) {
+      /* surrogate form: select, evaluate the network, records of the
+         selected pairs; the full record kernel takes the rest */
+      if ((e = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(hook->ecount, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+      if (njobs)
+        lattice_sur_select_kernel<true><<<rec_grid(lattice_sur_select_kernel<true>, nu * kTile), 64,
+                                          0, s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
+                                                  orig2_of(cfg), hook->d);
+      else
+        lattice_sur_select_kernel<false><<<rec_grid(lattice_sur_select_kernel<false>, nu * kTile),
+                                           64, 0, s>>>(T, a, jobs, njobs, u0, nu, near2_of(cfg),
+                                                       orig2_of(cfg), hook->d);
+      g_launches++;
+      if ((e = hook->run(hook->state, nu * kTile, s)) != cudaSuccess) return e;
+      if (njobs)
+        lattice_sur_record_kernel<true><<<rec_grid(lattice_sur_record_kernel<true>, nu * kTile), 64,
+                                          0, s>>>(T, a, jobs, njobs, u0, hook->d);
+      else
+        lattice_sur_record_kernel<false><<<rec_grid(lattice_sur_record_kernel<false>, nu * kTile),
+                                           64, 0, s>>>(T, a, jobs, njobs, u0, hook->d);
+      g_launches++;
+    } else if (lean) {
       if ((e = cudaMemsetAsync(a.count, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
       if (njobs)
         lattice_rec_lean_kernel<true><<<rec_grid(lattice_rec_lean_kernel<true>, nu * kTile), 64, 0,
@@ -2425,6 +2598,24 @@ static cudaError_t launch_lattice_t(const DevTables &T, const DevMaps &M, const 
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+cudaError_t launch_lattice_surrogate(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                     const LaunchCfg &cfg, const SurHook &hook, cudaStream_t s)
+{
+  if (!a.list || !a.count || !hook.d || !hook.run || !hook.ecount) return cudaErrorInvalidValue;
+  return launch_lattice_t<float, float>(T, M, a, nullptr, 0, a.nx * (size_t)a.tiles, cfg, s,
+                                        &hook);
+}
+
+cudaError_t launch_weight_labels(const DevTables &T, const double *u, size_t n, double *W,
+                                 cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  const size_t b = min((n + 63) / 64, (size_t)num_sms() * 16);
+  weight_labels_kernel<<<(unsigned)b, 64, 0, s>>>(T, u, n, W);
+  g_launches++;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_lattice_fp64(const DevTables &T, const DevMaps &M, const LatticeArgs &a,

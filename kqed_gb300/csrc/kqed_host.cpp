@@ -530,6 +530,7 @@ extern "C" void free_QED_temps(struct QED_kernel_temps *t)
   Ctx *c = ctx_of(t);
   if (c) {
     if (tl_stage.owner == c->id) tl_stage.reset();
+    surrogate_forget(c);
     for (void *p : c->allocs) cudaFree(p);
     delete c;
     free(t->Grid.PC);
@@ -581,8 +582,21 @@ static int check_variant_precision(int variant, int precision)
 {
   if (variant < 0 || variant > 3) return fail("variant %d not in 0..3", variant);
   if (precision != KQED_FP64 && precision != KQED_FP32_MIXED)
-    return fail("precision mode %d is not available in this build", precision);
+    return fail("precision mode %d is not available for this entry point", precision);
   return 0;
+}
+
+/* the lattice sums also take the surrogate form, once a network is attached */
+static int check_lattice_precision(Ctx *c, int variant, int precision)
+{
+  if (precision == KQED_SURROGATE) {
+    if (variant < 0 || variant > 3) return fail("variant %d not in 0..3", variant);
+    if (!surrogate_ready(c))
+      return fail("precision KQED_SURROGATE: no surrogate trained for these tables "
+                  "(kqed_surrogate_train)");
+    return 0;
+  }
+  return check_variant_precision(variant, precision);
 }
 
 /* L0 over n pairs on the device */
@@ -902,7 +916,7 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.partial = st.d_tmp.get(nx * (size_t)std::max(R.tiles, 1) * 2);
   if (!R.partial) return fail("out of device memory for partial sums");
   const size_t ncol = nx * (size_t)c->T.nstpy * c->T.NK * kRow;
-  const bool mixed = precision == KQED_FP32_MIXED;
+  const bool mixed = precision == KQED_FP32_MIXED || precision == KQED_SURROGATE;
   /* FP64 columns always (the FP64 form, and the float form's pairs near
      cb = +-1 or assembled in FP64); float columns for the float
      interpolation of the mixed form */
@@ -944,6 +958,7 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
 {
   const size_t per_x = (size_t)R.c->T.nstpy * R.c->T.NK * kRow;
   const bool mixed = R.precision == KQED_FP32_MIXED;
+  const bool sur = R.precision == KQED_SURROGATE;
   LatticeArgs a{};
   a.x = R.d_x + 4 * x0;
   a.y = R.d_y;
@@ -971,8 +986,15 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
   a.n0 = R.y_offset;
   TimedLaunch tl;
   prof_begin(s, tl);
-  if (mixed) CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s));
-  else CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, R.c->cfg, s));
+  if (sur) {
+    SurHook hook;
+    if (surrogate_hook(R.c, R.rec_cap, &hook)) return 1;
+    CUDA_OK(launch_lattice_surrogate(R.c->T, R.c->M, a, R.c->cfg, hook, s));
+  } else if (mixed) {
+    CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s));
+  } else {
+    CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, R.c->cfg, s));
+  }
   prof_end(s, tl);
   return 0;
 }
@@ -983,7 +1005,7 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
 {
   Ctx *c = ctx_of(t);
   if (!c) return fail("tables not initialised");
-  if (check_variant_precision(variant, precision)) return 1;
+  if (check_lattice_precision(c, variant, precision)) return 1;
   if (nx == 0) return 0;
   if (!d_sums) return fail("null buffer");
   cudaStream_t s = (cudaStream_t)stream;
@@ -1008,7 +1030,7 @@ extern "C" int kqed_lattice_sum_synth(const struct QED_kernel_temps *t, int vari
 {
   Ctx *c = ctx_of(t);
   if (!c) return fail("tables not initialised");
-  if (check_variant_precision(variant, precision)) return 1;
+  if (check_lattice_precision(c, variant, precision)) return 1;
   if (nx == 0) return 0;
   if (!d_sums) return fail("null buffer");
   cudaStream_t s = (cudaStream_t)stream;
@@ -1049,7 +1071,7 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
 {
   Ctx *c = ctx_of(t);
   if (!c) return fail("tables not initialised");
-  if (check_variant_precision(variant, precision)) return 1;
+  if (check_lattice_precision(c, variant, precision)) return 1;
   if (nx == 0) return 0;
   if (!sums) return fail("null buffer");
   if (ny == 0) {   /* an empty lattice sums to zero (its site and Pi pointers may be NULL) */

@@ -126,6 +126,48 @@ struct LatticeArgs {
   size_t u_begin;       /* batch: first unit of this job */
 };
 
+/* The learned weight-function surrogate as the lattice kernels see it (a
+   device struct, filled by kqed_mlp.cu).  Features of a generic pair are its
+   post-swap invariants u = (ln|x|, ln|y|, cb) mapped to [-1, 1]^3; the
+   network predicts the 39 interpolated weight functions of interp_generic
+   scaled by a power law, W_i = out_i * os_i * |x|^oa_i * |y|^ob_i. */
+constexpr int kSurOut = 39;
+constexpr int kSurOutPad = 48;   /* output layer width on the tensor cores */
+struct SurDev {
+  const float *cell;      /* [2][nb0][nb1][nb2] error bound of the network per feature cell:
+                             the 37 weight functions of every pair, then all 39 (swapped
+                             pairs also use the two y-derivative differences) */
+  int nb[3];
+  float lo[3], sc[3];     /* f_j = (u_j - lo_j) * sc_j - 1 */
+  float tau;              /* a pair uses the network when its cell's bound <= tau */
+  float oa[kSurOut], ob[kSurOut], os[kSurOut];
+  float4 *feat;           /* [cap] features of the selected pairs, in selection order */
+  uint32_t *elist;        /* [cap] record index of each selected pair */
+  unsigned *ecount;       /* selected pairs */
+  const float *Y;         /* [cap][kSurOutPad] network outputs in selection order */
+};
+/* host side of a lattice launch with the surrogate: d = the device struct;
+   run(state, rows, stream) evaluates the network on the first *ecount of at
+   most `rows` selected pairs (features -> Y) */
+struct SurHook {
+  const SurDev *d;
+  unsigned *ecount;       /* the device counter of d (reset before each chunk) */
+  cudaError_t (*run)(void *state, size_t rows, cudaStream_t s);
+  void *state;
+};
+cudaError_t launch_lattice_surrogate(const DevTables &T, const DevMaps &M, const LatticeArgs &a,
+                                     const LaunchCfg &cfg, const SurHook &hook, cudaStream_t s);
+/* labels: W[i][39] = the FP64 interpolation at post-swap invariants
+   u[i] = (|x|, |y|, cb), zero outside the grid */
+cudaError_t launch_weight_labels(const DevTables &T, const double *u, size_t n, double *W,
+                                 cudaStream_t s);
+/* the surrogate attached to a device context (kqed_mlp.cu): the lattice
+   launch hook for `cap` records per chunk, whether one exists, and its
+   release when the context is freed */
+int surrogate_hook(const void *ctx, size_t cap, SurHook *hook);
+bool surrogate_ready(const void *ctx);
+void surrogate_forget(const void *ctx);
+
 int upload_map_constants();
 cudaError_t launch_l0_fp64(const DevTables &T, const DevMaps &M, const L0Args &a,
                            const LaunchCfg &cfg, cudaStream_t s);

@@ -54,3 +54,141 @@ def test_bf16_gemm_matches_float64(built, M, N, Kd, ta, tb, splits):
     assert np.all(np.isfinite(got))
     err = np.abs(got - ref) / (scale + 1e-30)
     assert err.max() <= 1e-5, (err.max(), np.unravel_index(np.argmax(err), err.shape))
+
+
+@pytest.fixture(scope="module")
+def temps(built):
+    import kqed_gb300 as K
+    t = K.KernelTemps()
+    yield t
+    t.free()
+
+
+def _oracle():
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                    "oracle"))
+    import mlp_oracle
+    return mlp_oracle
+
+
+def test_weight_labels_match_oracle(temps):
+    """the FP64 labels (interpolated weight functions at post-swap invariants)
+    against the oracle's restatement of extractff2: <= 1e-12 of each sample's
+    largest weight"""
+    import ctypes
+    import torch
+
+    from _helpers import oracle
+    g = temps.grid()
+    rng = np.random.default_rng(12)
+    n = 4096
+    lo, hi = max(g["XX"][0], g["YY"][0]), min(g["XX"][-1], g["YY"][-1])
+    u = np.empty((n, 3))
+    u[:, 0] = np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+    u[:, 1] = np.exp(rng.uniform(np.log(lo), np.log(g["YY"][-2]), n))
+    u[:, 2] = rng.uniform(-1, 1, n)
+    du = torch.as_tensor(u, device="cuda")
+    w = torch.zeros((n, 39), dtype=torch.float64, device="cuda")
+    K().surrogate_weights(temps, du.data_ptr(), n, None, w.data_ptr())
+    got = w.cpu().numpy()
+    O = oracle()
+    ref = np.zeros((n, 37))
+    dp = ctypes.POINTER(ctypes.c_double)
+    X, Y, C = (np.ascontiguousarray(u[:, i]) for i in range(3))
+    assert O.oracle_weights(n, X.ctypes.data_as(dp), Y.ctypes.data_as(dp), C.ctypes.data_as(dp),
+                            ref.ctypes.data_as(dp), 0) == 0
+    err = np.abs(got[:, :37] - ref).max(1) / np.abs(ref).max(1)
+    assert err.max() <= 1e-12, err.max()
+
+
+def test_network_forward_and_gradient_match_oracle(built):
+    """one forward/backward pass through the GPU kernels (BF16 tensor-core
+    products, FP32 accumulation) against the float64 oracle that rounds to
+    bf16 at the same points.  Remaining differences: FP32 accumulation order
+    and the rare activation that lands on the other side of a bf16 rounding
+    boundary.  Bounds: outputs 2e-3 of their largest magnitude; each
+    parameter block's gradient 1e-2 in relative 2-norm."""
+    MO = _oracle()
+    rng = np.random.default_rng(4)
+    n = 512
+    p = MO.init_params(11)
+    feat = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    target = rng.normal(size=(n, 39)).astype(np.float32)
+    y, g, loss = K().mlp_forward_backward(p, feat, target)
+    lref, gref, yref = MO.loss_and_grad(p, feat, target, bf=True)
+    assert np.abs(y - yref).max() <= 2e-3 * np.abs(yref).max()
+    assert abs(loss - lref) <= 1e-3 * lref
+    for name, (a, b) in MO.BLOCKS.items():
+        rel = np.linalg.norm(g[a:b] - gref[a:b]) / np.linalg.norm(gref[a:b])
+        assert rel <= 1e-2, (name, rel)
+
+
+@pytest.fixture(scope="module")
+def trained(temps):
+    rep = K().surrogate_train(temps, samples=2_000_000, heldout=200_000, batch=8192, epochs=3,
+                              lr=2e-3, seed=9, tau=1e-2)
+    return rep
+
+
+def test_training_gains_over_the_untrained_network(temps, trained):
+    """training on the GPU (a short run: 2e6 samples, 3 epochs) cuts the
+    held-out error of the weight functions (in units of their local scale)
+    at least fivefold, and the cell bounds accept part of feature space at a
+    5% bound"""
+    r = trained
+    assert r["steps"] > 0 and np.isfinite(r["loss_final"])
+    assert r["heldout_rms"] * 5 <= r["untrained_rms"], r
+    assert K().surrogate_cells(temps, 0.05) > 0.0, r
+    assert K().surrogate_cells(temps, np.inf) == 1.0
+
+
+def test_network_weights_track_the_interpolation(temps, trained):
+    """the network's weight functions against the FP64 interpolation on fresh
+    samples: the RMS error in local-scale units of the 37 weight functions
+    every generic pair uses stays near the held-out one"""
+    import torch
+    g = temps.grid()
+    rng = np.random.default_rng(13)
+    n = 8192
+    u = np.empty((n, 3))
+    u[:, 0] = np.exp(rng.uniform(np.log(g["XX"][0]), np.log(g["XX"][-1]), n))
+    u[:, 1] = np.exp(rng.uniform(np.log(g["YY"][0]), np.log(g["YY"][-1]), n))
+    u[:, 2] = rng.uniform(-1, 1, n)
+    du = torch.as_tensor(u, device="cuda")
+    wn = torch.zeros((n, 39), dtype=torch.float32, device="cuda")
+    wi = torch.zeros((n, 39), dtype=torch.float64, device="cuda")
+    K().surrogate_weights(temps, du.data_ptr(), n, wn.data_ptr(), wi.data_ptr())
+    _, norm = K().surrogate_export(temps)
+    oa, ob, os_ = norm[9:48], norm[48:87], norm[87:126]
+    scale = os_[None, :] * u[:, :1] ** oa[None, :] * u[:, 1:2] ** ob[None, :]
+    e = (np.abs(wn.cpu().numpy() - wi.cpu().numpy()) / scale)[:, :37]
+    rms = np.sqrt(np.mean(e ** 2))
+    assert rms <= 3 * trained["heldout_rms"] + 1e-6, (rms, trained["heldout_rms"])
+
+
+def test_surrogate_lattice_sum_falls_back_and_converges(temps, trained):
+    """lattice sums with precision KQED_SURROGATE: with tau = 0 every pair
+    falls back to the interpolation and the sums are the mixed form's bit for
+    bit; with every cell accepted the network serves the float pairs and the
+    integrand stays within 10% of rms_x(S_fp64); restoring tau restores the
+    fallback"""
+    from kqed_gb300.workloads import diagonal_x, lattice_sites, pi_synth_numpy
+    ys = lattice_sites(8, 0.2)
+    xs = diagonal_x(6, 0.2) + 0.013
+    pi = pi_synth_numpy(xs, ys, seed=5)
+    ref = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_FP64)
+    mixed = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_FP32_MIXED)
+    K().surrogate_set_tolerance(temps, 0.0)
+    fb = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_SURROGATE)
+    assert np.array_equal(fb, mixed)
+    K().surrogate_set_tolerance(temps, np.inf)
+    net = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_SURROGATE)
+    rms = np.sqrt(np.mean(ref ** 2))
+    assert np.all(np.isfinite(net))
+    assert not np.array_equal(net, mixed)
+    assert np.abs(net - ref).max() <= 0.1 * rms, (net, ref)
+    K().surrogate_set_tolerance(temps, 0.0)
+    assert np.array_equal(K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_SURROGATE),
+                          mixed)
