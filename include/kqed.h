@@ -277,6 +277,9 @@ struct kqed_surrogate_report {
 int kqed_surrogate_train(const struct QED_kernel_temps *t, const struct kqed_surrogate_opts *opts,
                          struct kqed_surrogate_report *report);
 int kqed_surrogate_set_tolerance(const struct QED_kernel_temps *t, double tau);
+/* pairs the network evaluated in lattice sums since the last call (the
+   counter is then reset); synchronises the device */
+int kqed_surrogate_served(const struct QED_kernel_temps *t, uint64_t *served);
 /* fraction of the feature cells whose bound is <= tau */
 int kqed_surrogate_cells(const struct QED_kernel_temps *t, double tau, double *accepted_fraction);
 /* at post-swap invariants d_u[n][3] = (|x|, |y|, cb) (device): the network's

@@ -165,6 +165,8 @@ def lib():
         L.kqed_surrogate_train.restype = ctypes.c_int
         L.kqed_surrogate_set_tolerance.argtypes = [T_, ctypes.c_double]
         L.kqed_surrogate_set_tolerance.restype = ctypes.c_int
+        L.kqed_surrogate_served.argtypes = [T_, ctypes.POINTER(ctypes.c_uint64)]
+        L.kqed_surrogate_served.restype = ctypes.c_int
         L.kqed_surrogate_cells.argtypes = [T_, ctypes.c_double, dp]
         L.kqed_surrogate_cells.restype = ctypes.c_int
         L.kqed_surrogate_weights.argtypes = [T_, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
@@ -425,6 +427,13 @@ def surrogate_train(t, samples=10_000_000, heldout=1_000_000, batch=8192, epochs
 
 def surrogate_set_tolerance(t, tau):
     _check(lib().kqed_surrogate_set_tolerance(t.ptr, tau))
+
+
+def surrogate_served(t):
+    """pairs the network evaluated in lattice sums since the last call"""
+    v = ctypes.c_uint64()
+    _check(lib().kqed_surrogate_served(t.ptr, ctypes.byref(v)))
+    return int(v.value)
 
 
 def surrogate_cells(t, tau):

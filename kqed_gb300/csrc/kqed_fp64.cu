@@ -2306,7 +2306,8 @@ __device__ __forceinline__ int sur_features(const SurDev &S, double x, double y,
    would evaluate in float (generic, on the grid, not assembled in FP64,
    |cb| <= 0.99) whose feature cell has an error bound <= tau is selected
    for the network (features appended in selection order); every other pair
-   goes to A.list for the full record kernel -- the interpolation fallback. */
+   falls back to the interpolation exactly as the mixed form evaluates it
+   (the lean float pass here, or A.list for the full record kernel). */
 template <bool BATCH>
 __global__ void __launch_bounds__(64) lattice_sur_select_kernel(DevTables T,
                                                                 const __grid_constant__ LatticeArgs A,
@@ -2344,9 +2345,25 @@ __global__ void __launch_bounds__(64) lattice_sur_select_kernel(DevTables T,
       const unsigned slot = atomicAdd(S.ecount, 1u);
       S.elist[slot] = (uint32_t)r;
       S.feat[slot] = f;
-    } else {
-      A.list[atomicAdd(A.count, 1u)] = (uint32_t)r;
+      continue;
     }
+    /* not for the network: the mixed form's own handling, so that a pair
+       falls back to exactly what the mixed form computes -- the lean float
+       pass for the float pairs, the full record kernel for the rest */
+    int kind = -1, status = 0;
+    if (!fp64_assembly(xv, yv, near2, orig2)) {
+      Sink sk;
+      sk.f = nullptr;
+      sk.d = A.rec + r * REC;
+      const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
+      kind = phase_a_lean(T, xv, yv, sk, status, J.col32 ? J.col32 + k * per_x : nullptr);
+    }
+    if (kind < 0) {
+      A.list[atomicAdd(A.count, 1u)] = (uint32_t)r;
+      continue;
+    }
+    A.code[r] = pair_code(kind, false, status);
+    if (!J.pi) A.env[r] = pi_envelope(xv, yv);
   }
 }
 
@@ -2361,6 +2378,7 @@ __global__ void __launch_bounds__(64) lattice_sur_record_kernel(DevTables T,
 {
   const SurDev &S = *Sp;
   const size_t ne = *S.ecount;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(S.etotal, (unsigned long long)ne);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ne;
        i += (size_t)gridDim.x * blockDim.x) {
     const size_t r = S.elist[i];

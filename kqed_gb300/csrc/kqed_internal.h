@@ -144,6 +144,7 @@ struct SurDev {
   float4 *feat;           /* [cap] features of the selected pairs, in selection order */
   uint32_t *elist;        /* [cap] record index of each selected pair */
   unsigned *ecount;       /* selected pairs */
+  unsigned long long *etotal;   /* selected pairs summed over chunks (read by the host) */
   const float *Y;         /* [cap][kSurOutPad] network outputs in selection order */
 };
 /* host side of a lattice launch with the surrogate: d = the device struct;

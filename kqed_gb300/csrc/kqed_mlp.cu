@@ -632,6 +632,7 @@ static cudaError_t surrogate_device_struct(Surrogate &S)
   d.feat = S.efeat;
   d.elist = S.elist;
   d.ecount = S.ecount;
+  d.etotal = reinterpret_cast<unsigned long long *>(S.ecount + 2);
   d.Y = S.ework.Y;
   if (!S.sdev) TRY(cudaMalloc(&S.sdev, sizeof(SurDev)));
   return cudaMemcpy(S.sdev, &d, sizeof(SurDev), cudaMemcpyHostToDevice);
@@ -845,7 +846,11 @@ static int ensure_capacity(Surrogate &S, size_t cap)
   if (S.elist) cudaFree(S.elist);
   S.efeat = nullptr;
   S.elist = nullptr;
-  if (!S.ecount && cudaMalloc(&S.ecount, sizeof(unsigned)) != cudaSuccess) return 1;
+  /* the per-chunk count, then (8-byte aligned) the running total */
+  if (!S.ecount) {
+    if (cudaMalloc(&S.ecount, 4 * sizeof(unsigned)) != cudaSuccess) return 1;
+    if (cudaMemset(S.ecount, 0, 4 * sizeof(unsigned)) != cudaSuccess) return 1;
+  }
   if (cudaMalloc(&S.efeat, cap * sizeof(float4)) != cudaSuccess ||
       cudaMalloc(&S.elist, cap * sizeof(uint32_t)) != cudaSuccess || S.ework.alloc(cap, false))
     return 1;
@@ -1072,5 +1077,23 @@ extern "C" int kqed_surrogate_export(const struct QED_kernel_temps *t, float *pa
       norm[9 + 78 + j] = S->norm.os[j];
     }
   }
+  return 0;
+}
+
+/* pairs the network evaluated in lattice sums since the last call (then
+   reset); synchronises the device */
+extern "C" int kqed_surrogate_served(const struct QED_kernel_temps *t, uint64_t *served)
+{
+  if (!t || !t->Grid.PC || !served) return set_error("tables not initialised");
+  mlp::Surrogate *S = mlp::find(t->Grid.PC->Fm);
+  if (!S) return set_error("no surrogate: train one for these tables first");
+  *served = 0;
+  if (!S->ecount) return 0;
+  unsigned long long v = 0;
+  if (cudaDeviceSynchronize() != cudaSuccess ||
+      cudaMemcpy(&v, S->ecount + 2, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemset(S->ecount + 2, 0, sizeof(v)) != cudaSuccess)
+    return set_error("kqed_surrogate_served: copy failed");
+  *served = v;
   return 0;
 }

@@ -180,11 +180,15 @@ def test_surrogate_lattice_sum_falls_back_and_converges(temps, trained):
     pi = pi_synth_numpy(xs, ys, seed=5)
     ref = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_FP64)
     mixed = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_FP32_MIXED)
+    K().surrogate_served(temps)
     K().surrogate_set_tolerance(temps, 0.0)
     fb = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_SURROGATE)
     assert np.array_equal(fb, mixed)
+    assert K().surrogate_served(temps) == 0
     K().surrogate_set_tolerance(temps, np.inf)
     net = K().lattice_sum(temps, 2, xs, ys, pi, precision=K().KQED_SURROGATE)
+    served = K().surrogate_served(temps)
+    assert 0 < served < len(xs) * len(ys), served
     rms = np.sqrt(np.mean(ref ** 2))
     assert np.all(np.isfinite(net))
     assert not np.array_equal(net, mixed)
