@@ -298,6 +298,10 @@ size_t kqed_mlp_param_count(void);
    of the mean-square loss, *loss.  n a multiple of 128. */
 int kqed_mlp_forward_backward(const float *params, size_t n, const float *feat,
                               const float *target, float *y, float *grad, double *loss);
+/* The network through the fused evaluation kernel that serves the lattice
+   sums (layers 2-4 on the tensor cores with activations kept in shared
+   memory), host buffers: y[n][39] for feat[n][3]. */
+int kqed_mlp_infer(const float *params, size_t n, const float *feat, float *y);
 
 /* Diagnostics.  kqed_profile(1) starts recording CUDA events on the
    launching stream around every main launch (the record + assembly kernel

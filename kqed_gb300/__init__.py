@@ -178,6 +178,8 @@ def lib():
         L.kqed_mlp_param_count.restype = ctypes.c_size_t
         L.kqed_mlp_forward_backward.argtypes = [fp, ctypes.c_size_t, fp, fp, fp, fp, dp]
         L.kqed_mlp_forward_backward.restype = ctypes.c_int
+        L.kqed_mlp_infer.argtypes = [fp, ctypes.c_size_t, fp, fp]
+        L.kqed_mlp_infer.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
         L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
@@ -477,3 +479,14 @@ def mlp_forward_backward(params, feat, target):
                                            target.ctypes.data_as(fp), y.ctypes.data_as(fp),
                                            g.ctypes.data_as(fp), ctypes.byref(loss)))
     return y, g, loss.value
+
+
+def mlp_infer(params, feat):
+    """the network through the fused evaluation kernel: y [n][39]"""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    feat = np.ascontiguousarray(feat, dtype=np.float32)
+    y = np.zeros((feat.shape[0], 39), dtype=np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    _check(lib().kqed_mlp_infer(params.ctypes.data_as(fp), feat.shape[0], feat.ctypes.data_as(fp),
+                                y.ctypes.data_as(fp)))
+    return y

@@ -45,10 +45,10 @@
 namespace kqed {
 namespace mlp {
 
-constexpr int H = 256, NIN = 3, NO = kSurOut, NOP = kSurOutPad;
-constexpr size_t oW1 = 0, ob1 = oW1 + (size_t)H * NIN, oW2 = ob1 + H, ob2 = oW2 + (size_t)H * H,
-                 oW3 = ob2 + H, ob3 = oW3 + (size_t)H * H, oW4 = ob3 + H,
-                 ob4 = oW4 + (size_t)NOP * H, kParams = ob4 + NOP;
+constexpr int H = kH, NIN = kNin, NO = kNo, NOP = kNop;
+static_assert(kNo == kSurOut && kNop == kSurOutPad, "surrogate widths");
+constexpr size_t oW1 = kOW1, ob1 = kOB1, oW2 = kOW2, ob2 = kOB2, oW3 = kOW3, ob3 = kOB3,
+                 oW4 = kOW4, ob4 = kOB4, kParams = kParamCount;
 constexpr int kSplits = 32;    /* K splits of the weight-gradient products */
 
 /* ------------------------------------------------------------- kernels */
@@ -285,6 +285,7 @@ static unsigned grid_for(size_t n, int threads = 256)
 struct Net {
   float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr;
   __nv_bfloat16 *W2h = nullptr, *W3h = nullptr, *W4h = nullptr;
+  __nv_bfloat16 *wimg = nullptr;     /* weight image of the fused evaluation kernel */
   int step = 0;
   int alloc()
   {
@@ -297,14 +298,16 @@ struct Net {
       return 1;
     W3h = W2h + (size_t)H * H;
     W4h = W3h + (size_t)H * H;
+    if (cudaMalloc(&wimg, kWimgBytes) != cudaSuccess) return 1;
     return 0;
   }
   void release()
   {
     if (P) cudaFree(P);
     if (W2h) cudaFree(W2h);
+    if (wimg) cudaFree(wimg);
     P = G = M = V = nullptr;
-    W2h = W3h = W4h = nullptr;
+    W2h = W3h = W4h = wimg = nullptr;
   }
 };
 
@@ -321,7 +324,7 @@ struct Work {
     rows = n;
     const size_t f = train ? (3 * n * H + 2 * n * NOP + n * H + (size_t)kSplits * H * H + 1024)
                            : (n * NOP);
-    const size_t h = train ? (5 * n * H + n * NOP) : (3 * n * H);
+    const size_t h = train ? (5 * n * H + n * NOP) : 0;
     if (cudaMalloc(&mem, f * sizeof(float) + h * sizeof(__nv_bfloat16) + 256) != cudaSuccess)
       return 1;
     float *fp = static_cast<float *>(mem);
@@ -335,11 +338,11 @@ struct Work {
       lossp = fp; fp += 1024;
     }
     Y = fp; fp += n * NOP;
-    __nv_bfloat16 *hp = reinterpret_cast<__nv_bfloat16 *>(fp);
-    H1 = hp; hp += n * H;
-    H2 = hp; hp += n * H;
-    H3 = hp; hp += n * H;
     if (train) {
+      __nv_bfloat16 *hp = reinterpret_cast<__nv_bfloat16 *>(fp);
+      H1 = hp; hp += n * H;
+      H2 = hp; hp += n * H;
+      H3 = hp; hp += n * H;
       dZa = hp; hp += n * H;
       dZb = hp; hp += n * H;
       dYb = hp; hp += n * NOP;
@@ -391,6 +394,15 @@ static cudaError_t forward(const Net &N, const float4 *feat, const unsigned *cou
   g.Mdev = countp;
   TRY(launch_gemm(g, 1, s));
   return cudaGetLastError();
+}
+
+/* Y = net(feat) by the fused evaluation kernel (the weight image must be
+   current: launch_build_wimg after the parameters change) */
+static cudaError_t infer(const Net &N, const float4 *feat, const unsigned *countp, size_t rows,
+                         float *Y, int *err, cudaStream_t s)
+{
+  InferArgs a{feat, countp, rows, N.P, N.wimg, Y, err};
+  return launch_mlp_infer(a, s);
 }
 
 /* gradient of the mean-square loss at the current weights into N.G */
@@ -515,6 +527,7 @@ static cudaError_t evaluate(const Net &N, const float4 *feat, const float *T, si
   const size_t chunk = 65536;
   Work w;
   if (w.alloc(chunk, false)) return cudaErrorMemoryAllocation;
+  TRY(launch_build_wimg(N.P, N.wimg, s));
   double *sums = nullptr;
   cudaError_t e = cudaMalloc(&sums, 2 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemsetAsync(sums, 0, 2 * sizeof(double), s);
@@ -525,7 +538,7 @@ static cudaError_t evaluate(const Net &N, const float4 *feat, const float *T, si
   }
   for (size_t o = 0; e == cudaSuccess && o < n; o += chunk) {
     const size_t m = std::min(chunk, n - o);
-    e = forward(N, feat + o, nullptr, m, w, false, err, s);
+    e = infer(N, feat + o, nullptr, m, w.Y, err, s);
     if (e != cudaSuccess) break;
     if (cell)
       cell_error_kernel<<<grid_for(m), 256, 0, s>>>(w.Y, T + 40 * o, feat + o, m, nb[0], nb[1],
@@ -834,7 +847,7 @@ static int train(const DevTables &T, const kqed_surrogate_opts &o, kqed_surrogat
 static cudaError_t run_hook(void *state, size_t rows, cudaStream_t s)
 {
   Surrogate *S = static_cast<Surrogate *>(state);
-  return forward(S->net, S->efeat, S->ecount, rows, S->ework, false, S->err, s);
+  return infer(S->net, S->efeat, S->ecount, rows, S->ework.Y, S->err, s);
 }
 
 /* evaluation buffers for `cap` selected pairs */
@@ -974,7 +987,7 @@ extern "C" int kqed_surrogate_weights(const struct QED_kernel_temps *t, size_t n
       mlp::prep_kernel<<<mlp::grid_for(n), 256, 0, s>>>(d_u, W, n, S->norm, feat, Tg);
       g_launches++;
       if (cudaGetLastError() != cudaSuccess ||
-          mlp::forward(S->net, feat, nullptr, n, w, false, S->err, s) != cudaSuccess)
+          mlp::infer(S->net, feat, nullptr, n, w.Y, S->err, s) != cudaSuccess)
         rc = set_error("kqed_surrogate_weights: evaluation failed");
     }
   }
@@ -1096,4 +1109,43 @@ extern "C" int kqed_surrogate_served(const struct QED_kernel_temps *t, uint64_t 
     return set_error("kqed_surrogate_served: copy failed");
   *served = v;
   return 0;
+}
+
+/* The fused evaluation kernel on host data (for checking it): params as
+   exported, feat[n][3]; y[n][39] */
+extern "C" int kqed_mlp_infer(const float *params, size_t n, const float *feat, float *y)
+{
+  using namespace mlp;
+  if (!params || !feat || !y || n == 0) return set_error("kqed_mlp_infer: bad arguments");
+  Net N;
+  float4 *df = nullptr;
+  float *dy = nullptr;
+  int *err = nullptr;
+  cudaStream_t s = nullptr;
+  int rc = 0;
+  std::vector<float4> hf(n);
+  for (size_t i = 0; i < n; i++) hf[i] = make_float4(feat[3 * i], feat[3 * i + 1], feat[3 * i + 2], 0.0f);
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess || N.alloc() ||
+      cudaMalloc(&df, n * sizeof(float4)) != cudaSuccess ||
+      cudaMalloc(&dy, n * NOP * sizeof(float)) != cudaSuccess || device_error_flag(&err))
+    rc = set_error("kqed_mlp_infer: out of memory");
+  if (!rc && (cudaMemcpyAsync(df, hf.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s) ||
+              cudaMemsetAsync(err, 0, sizeof(int), s) || upload_params(N, params, s) ||
+              launch_build_wimg(N.P, N.wimg, s) || infer(N, df, nullptr, n, dy, err, s)))
+    rc = set_error("kqed_mlp_infer: launch failed");
+  std::vector<float> hy(n * NOP);
+  int herr = 0;
+  if (!rc && (cudaMemcpyAsync(hy.data(), dy, n * NOP * sizeof(float), cudaMemcpyDeviceToHost, s) ||
+              cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s) ||
+              cudaStreamSynchronize(s)))
+    rc = set_error("kqed_mlp_infer: execution failed");
+  if (!rc && herr) rc = set_error("kqed_mlp_infer: a tensor-core wait timed out");
+  if (!rc)
+    for (size_t i = 0; i < n; i++)
+      for (int j = 0; j < NO; j++) y[i * NO + j] = hy[i * NOP + j];
+  N.release();
+  if (df) cudaFree(df);
+  if (dy) cudaFree(dy);
+  if (s) cudaStreamDestroy(s);
+  return rc;
 }
