@@ -10,9 +10,9 @@
  *                         weight chunk, K = 256, FP32 accumulator in tensor
  *                         memory (256 columns); the weights stream from the
  *                         pre-laid-out weight image (L2-resident, 8 chunks of
- *                         32 KB) into two shared-memory buffers by bulk TMA
- *                         copies, the next chunk landing while the tensor
- *                         cores work on the current one; the epilogue (bias,
+ *                         32 KB) into a ring of four shared-memory buffers by
+ *                         bulk TMA copies issued up to four chunks ahead, so the
+ *                         next layer's weights land during an epilogue; the epilogue (bias,
  *                         SiLU, BF16) reads the accumulator with tcgen05.ld
  *                         and writes the next layer's A tile in place
  *   layer 4 (256 -> 48)   tensor cores, N = 48, W4 resident in shared memory;
@@ -40,8 +40,9 @@ using namespace umma;
 constexpr int kIThreads = 256;
 constexpr int kIA = 128 * kH * 2;                 /* A tile, 64 KB */
 constexpr int kIParams = kH * 3 + kH + kH + kH + kNop;   /* W1 b1 b2 b3 b4 */
+constexpr int kWBufs = 4;                         /* weight-chunk ring in shared memory */
 constexpr int kInferSmem =
-    kIA + 2 * (int)kWimgChunk + (int)kWimgW4 + kIParams * 4 + 1024;
+    kIA + kWBufs * (int)kWimgChunk + (int)kWimgW4 + kIParams * 4 + 1024;
 
 __device__ __forceinline__ float silu_i(float z) { return z / (1.0f + __expf(-z)); }
 
@@ -82,11 +83,12 @@ __global__ void __launch_bounds__(kIThreads, 1) mlp_infer_kernel(InferArgs a)
   unsigned char *base = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   unsigned char *sA = base;
-  unsigned char *sW[2] = {base + kIA, base + kIA + kWimgChunk};
-  unsigned char *sW4 = base + kIA + 2 * kWimgChunk;
+  unsigned char *sW[kWBufs];
+  for (int i = 0; i < kWBufs; i++) sW[i] = base + kIA + i * kWimgChunk;
+  unsigned char *sW4 = base + kIA + kWBufs * kWimgChunk;
   float *sP = reinterpret_cast<float *>(sW4 + kWimgW4);
   float *sW1 = sP, *sb1 = sP + 3 * kH, *sb2 = sb1 + kH, *sb3 = sb2 + kH, *sb4 = sb3 + kH;
-  __shared__ uint64_t wbar[2], w4bar, ldone, mdone[2];
+  __shared__ uint64_t wbar[kWBufs], w4bar, ldone, mdone[kWBufs];
   __shared__ uint32_t s_taddr;
   __shared__ int s_fail;
 
@@ -99,12 +101,12 @@ __global__ void __launch_bounds__(kIThreads, 1) mlp_infer_kernel(InferArgs a)
   const unsigned char *img = reinterpret_cast<const unsigned char *>(a.wimg);
 
   if (tid == 0) {
-    mbar_init(&wbar[0], 1);
-    mbar_init(&wbar[1], 1);
+    for (int i = 0; i < kWBufs; i++) {
+      mbar_init(&wbar[i], 1);
+      mbar_init(&mdone[i], 1);
+    }
     mbar_init(&w4bar, 1);
     mbar_init(&ldone, 1);
-    mbar_init(&mdone[0], 1);
-    mbar_init(&mdone[1], 1);
     fence_mbar_init();
     s_fail = 0;
   }
@@ -130,12 +132,12 @@ __global__ void __launch_bounds__(kIThreads, 1) mlp_infer_kernel(InferArgs a)
   if (tid == 0) {
     mbar_expect_tx(&w4bar, (uint32_t)kWimgW4);
     bulk_g2s(sW4, img + 8 * kWimgChunk, (uint32_t)kWimgW4, &w4bar);
-    for (int c = 0; c < 2; c++) {
+    for (int c = 0; c < kWBufs; c++) {
       mbar_expect_tx(&wbar[c], (uint32_t)kWimgChunk);
       bulk_g2s(sW[c], img + c * kWimgChunk, (uint32_t)kWimgChunk, &wbar[c]);
     }
   }
-  loads = 2;
+  loads = kWBufs;   /* total_chunks >= 8 >= kWBufs */
   bool w4_ready = false;
   const uint32_t a0 = smem_u32(sA);
 
@@ -172,8 +174,8 @@ __global__ void __launch_bounds__(kIThreads, 1) mlp_infer_kernel(InferArgs a)
       if (tid == 0) {
         fence_after_sync();
         for (int q = 0; q < 4 && !s_fail; q++) {
-          const int b = (int)(g & 1);
-          if (!mbar_wait(&wbar[b], (uint32_t)((g >> 1) & 1))) { s_fail = 1; break; }
+          const int b = (int)(g % kWBufs);
+          if (!mbar_wait(&wbar[b], (uint32_t)((g / kWBufs) & 1))) { s_fail = 1; break; }
           const uint32_t b0 = smem_u32(sW[b]);
 #pragma unroll
           for (int kk = 0; kk < kH / 16; kk++)
@@ -182,16 +184,18 @@ __global__ void __launch_bounds__(kIThreads, 1) mlp_infer_kernel(InferArgs a)
                      kk > 0 ? 1u : 0u);
           mma_commit(&mdone[b]);
           if (g >= 1) {
-            /* the MMAs of chunk g - 1 are done with their buffer: refill it */
-            if (!mbar_wait(&mdone[(g - 1) & 1], (uint32_t)(((g - 1) >> 1) & 1))) {
+            /* the MMAs of chunk g - 1 are done with their buffer: refill it
+               with chunk g - 1 + kWBufs, kWBufs - 1 chunks ahead */
+            if (!mbar_wait(&mdone[(g - 1) % kWBufs], (uint32_t)(((g - 1) / kWBufs) & 1))) {
               s_fail = 1;
               g++;
               break;
             }
-            if (g + 1 < total_chunks) {
-              const size_t c = g + 1;
-              mbar_expect_tx(&wbar[c & 1], (uint32_t)kWimgChunk);
-              bulk_g2s(sW[c & 1], img + (c & 7) * kWimgChunk, (uint32_t)kWimgChunk, &wbar[c & 1]);
+            const size_t c = g - 1 + kWBufs;
+            if (c < total_chunks) {
+              const int cb = (int)(c % kWBufs);
+              mbar_expect_tx(&wbar[cb], (uint32_t)kWimgChunk);
+              bulk_g2s(sW[cb], img + (c & 7) * kWimgChunk, (uint32_t)kWimgChunk, &wbar[cb]);
               loads = c + 1;
             }
           }
@@ -283,7 +287,8 @@ __global__ void __launch_bounds__(kIThreads, 1) mlp_infer_kernel(InferArgs a)
      consumed, W4 if never waited for) and, after a failure, the MMAs */
   if (tid == 0) {
     if (s_fail && a.err) atomicExch(a.err, 1);
-    for (size_t c = g; c < loads; c++) mbar_wait(&wbar[c & 1], (uint32_t)((c >> 1) & 1), 1u << 26);
+    for (size_t c = g; c < loads; c++)
+      mbar_wait(&wbar[c % kWBufs], (uint32_t)((c / kWBufs) & 1), 1u << 26);
     if (!w4_ready) mbar_wait(&w4bar, 0, 1u << 26);
     if (s_fail) {
       mma_commit(&ldone);
