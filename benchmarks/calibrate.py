@@ -1,18 +1,21 @@
-"""Calibration of the FP64 work model in flops.py.
+"""Calibration of the work model in flops.py: the FP64 and the FP32 operations
+the lattice kernels execute per pair, per kernel.
 
   python -m benchmarks.calibrate --run            launches one fused lattice sum (L2)
                                                   per branch-uniform case (a record kernel
                                                   and an assembly kernel each); run it
-                                                  under ncu with the FP64 instruction
-                                                  counters
-  python -m benchmarks.calibrate --fit CSV        fits PER_K / FIXED / AXIS from the ncu CSV
-                                                  and writes flops_table.json
+                                                  under ncu with the FP64 and FP32
+                                                  instruction counters
+  python -m benchmarks.calibrate --fit CSV        fits, per kernel and pipe, PER_K /
+                                                  FIXED / AXIS from the ncu CSV and writes
+                                                  flops_table.json
 
 Cases: one x point against 4096 sites of a shifted 8^4 lattice (no site is 0
 or equal to x), at |x| in several grid cells (different Chebyshev lengths),
-plus x = 0 (every pair takes the x = 0 form).  Per-pair FP64 flops are the
-executed DFMA x 2 + DADD + DMUL of the case's lattice record and assembly
-kernels divided by its pairs.
+plus x = 0 (every pair takes the x = 0 form).  Per-pair flops of a pipe are
+the executed FMA x 2 + ADD + MUL thread instructions of that precision
+(DFMA/DADD/DMUL, FFMA/FADD/FMUL) of the case's record or assembly kernel
+divided by its pairs.
 """
 import argparse
 import csv
@@ -89,31 +92,42 @@ def fit(path, cases_path):
     ids = sorted(per_launch)
     if len(ids) != 2 * len(cases):
         raise SystemExit("expected %d lattice kernel launches, found %d" % (2 * len(cases), len(ids)))
-    launches = []
-    for i in range(len(cases)):
-        a, b = per_launch[ids[2 * i]], per_launch[ids[2 * i + 1]]
-        launches.append({m: a.get(m, 0.0) + b.get(m, 0.0) for m in set(a) | set(b)})
-    pts = []
-    axis = None
-    for c, m in zip(cases, launches):
-        fl = (2 * m["smsp__sass_thread_inst_executed_op_dfma_pred_on.sum"] +
-              m["smsp__sass_thread_inst_executed_op_dadd_pred_on.sum"] +
-              m["smsp__sass_thread_inst_executed_op_dmul_pred_on.sum"]) / c["pairs"]
-        c["flops_per_pair"] = fl
-        rd = m.get("dram__bytes_read.sum")
-        if c["ktop"] == 0:
-            axis = fl
-        else:
-            pts.append((c["ktop"], fl))
-    kt = np.array([p[0] for p in pts], float)
-    fl = np.array([p[1] for p in pts], float)
-    A = np.vstack([kt, np.ones_like(kt)]).T
-    (per_k, fixed), res, _, _ = np.linalg.lstsq(A, fl, rcond=None)
-    table = {"PER_K": float(per_k), "FIXED": float(fixed), "AXIS": float(axis), "CONTRACT": 0.0,
-             "CONTRACT_EXTRA": 0.0,
-             "source": "ncu executed FP64 ops of lattice_rec_kernel + lattice_asm_kernel "
-                       "(FP64 form), L2, benchmarks/calibrate.py",
-             "cases": cases}
+    ops = {"fp64": ("dfma", "dadd", "dmul"), "fp32": ("ffma", "fadd", "fmul")}
+
+    def count(m, pipe):
+        f, a, mu = ops[pipe]
+        g = lambda o: m.get("smsp__sass_thread_inst_executed_op_%s_pred_on.sum" % o, 0.0)
+        return 2 * g(f) + g(a) + g(mu)
+
+    table = {"source": "ncu executed FMA x 2 + ADD + MUL thread instructions of "
+                       "lattice_rec_kernel<double> and lattice_asm_kernel<double> (FP64 form), "
+                       "L2, benchmarks/calibrate.py",
+             "CONTRACT": 0.0, "CONTRACT_EXTRA": 0.0, "cases": cases, "kernels": {}}
+    for kname, off in (("record", 0), ("assembly", 1)):
+        for pipe in ("fp64", "fp32"):
+            pts, axis = [], None
+            for i, c in enumerate(cases):
+                fl = count(per_launch[ids[2 * i + off]], pipe) / c["pairs"]
+                c["%s_%s" % (kname, pipe)] = fl
+                if c["ktop"] == 0:
+                    axis = fl
+                else:
+                    pts.append((c["ktop"], fl))
+            kt = np.array([p[0] for p in pts], float)
+            fl = np.array([p[1] for p in pts], float)
+            A = np.vstack([kt, np.ones_like(kt)]).T
+            (per_k, fixed), _, _, _ = np.linalg.lstsq(A, fl, rcond=None)
+            table["kernels"]["%s_%s" % (kname, pipe)] = {
+                "PER_K": float(per_k), "FIXED": float(fixed), "AXIS": float(axis)}
+    # the FP64-equivalent model of earlier versions (all FP64 operations of
+    # both kernels, counted when the assembly ran in FP64) is kept as such
+    old = {}
+    prev = os.path.join(HERE, "flops_table.json")
+    if os.path.exists(prev):
+        old = json.load(open(prev))
+    for k in ("PER_K", "FIXED", "AXIS", "TRAFFIC_BYTES_PER_PAIR", "traffic_source"):
+        if k in old:
+            table[k] = old[k]
     with open(os.path.join(HERE, "flops_table.json"), "w") as f:
         json.dump(table, f, indent=1)
     print(json.dumps(table, indent=1))

@@ -31,9 +31,17 @@ def table():
     return dict(_DEFAULT)
 
 
-def lattice_flops(xs, ys, XX, nfx, variant):
-    """FP64 flops of one fused lattice launch over all (x_k, y_n)."""
+def lattice_flops(xs, ys, XX, nfx, variant, model=None):
+    """Flops of one fused lattice launch over all (x_k, y_n): the FP64-
+    equivalent model (model None), or one kernel's executed operations on one
+    pipe, model = "record_fp64", "record_fp32", "assembly_fp64",
+    "assembly_fp32" (calibrated per kernel and pipe)."""
     T = table()
+    if model is not None:
+        K = T.get("kernels", {}).get(model)
+        if K is None:
+            return None
+        T = dict(K, CONTRACT=0.0, CONTRACT_EXTRA=0.0)
     xs = np.asarray(xs)
     ys = np.asarray(ys)
     nx, ny = len(xs), len(ys)
@@ -43,6 +51,8 @@ def lattice_flops(xs, ys, XX, nfx, variant):
         xv = xs[k]
         xz = float(xv @ xv) < 1e-28
         same = ((ys - xv) ** 2).sum(1) < 1e-28
+        if xz and variant >= 2:
+            continue            # every L2 / L3 term at x = 0 cancels: the pairs are skipped
         if xz:
             n_axis = int(ynz.sum())
             n_gen = 0

@@ -324,6 +324,8 @@ int kqed_bf16_gemm(const void *d_a, long long sam, long long sak, const void *d_
 int kqed_profile_read(double *total_ms, uint64_t *launches);
 int kqed_profile_read_copies(double *total_ms, uint64_t *copies);
 int kqed_fp64_peak_gflops(double *gflops);
+/* the same FMA-chain probe on the FP32 pipe (GFLOP/s) */
+int kqed_fp32_peak_gflops(double *gflops);
 
 #ifdef __cplusplus
 }

@@ -180,6 +180,8 @@ def lib():
         L.kqed_mlp_forward_backward.restype = ctypes.c_int
         L.kqed_mlp_infer.argtypes = [fp, ctypes.c_size_t, fp, fp]
         L.kqed_mlp_infer.restype = ctypes.c_int
+        L.kqed_fp32_peak_gflops.argtypes = [dp]
+        L.kqed_fp32_peak_gflops.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
         L.kqed_fp64_peak_gflops.restype = ctypes.c_int
         _lib = L
@@ -402,6 +404,12 @@ def profile_read_copies():
     n = ctypes.c_uint64()
     _check(lib().kqed_profile_read_copies(ctypes.byref(ms), ctypes.byref(n)))
     return ms.value, int(n.value)
+
+
+def fp32_peak_gflops():
+    g = ctypes.c_double()
+    _check(lib().kqed_fp32_peak_gflops(ctypes.byref(g)))
+    return g.value
 
 
 def fp64_peak_gflops():

@@ -91,8 +91,10 @@ enum { alpha0dx_0p = 0, alpha0_1p, alpha3_0p, beta2_1p, alpha3_1p, alpha1_0p, be
 
 /* ------------------------------------------------------------ records */
 
-/* K_GEN64: a generic pair assembled in FP64 proper (near-parallel x, y) */
-enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4, K_GEN64 = 5 };
+/* K_GEN64: a generic pair whose STV components are taken in FP64
+   (near-parallel x, y); K_VANISH: a lattice pair whose whole contribution
+   (kernel and per-site / per-x terms) cancels identically */
+enum Kind { K_NONE = 0, K_GEN = 1, K_X0 = 2, K_Y0 = 3, K_Y0PERM = 4, K_GEN64 = 5, K_VANISH = 6 };
 
 /* generic record (doubles) */
 enum {
@@ -132,6 +134,26 @@ __device__ __forceinline__ double dot4_rn(const double *a, const double *b)
   s = __dadd_rn(s, __dmul_rn(a[1], b[1]));
   s = __dadd_rn(s, __dmul_rn(a[2], b[2]));
   return __dadd_rn(s, __dmul_rn(a[3], b[3]));
+}
+
+/* The same products with multiply-add contraction, in a fixed order (so
+   every caller gets the same bits); within 1e-14 of a decision boundary
+   their rounding can differ from dot4_rn's, so the decided forms below
+   re-evaluate with dot4_rn there.  Away from the boundaries the decision
+   cannot flip and the cheaper evaluation stands (the portable evaluation
+   everywhere cost 1.6% of the lattice sum). */
+__device__ __forceinline__ double dot4_fma(const double *a, const double *b)
+{
+  return fma(a[3], b[3], fma(a[2], b[2], fma(a[1], b[1], a[0] * b[0])));
+}
+
+/* v.v for a decision against the squared edges e0^2 and e1^2 */
+__device__ __forceinline__ double sq4_decided(const double *v, double e0, double e1)
+{
+  const double s = dot4_fma(v, v);
+  const double q0 = e0 * e0, q1 = e1 * e1;
+  if (fabs(s - q0) <= 2e-14 * q0 || fabs(s - q1) <= 2e-14 * q1) return dot4_rn(v, v);
+  return s;
 }
 
 /* bsrch, src/LIBFILES/getff-new.c:199-210 */
@@ -462,7 +484,8 @@ __global__ void build_columns_kernel(DevTables T, const double *__restrict__ xs,
     const int iy = rem / T.NK, K = rem % T.NK;
     S *out = col + u * kRow;
     const double *xv = xs + 4 * k;
-    double xsq = dot4_rn(xv, xv);   /* the same |x| as the pairs' invariants */
+    /* the same |x| as the pairs' invariants */
+    double xsq = sq4_decided(xv, __ldg(T.XX), __ldg(T.XX + T.nstpx - 1));
     xsq = xsq < 1E-7 ? 1E-7 : xsq;
     const double X = sqrt(fabs(xsq));
     const double xlo = __ldg(T.XX), xhi = __ldg(T.XX + T.nstpx - 1);
@@ -563,23 +586,27 @@ __device__ __forceinline__ void invariants(const DevTables &T, const double *xv,
                                            Inv &I)
 {
   const double EPSIN = 1E-7;
-  I.xsq = dot4_rn(xv, xv);
+  /* |x| decides the grid (beyond the last node: zero kernel; below the
+     first: the Taylor branch), so it is evaluated as the reference's
+     portable build does within 1e-14 of those edges; the other invariants
+     drive only continuous choices */
+  I.xsq = sq4_decided(xv, __ldg(T.XX), __ldg(T.XX + T.nstpx - 1));
   I.xsq = I.xsq < EPSIN ? EPSIN : I.xsq;
   I.x = sqrt(fabs(I.xsq));
-  I.ysq = dot4_rn(yv, yv);
+  I.ysq = dot4_fma(yv, yv);
   I.ysq = I.ysq < EPSIN ? EPSIN : I.ysq;
   I.y = sqrt(fabs(I.ysq));
-  I.xdoty = dot4_rn(xv, yv);
-  I.cb = I.xdoty / __dmul_rn(I.x, I.y);
+  I.xdoty = dot4_fma(xv, yv);
+  I.cb = I.xdoty / (I.x * I.y);
   I.cborig = I.cb;
   I.yorig = I.y;
-  I.xmysq = __dsub_rn(__dmul_rn(__dadd_rn(I.xsq, I.ysq), 1.00000000000001), __dmul_rn(2.0, I.xdoty));
+  I.xmysq = (I.xsq + I.ysq) * (1.00000000000001) - 2.0 * I.xdoty;
   I.xmy = sqrt(fabs(I.xmysq));
   I.flag2 = 0;
   const double rx = (I.x > I.xmy ? I.xmy / I.x : I.x / I.xmy);
   const double rxy = (I.x > I.y ? I.y / I.x : I.x / I.y);
   if (rx < rxy && I.xmy < __ldg(T.YY + T.nstpy - 1) && fabs(I.xmysq) > 1E-28) {
-    I.cb = __dsub_rn(I.x, __dmul_rn(I.y, I.cb)) / I.xmy;
+    I.cb = (I.x - I.y * I.cb) / I.xmy;
     I.y = I.xmy;
     I.flag2 = 1;
   }
@@ -1008,7 +1035,7 @@ __device__ void fill_generic_record(const Sink &R, const double *xvd, const doub
    the TAYLORX grid (zero kernel) */
 __device__ int fill_x0_record(const DevTables &T, const Sink &R, const double *yv)
 {
-  const double ysq = dot4_rn(yv, yv);
+  const double ysq = sq4_decided(yv, __ldg(T.TX + T.ny_tay - 1), __ldg(T.TX + T.ny_tay - 1));
   const double y = sqrt(fabs(ysq));
   const int it = bsrch(T.TX, y, 0, T.ny_tay);
   if (it == T.ny_tay - 1) return 1;
@@ -1055,7 +1082,7 @@ __device__ int fill_x0_record(const DevTables &T, const Sink &R, const double *y
    beyond the grid (zero kernel) */
 __device__ int fill_y0_record(const DevTables &T, const Sink &R, const double *xv)
 {
-  const double xsq = dot4_rn(xv, xv);
+  const double xsq = sq4_decided(xv, __ldg(T.XX), __ldg(T.XX + T.nstpx - 1));
   const double x = sqrt(fabs(xsq));
   int ix = bsrch(T.XX, x, 0, T.nstpx);
   if (x > __ldg(T.XX + T.nstpx - 1)) return 1;
@@ -1105,7 +1132,8 @@ __device__ int fill_y0_record(const DevTables &T, const Sink &R, const double *x
 
 __device__ __forceinline__ bool is_zero4(const double *v)
 {
-  return dot4_rn(v, v) < 1E-28;
+  const double s = dot4_fma(v, v);
+  return (fabs(s - 1E-28) <= 2e-14 * 1E-28 ? dot4_rn(v, v) : s) < 1E-28;
 }
 
 __device__ __forceinline__ double to_double(double v) { return v; }
@@ -1754,6 +1782,10 @@ __global__ void __launch_bounds__(64) lattice_rec_kernel(DevTables T, const __gr
     const LatticeArgs &J = *Jp;
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
+    if (J.zero_x_vanishes && is_zero4(xv)) {
+      A.code[r] = pair_code(K_VANISH, false, 0);
+      continue;
+    }
     const bool f64 = mixed && fp64_assembly(xv, yv, near2, orig2);
     Sink sk;
     sk.f = nullptr;
@@ -1915,34 +1947,61 @@ __device__ __forceinline__ float d2f_round(double v)
    Two kinds of pair leave the assembly with their components rounded
    through FP64:
    - near-parallel generic pairs (K_GEN64: max(|cb|, |cb'|) > 0.99, in the
-     FP64 form and among the mixed form's FP64-assembled pairs) are
-     assembled in FP64 proper and then split to double-float.  Their STV
-     components cancel strongly (the reference's own AVX2/FMA and portable
-     builds differ by up to 6e-13 there); in double-float, with 5 bits less
-     than FP64, the cancellation left errors up to 1.3e-11;
-   - the x = 0 / y = 0 / x = y forms are the kernels that the per-site and
-     per-x terms of L1..L3 repeat, and those terms are FP64 values of the
-     same double-float results (L2(0, y) = L0(0, y) - L0(0, y) - L0(0, 0) is
-     zero in the reference, src/LIBFILES/kernels.c:136-177): their components
-     are rounded to FP64 and split again, exactly as the terms were, so the
-     cancellation in the contraction is exact as in the reference. */
+     FP64 form and among the mixed form's FP64-assembled pairs) compute
+     their STV components in FP64 from the FP64 record and only the map in
+     double-float: the Tx / Ty formulas cancel strongly there (the
+     reference's own AVX2/FMA and portable builds differ by up to 6e-13),
+     and in double-float, with 5 bits less than FP64, the cancellation left
+     errors up to 1.3e-11 (the map itself amplifies rounding at most ~3x);
+   - in lattice sums (round_axis), the y = 0 and x = y forms, which the
+     per-x terms of L1..L3 repeat as FP64 values of the same double-float
+     results (L2(x, 0) = L0(x, 0) - L0(0, 0) - L0(x, 0) and L1(x, x),
+     L3(x, x) are zero in the reference, src/LIBFILES/kernels.c:117-177):
+     their components are rounded to FP64 and split again, exactly as the
+     terms were, so the cancellation in the contraction is exact as in the
+     reference.  (At x = 0 every L2 / L3 term cancels identically; those
+     pairs are K_VANISH and skipped.) */
+/* the rare pairs of asm_pair, out of line so that the hot loop of the
+   assembly kernels keeps its size and registers (inlined, these paths cost
+   2.5% of the FP64 lattice sum) */
+__device__ __noinline__ void asm_pair_rare(const AsmSmem &L, const DevMaps &M, const double *grec,
+                                           int kind, bool g64, int lane)
+{
+  df *tb = reinterpret_cast<df *>(L.tbuf);
+  if (g64) {
+    /* STV in FP64 from the FP64 record, then the map in double-float */
+    for (int i = lane; i < REC; i += 32) L.rec[i] = __ldg(grec + i);
+    if (lane == 0) { L.stv[200] = 0.0; L.stv[201] = 0.0; }
+    __syncwarp();
+    stv_generic<double>(L.rec, L.stv, lane);
+    __syncwarp();
+    df *stv = reinterpret_cast<df *>(L.stv);
+    for (int i = lane; i < 202; i += 32) stv[i] = split_d<true>(L.stv[i]);
+    __syncwarp();
+    apply_map_warp_df(L.eg, L.rg, M.gen, L.coeff, stv, tb, lane);
+  } else {
+    df *rd = reinterpret_cast<df *>(L.rec);
+    for (int i = lane; i < REC; i += 32) rd[i] = split_d(__ldg(grec + i));
+    __syncwarp();
+    assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), tb, lane);
+    for (int i = lane; i < 384; i += 32) tb[i] = split_d<true>(df_to_d<true>(tb[i]));
+  }
+  __syncwarp();
+}
+
 template <typename S>
 __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, const double *grec,
-                                         int code, int lane, bool &perm, bool &t64)
+                                         int code, int lane, bool &perm, bool &t64,
+                                         bool round_axis = false)
 {
   const int kind0 = code & 7;
   const bool g64 = kind0 == K_GEN64;
   const int kind = g64 ? K_GEN : kind0;
   perm = (kind == K_Y0PERM);
   t64 = sizeof(S) == 8 || (code & 8) || g64;
-  if (kind == K_NONE) return false;
-  df *tb = reinterpret_cast<df *>(L.tbuf);
-  if (g64) {
-    for (int i = lane; i < REC; i += 32) L.rec[i] = __ldg(grec + i);
-    __syncwarp();
-    assemble<double>(L, M, K_GEN, L.rec, L.stv, L.tbuf, L.coefd, lane);
-    for (int i = lane; i < 384; i += 32) tb[i] = split_d<true>(L.tbuf[i]);
-    __syncwarp();
+  if (kind == K_NONE || kind == K_VANISH) return false;
+  if (t64 && (g64 || (round_axis && (kind == K_Y0 || kind == K_Y0PERM)))) {
+    asm_pair_rare(L, M, grec, kind, g64, lane);
   } else if (t64) {
     /* FP64 records assembled in double-float on the FP32 pipe; the same
        (hardware) split in both forms, so that the mixed form's FP64 pairs
@@ -1950,11 +2009,8 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
     df *rd = reinterpret_cast<df *>(L.rec);
     for (int i = lane; i < REC; i += 32) rd[i] = split_d(__ldg(grec + i));
     __syncwarp();
-    assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), tb, lane);
-    if (kind != K_GEN) {
-      for (int i = lane; i < 384; i += 32) tb[i] = split_d<true>(df_to_d<true>(tb[i]));
-      __syncwarp();
-    }
+    assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), reinterpret_cast<df *>(L.tbuf),
+                lane);
   } else {
     float *rf = reinterpret_cast<float *>(L.rec);
     for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));
@@ -2134,8 +2190,10 @@ __global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __
         if (J.pi) prefetch_l2(J.pi + (k * J.ny + nn) * 384 + lane * 16);
         if (J.Ky2) prefetch_l2(J.Ky2 + nn * 384 + lane * 16);
       }
+      const int code = A.code[r];
+      if ((code & 7) == K_VANISH) continue;
       bool perm, t64;
-      const bool live = asm_pair<S>(L, M, A.rec + r * REC, A.code[r], lane, perm, t64);
+      const bool live = asm_pair<S>(L, M, A.rec + r * REC, code, lane, perm, t64, true);
       const double *ky = J.Ky ? J.Ky + n * 384 : nullptr, *bx = J.Bx ? J.Bx + k * 384 : nullptr;
       const float2 *ky2 = J.Ky2 ? J.Ky2 + n * 384 : nullptr;
       const float2 *bx2 = J.Bx2 ? J.Bx2 + k * 384 : nullptr;
@@ -2234,6 +2292,22 @@ __global__ void dfma_probe_kernel(double *out, int iters, double a, double b)
     for (int c = 0; c < 8; c++) v[c] = fma(v[c], a, b);
   }
   double s = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) s += v[c];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+/* the same chain pattern on the FP32 pipe */
+__global__ void ffma_probe_kernel(float *out, int iters, float a, float b)
+{
+  float v[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) v[c] = threadIdx.x * 1e-3f + c;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) v[c] = fmaf(v[c], a, b);
+  }
+  float s = 0;
 #pragma unroll
   for (int c = 0; c < 8; c++) s += v[c];
   out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
@@ -2816,6 +2890,36 @@ cudaError_t launch_axpy(double *y, const double *x, double a, size_t n, cudaStre
   axpy_kernel<<<(unsigned)b, 256, 0, s>>>(y, x, a, n);
   g_launches++;
   return cudaGetLastError();
+}
+
+cudaError_t probe_fp32_peak(double *gflops)
+{
+  const int blocks = num_sms() * 8, threads = 256, iters = 4096;
+  float *out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(float) * blocks * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  ffma_probe_kernel<<<blocks, threads>>>(out, 64, 0.999999f, 1e-7f);
+  cudaDeviceSynchronize();
+  float best = 1e30f;
+  for (int r = 0; r < 5; r++) {
+    cudaEventRecord(e0);
+    ffma_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999f, 1e-7f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  g_launches += 6;
+  *gflops = 2.0 * 8 * (double)iters * blocks * threads / best / 1e6;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  e = cudaGetLastError();
+  cudaFree(out);
+  return e;
 }
 
 cudaError_t probe_fp64_peak(double *gflops)

@@ -129,6 +129,12 @@ extern "C" int kqed_fp64_peak_gflops(double *gflops)
   return 0;
 }
 
+extern "C" int kqed_fp32_peak_gflops(double *gflops)
+{
+  CUDA_OK(probe_fp32_peak(gflops));
+  return 0;
+}
+
 
 /* ---------------------------------------------------------- context */
 
@@ -984,6 +990,7 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
   a.pi_stream = R.pi_stream;
   a.k0 = R.x_offset + x0;
   a.n0 = R.y_offset;
+  a.zero_x_vanishes = R.variant >= 2;
   TimedLaunch tl;
   prof_begin(s, tl);
   if (sur) {
@@ -1421,6 +1428,7 @@ extern "C" int kqed_batch_plan_create(const struct QED_kernel_temps *t, int njob
       }
       A.Ky = Y->ky;
       A.Ky2 = Y->ky2;
+      A.zero_x_vanishes = J.variant >= 2;
       if (plan_alloc(p, &p->bx[j], J.nx * 384)) return 1;
       if (J.variant == 3 && plan_alloc(p, &p->bt[j], J.nx * 384)) return 1;
       if (plan_alloc(p, &p->bx2[j], J.nx * 384)) return 1;

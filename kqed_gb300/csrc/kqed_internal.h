@@ -124,6 +124,9 @@ struct LatticeArgs {
   size_t k0;            /* generated Pi: global index of x[0] */
   size_t n0;            /* generated Pi: global index of y[0] */
   size_t u_begin;       /* batch: first unit of this job */
+  int zero_x_vanishes;  /* L2 / L3: at x = 0 every term cancels identically
+                           (L2(0, y) = L0(0, y) - L0(0, y) - L0(0, 0)), so such pairs
+                           contribute exactly zero and are skipped */
 };
 
 /* The learned weight-function surrogate as the lattice kernels see it (a
@@ -202,6 +205,7 @@ cudaError_t launch_fill_pairs(const double *src, size_t n, int mode, double *dst
                               cudaStream_t s);
 size_t smem_bytes_l0(int warps_per_block);
 cudaError_t probe_fp64_peak(double *gflops);
+cudaError_t probe_fp32_peak(double *gflops);
 extern std::atomic<uint64_t> g_launches;
 
 /* device handles of an initialised struct QED_kernel_temps (0 on success) */

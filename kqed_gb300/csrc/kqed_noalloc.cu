@@ -237,6 +237,7 @@ extern "C" int kqed_lattice_sum_noalloc(const struct QED_kernel_temps *t, int va
   a.rec = RC.rec;
   a.code = RC.code;
   a.rec_cap = RC.cap;
+  a.zero_x_vanishes = variant >= 2;
   if (kqed::launch_lattice_fp64(T, M, a, cfg, s) != cudaSuccess ||
       kqed::launch_reduce_partials(partial, nx, (int)tiles, d_sums, s) != cudaSuccess)
     return kqed::set_error("kqed_lattice_sum_noalloc: lattice kernel launch failed");
