@@ -2,7 +2,9 @@
 its per-branch accounting of a lattice launch agrees with the oracle's own
 classification of every (x, y) pair -- x = 0 / y = 0 / x = y pairs at the
 axis cost, generic pairs (on or below the x grid, swapped or not) at
-PER_K * Ktop + FIXED, zero kernels (x = y = 0) free.  The grid is given
+PER_K * Ktop + FIXED, zero kernels (x = y = 0) free, and for L2 / L3 the
+x = 0 rows free (their terms cancel identically and the kernels skip
+them).  The grid is given
 the table's x extents and a constant Chebyshev length, so Ktop is the same
 in every cell."""
 import ctypes
@@ -32,6 +34,8 @@ def test_lattice_work_model_matches_oracle_branches():
     for variant in (0, 2):
         expect = 0.0
         for xv in xs:
+            if variant >= 2 and float(xv @ xv) < 1e-28:
+                continue
             code = oracle_branch(np.repeat(xv[None, :], len(ys), 0), ys)
             base = code & 7
             assert not np.any(code & 16)
