@@ -91,6 +91,73 @@ void QED_kernel_L2(const double xv[4], const double yv[4], const struct QED_kern
 void QED_kernel_L3(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
                    double kerv[6][4][4][4]);
 
+/* src/HEADERS/KQED.h:101-125: the composite kernels' output structs (the
+   reference aligns their arrays to 32 bytes in AVX builds; the layout --
+   sizes and offsets -- is the same either way). */
+struct Kernel {
+  double xy[6][4][4][4];
+  double yx[6][4][4][4];
+};
+struct Kernels {
+  double L0[6][4][4][4];
+  double L1[6][4][4][4];
+  double L2[6][4][4][4];
+  double L3[6][4][4][4];
+};
+struct QED_Kernels {
+  struct Kernel L0;
+  struct Kernel L1;
+  struct Kernel L2;
+  struct Kernel L3;
+};
+struct QED_Con_Kernels {
+  struct Kernels A;
+  struct Kernels B;
+  struct Kernels C;
+};
+
+/* Replace QED_Mkernel_L2, src/LIBFILES/kernels.c:181-231 (kernels.h:23-28):
+   L0(x,y) - exp(-M x^2/2)[L0(0,y) - M x_mu x.L0(0,y)]
+           - exp(-M y^2/2)[L0(x,0) - M y_nu y.L0(x,0)]. */
+void QED_Mkernel_L2(const double M, const double xv[4], const double yv[4],
+                    const struct QED_kernel_temps t, double kerv[6][4][4][4]);
+
+/* Replace the composite kernels of src/LIBFILES/all_kernels.c, con_kernel.c,
+   sub_kernel.c, SYMXY.c and SYMXY0.c (declared in src/HEADERS/all_kernels.h,
+   con_kernel.h, sub_kernel.h, SYMXY.h, SYMXY0.h): the same combinations of
+   L0 at derived arguments, evaluated on the GPU (kqed_composite_batch below
+   is the batched form).  Outputs fully overwritten; on an error a message
+   goes to stderr and the output is zero. */
+void compute_all_kernels(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                         struct QED_Kernels *K);
+void compute_all_Mkernels(const double M[4], const double xv[4], const double yv[4],
+                          const struct QED_kernel_temps t, struct QED_Kernels *K);
+void compute_all_Mkernels_v2(const double M[4], const double xv[4], const double yv[4],
+                             const struct QED_kernel_temps t, struct QED_Kernels *K);
+void compute_con_kernels(const double xv[4], const double yv[4], const struct QED_kernel_temps t,
+                         struct QED_Kernels *K);
+void compute_con_kernels_v2(const double xv[4], const double yv[4],
+                            const struct QED_kernel_temps t, struct Kernels *K);
+void compute_con_kernelsM_L2(const double M[4], const double xv[4], const double yv[4],
+                             const struct QED_kernel_temps t, struct Kernels *K);
+void compute_sub_kernelsM_L2(const double M[4], const double xv[4], const double yv[4],
+                             const struct QED_kernel_temps t, struct Kernels *K);
+void compute_all_kernels_SYMXY(const double xv[4], const double yv[4],
+                               const struct QED_kernel_temps t, struct QED_Kernels *K);
+void compute_all_kernels_SYMXY_v2(const double xv[4], const double yv[4],
+                                  const struct QED_kernel_temps t, struct Kernels *K);
+void compute_all_kernels_SYMXY0(const double xv[4], const double yv[4],
+                                const struct QED_kernel_temps t, struct QED_Kernels *K);
+void compute_all_kernels_SYMXY0_v2(const double xv[4], const double yv[4],
+                                   const struct QED_kernel_temps t, struct Kernels *K);
+/* host helpers of the same files: K = (K + W)/2 (all_kernels.c:19-82,
+   con_kernel.c:14-59, over K[0..2]) and mu <-> nu on every L<i>.yx
+   (all_kernels.c:373-406) */
+void average_all_kernels(struct Kernels *K, const struct Kernels W);
+void average_all_QED_kernels(struct QED_Kernels *K, const struct QED_Kernels W);
+void average_con_kernels(struct Kernels *K, const struct Kernels *W);
+void swap_munu_Lyx(struct QED_Kernels *K);
+
 /* ------------------------------------------------------------------------
  * Part 2: batched and fused entry points (no counterpart in the reference's
  * library; they replace the caller-side loop of src/amu_forlattice.c:1419-1429
@@ -122,6 +189,52 @@ int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, size_t n, c
 int kqed_kernel_batch_dev(const struct QED_kernel_temps *t, int variant, size_t n,
                           const double *d_x, const double *d_y, double *d_kerv,
                           uint8_t *d_status, int precision, void *stream);
+
+/* The composite kernels, batched.  Numbering and per-pair output (the
+   reference's struct, in its memory layout):
+     KQED_ALL_KERNELS      compute_all_kernels            struct QED_Kernels
+     KQED_ALL_MKERNELS     compute_all_Mkernels (M[4])    struct QED_Kernels
+     KQED_ALL_MKERNELS_V2  compute_all_Mkernels_v2 (M[4]) struct QED_Kernels
+     KQED_CON_KERNELS      compute_con_kernels            struct QED_Kernels
+     KQED_CON_KERNELS_V2   compute_con_kernels_v2         struct Kernels[3]
+     KQED_CON_KERNELSM_L2  compute_con_kernelsM_L2 (M[4]) struct Kernels[3]
+     KQED_SUB_KERNELSM_L2  compute_sub_kernelsM_L2 (M[4]) struct Kernels[3]
+     KQED_SYMXY            compute_all_kernels_SYMXY      struct QED_Kernels
+     KQED_SYMXY_V2         compute_all_kernels_SYMXY_v2   struct Kernels
+     KQED_SYMXY0           compute_all_kernels_SYMXY0     struct QED_Kernels
+     KQED_SYMXY0_V2        compute_all_kernels_SYMXY0_v2  struct Kernels
+     KQED_MKERNEL_L2       QED_Mkernel_L2 (M[0])          double[6][4][4][4] */
+enum kqed_composite {
+  KQED_ALL_KERNELS = 0,
+  KQED_ALL_MKERNELS = 1,
+  KQED_ALL_MKERNELS_V2 = 2,
+  KQED_CON_KERNELS = 3,
+  KQED_CON_KERNELS_V2 = 4,
+  KQED_CON_KERNELSM_L2 = 5,
+  KQED_SUB_KERNELSM_L2 = 6,
+  KQED_SYMXY = 7,
+  KQED_SYMXY_V2 = 8,
+  KQED_SYMXY0 = 9,
+  KQED_SYMXY0_V2 = 10,
+  KQED_MKERNEL_L2 = 11,
+  KQED_COMPOSITE_COUNT = 12
+};
+
+/* doubles per pair of a composite's output (0 for an unknown one) */
+size_t kqed_composite_size(int which);
+
+/* out[i][kqed_composite_size(which)] = composite `which` at (x[i], y[i]) for
+   i < n.  M: host pointer to the masses (4 doubles; 1 for
+   KQED_MKERNEL_L2), NULL for the forms without masses.  precision:
+   KQED_FP64 or KQED_FP32_MIXED (the form of the L0 evaluations; the
+   combinations are FP64).  Host buffers. */
+int kqed_composite_batch(const struct QED_kernel_temps *t, int which, const double *M, size_t n,
+                         const double *x, const double *y, double *out, int precision);
+
+/* Same with device pointers (M stays a host pointer), enqueued on `stream`. */
+int kqed_composite_batch_dev(const struct QED_kernel_temps *t, int which, const double *M,
+                             size_t n, const double *d_x, const double *d_y, double *d_out,
+                             int precision, void *stream);
 
 /* Fused lattice integrand.  For each of nx points x_k and all ny sites y_n:
      sums[k] = sum_n sum_c L<variant>_c(x_k, y_n) * pi[k][n][c]

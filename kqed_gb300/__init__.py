@@ -20,6 +20,16 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libkqed_gb300.so")
 
 KQED_FP64, KQED_FP32_MIXED, KQED_SURROGATE = 0, 1, 2
+
+# enum kqed_composite: the reference's composite kernels, by their function names
+COMPOSITE_FUNCS = ["compute_all_kernels", "compute_all_Mkernels", "compute_all_Mkernels_v2",
+                   "compute_con_kernels", "compute_con_kernels_v2", "compute_con_kernelsM_L2",
+                   "compute_sub_kernelsM_L2", "compute_all_kernels_SYMXY",
+                   "compute_all_kernels_SYMXY_v2", "compute_all_kernels_SYMXY0",
+                   "compute_all_kernels_SYMXY0_v2"]
+KQED_MKERNEL_L2 = 11
+_COMPOSITE_WITH_M = ("compute_all_Mkernels", "compute_all_Mkernels_v2",
+                     "compute_con_kernelsM_L2", "compute_sub_kernelsM_L2")
 ST_OUT_OF_GRID, ST_TAYLOR_X, ST_SWAP, ST_AXIS = 1, 2, 4, 8
 
 
@@ -180,6 +190,22 @@ def lib():
         L.kqed_mlp_forward_backward.restype = ctypes.c_int
         L.kqed_mlp_infer.argtypes = [fp, ctypes.c_size_t, fp, fp]
         L.kqed_mlp_infer.restype = ctypes.c_int
+        L.kqed_composite_size.argtypes = [ctypes.c_int]
+        L.kqed_composite_size.restype = ctypes.c_size_t
+        L.kqed_composite_batch.argtypes = [T, ctypes.c_int, dp, ctypes.c_size_t, dp, dp, dp,
+                                           ctypes.c_int]
+        L.kqed_composite_batch.restype = ctypes.c_int
+        L.kqed_composite_batch_dev.argtypes = [T, ctypes.c_int, dp, ctypes.c_size_t,
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_int, ctypes.c_void_p]
+        L.kqed_composite_batch_dev.restype = ctypes.c_int
+        for name in COMPOSITE_FUNCS:
+            f = getattr(L, name)
+            f.argtypes = ([dp] if name in _COMPOSITE_WITH_M else []) + [dp, dp, QED_kernel_temps,
+                                                                        dp]
+            f.restype = None
+        L.QED_Mkernel_L2.argtypes = [ctypes.c_double, dp, dp, QED_kernel_temps, dp]
+        L.QED_Mkernel_L2.restype = None
         L.kqed_fp32_peak_gflops.argtypes = [dp]
         L.kqed_fp32_peak_gflops.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
@@ -292,6 +318,59 @@ def kernel_batch_dev(t, variant, x_ptr, y_ptr, out_ptr, n, precision=KQED_FP64, 
     """Device-pointer form (e.g. torch tensor .data_ptr()); enqueued on stream."""
     _check(lib().kqed_kernel_batch_dev(t.ptr, variant, n, x_ptr, y_ptr, out_ptr, status_ptr,
                                        precision, stream))
+
+
+def composite_size(which):
+    """doubles per pair of composite `which` (enum kqed_composite)"""
+    return lib().kqed_composite_size(which)
+
+
+def _masses(M):
+    if M is None:
+        return None
+    return np.ascontiguousarray(np.atleast_1d(M), dtype=np.float64)
+
+
+def composite_batch(t, which, x, y, M=None, precision=KQED_FP64):
+    """Composite kernel `which` (enum kqed_composite) at every pair: returns
+    [n][composite_size(which)] in the reference's struct layout.  M: the four
+    masses of the M-subtracted forms (one for QED_Mkernel_L2)."""
+    x, y = _pairs(x), _pairs(y)
+    if x.shape != y.shape:
+        raise ValueError("x and y must have the same number of pairs")
+    n = x.shape[0]
+    out = np.empty((n, composite_size(which)))
+    Mv = _masses(M)
+    _check(lib().kqed_composite_batch(t.ptr, which, None if Mv is None else _dptr(Mv), n,
+                                      _dptr(x), _dptr(y), _dptr(out), precision))
+    return out
+
+
+def composite_batch_dev(t, which, x_ptr, y_ptr, out_ptr, n, M=None, precision=KQED_FP64,
+                        stream=None):
+    """Device-pointer form of composite_batch, enqueued on stream."""
+    Mv = _masses(M)
+    _check(lib().kqed_composite_batch_dev(t.ptr, which, None if Mv is None else _dptr(Mv), n,
+                                          x_ptr, y_ptr, out_ptr, precision, stream))
+
+
+def composite_call(name, x, y, t, M=None):
+    """One pair through the reference-signature function `name` (e.g.
+    "compute_con_kernelsM_L2", "QED_Mkernel_L2"); returns its output struct
+    as a flat array."""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(4)
+    y = np.ascontiguousarray(y, dtype=np.float64).reshape(4)
+    which = KQED_MKERNEL_L2 if name == "QED_Mkernel_L2" else COMPOSITE_FUNCS.index(name)
+    out = np.zeros(composite_size(which))
+    f = getattr(lib(), name)
+    if name == "QED_Mkernel_L2":
+        f(float(M), _dptr(x), _dptr(y), t.t, _dptr(out))
+    elif name in _COMPOSITE_WITH_M:
+        Mv = _masses(M)
+        f(_dptr(Mv), _dptr(x), _dptr(y), t.t, _dptr(out))
+    else:
+        f(_dptr(x), _dptr(y), t.t, _dptr(out))
+    return out
 
 
 def lattice_sum(t, variant, x, ysites, pi, precision=KQED_FP64):

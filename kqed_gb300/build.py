@@ -80,11 +80,12 @@ def build_lib(verbose=False):
     cu3 = os.path.join(CSRC, "kqed_mlp_gemm.cu")
     cu4 = os.path.join(CSRC, "kqed_mlp.cu")
     cu5 = os.path.join(CSRC, "kqed_mlp_infer.cu")
+    cu6 = os.path.join(CSRC, "kqed_composite.cu")
     host = os.path.join(CSRC, "kqed_host.cpp")
     crc = os.path.join(CSRC, "kqed_crc32c.c")
     hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
     hdrs.append(os.path.join(ROOT, "include", "kqed.h"))
-    srcs = [f for f in (cu, cu2, cu3, cu4, cu5, host, crc) if os.path.exists(f)]
+    srcs = [f for f in (cu, cu2, cu3, cu4, cu5, cu6, host, crc) if os.path.exists(f)]
     if _newer(so, srcs + hdrs):
         return so
     lib_default = '-DKQED_DEFAULT_LIB_PATH="%s"' % HERE
@@ -95,6 +96,7 @@ def build_lib(verbose=False):
     o_cu3 = os.path.join(OUT, "kqed_mlp_gemm.o")
     o_cu4 = os.path.join(OUT, "kqed_mlp.o")
     o_cu5 = os.path.join(OUT, "kqed_mlp_infer.o")
+    o_cu6 = os.path.join(OUT, "kqed_composite.o")
     jobs = [
         [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v" if verbose else "-O3", "-c", cu, "-o", o_cu],
@@ -107,7 +109,7 @@ def build_lib(verbose=False):
                          "-o", o_cu3],
     ]
     objs = [o_cu, o_cu2, o_cu3]
-    for src, obj in ((cu4, o_cu4), (cu5, o_cu5)):
+    for src, obj in ((cu4, o_cu4), (cu5, o_cu5), (cu6, o_cu6)):
         if os.path.exists(src):
             jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                                          "-c", src, "-o", obj])

@@ -185,7 +185,7 @@ struct ThreadStage {
   cudaStream_t stream = nullptr, copy_stream = nullptr;
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double *h_pin = nullptr;   /* 8 + 384 doubles */
-  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32, d_rec, d_sa, d_sb;
+  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32, d_rec, d_sa, d_sb, d_cmp, d_cmp_io;
   ~ThreadStage() { reset(); }
   void reset()
   {
@@ -199,7 +199,7 @@ struct ThreadStage {
     copy_stream = nullptr;
     if (h_pin) cudaFreeHost(h_pin);
     d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release(); d_col.release(); d_col32.release();
-    d_rec.release(); d_sa.release(); d_sb.release();
+    d_rec.release(); d_sa.release(); d_sb.release(); d_cmp.release(); d_cmp_io.release();
     stream = nullptr;
     h_pin = nullptr;
     owner = 0;
@@ -1146,6 +1146,35 @@ int set_error(const char *msg)
 {
   tl_err = msg;
   return 1;
+}
+
+int l0_pairs(const struct QED_kernel_temps *t, const double *dx, const double *dy, size_t n,
+             double *dout, int precision, cudaStream_t s)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return fail("tables not initialised");
+  if (check_variant_precision(0, precision)) return 1;
+  tl_precision = precision;
+  const int rc = run_l0(c, dx, dy, n, dout, nullptr, s, true);
+  tl_precision = KQED_FP64;
+  return rc;
+}
+
+double *stage_scratch(const struct QED_kernel_temps *t, int slot, size_t n)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return nullptr;
+  ThreadStage &st = stage_for(c);
+  return slot == 0 ? st.d_cmp.get(n) : st.d_cmp_io.get(n);
+}
+
+cudaStream_t stage_stream(const struct QED_kernel_temps *t)
+{
+  Ctx *c = ctx_of(t);
+  if (!c) return nullptr;
+  ThreadStage &st = stage_for(c);
+  if (!st.stream) cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking);
+  return st.stream;
 }
 
 } // namespace kqed

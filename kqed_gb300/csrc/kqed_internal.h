@@ -212,6 +212,15 @@ extern std::atomic<uint64_t> g_launches;
 int ctx_handles(const struct QED_kernel_temps *t, DevTables *T, DevMaps *M, LaunchCfg *cfg);
 /* record an error message for kqed_last_error(); returns 1 */
 int set_error(const char *msg);
+/* L0 over n device pairs, dout[n][384], in the given form (KQED_FP64 or
+   KQED_FP32_MIXED), enqueued on s */
+int l0_pairs(const struct QED_kernel_temps *t, const double *dx, const double *dy, size_t n,
+             double *dout, int precision, cudaStream_t s);
+/* the calling thread's device scratch (slot 0 or 1) of n doubles for this
+   context, grown on demand; NULL on failure */
+double *stage_scratch(const struct QED_kernel_temps *t, int slot, size_t n);
+/* the calling thread's staging stream for this context */
+cudaStream_t stage_stream(const struct QED_kernel_temps *t);
 
 } // namespace kqed
 

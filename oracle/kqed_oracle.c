@@ -1175,6 +1175,15 @@ int oracle_kernel(int variant, long n, const double *x, const double *y, double 
   return 0;
 }
 
+/* one L0 evaluation for the composite-kernel restatements
+   (kqed_composite_oracle.c) */
+int oracle_L0_one(const double xv[4], const double yv[4], double *out)
+{
+  if (!G_ready) return 1;
+  L0(xv, yv, out);
+  return 0;
+}
+
 int oracle_contract(int variant, long n, const double *x, const double *y, const double *pi,
                     double *dots, int nthreads)
 {

@@ -31,6 +31,21 @@ int oracle_grid(int *nstpx, int *nstpy, double *xlo, double *xhi, double *ylo, d
 int oracle_kernel(int variant, long n, const double *x, const double *y, double *out,
                   int nthreads);
 
+/* out[384] = QED_kernel_L0(xv, yv); 0 on success */
+int oracle_L0_one(const double xv[4], const double yv[4], double *out);
+
+/* The reference's composite kernels (src/LIBFILES/all_kernels.c,
+   con_kernel.c, sub_kernel.c, SYMXY.c, SYMXY0.c, kernels.c:181-231),
+   restated in kqed_composite_oracle.c.  `which` numbers them as enum
+   kqed_composite of the library's C ABI; out[n][oracle_composite_size(which)]
+   holds each pair's output struct (struct Kernels, struct QED_Kernels,
+   struct Kernels[3] or one kernel) in the reference's memory layout.  M:
+   the four masses of the M-subtracted forms, M[0] alone for QED_Mkernel_L2,
+   ignored otherwise. */
+long oracle_composite_size(int which);
+int oracle_composite(int which, const double *M, long n, const double *x, const double *y,
+                     double *out, int nthreads);
+
 /* dots[i] = sum_c L<variant>_c(x[i],y[i]) * pi[i][c] */
 int oracle_contract(int variant, long n, const double *x, const double *y, const double *pi,
                     double *dots, int nthreads);

@@ -115,3 +115,50 @@ int ref_contract(int variant, long n, const double *x, const double *y,
   }
   return 0;
 }
+
+/* The reference's composite kernels (src/LIBFILES/all_kernels.c,
+   con_kernel.c, sub_kernel.c, SYMXY.c, SYMXY0.c, kernels.c:181-231) over n
+   pairs, each pair's output struct copied to out[i][size]; `which` numbers
+   them as the oracle does (oracle_composite). */
+long ref_composite_size(int which)
+{
+  switch (which) {
+  case 0: case 1: case 2: case 3: case 7: case 9: return 3072;
+  case 4: case 5: case 6: return 4608;
+  case 8: case 10: return 1536;
+  case 11: return 384;
+  default: return 0;
+  }
+}
+
+int ref_composite(int which, const double *M, long n, const double *x, const double *y,
+                  double *out, int nthreads)
+{
+  const long sz = ref_composite_size(which);
+  if (!T_ready || sz == 0) return 1;
+  if (nthreads <= 0 || nthreads > T_threads) nthreads = T_threads;
+  long i;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4)
+  for (i = 0; i < n; i++) {
+    const double *xv = x + 4 * i, *yv = y + 4 * i;
+    double *o = out + sz * i;
+    struct QED_Kernels Q;
+    struct Kernels K[3];
+    double kerv[6][4][4][4] KQED_ALIGN;
+    switch (which) {
+    case 0: compute_all_kernels(xv, yv, T, &Q); memcpy(o, &Q, sizeof(Q)); break;
+    case 1: compute_all_Mkernels(M, xv, yv, T, &Q); memcpy(o, &Q, sizeof(Q)); break;
+    case 2: compute_all_Mkernels_v2(M, xv, yv, T, &Q); memcpy(o, &Q, sizeof(Q)); break;
+    case 3: compute_con_kernels(xv, yv, T, &Q); memcpy(o, &Q, sizeof(Q)); break;
+    case 4: compute_con_kernels_v2(xv, yv, T, K); memcpy(o, K, sizeof(K)); break;
+    case 5: compute_con_kernelsM_L2(M, xv, yv, T, K); memcpy(o, K, sizeof(K)); break;
+    case 6: compute_sub_kernelsM_L2(M, xv, yv, T, K); memcpy(o, K, sizeof(K)); break;
+    case 7: compute_all_kernels_SYMXY(xv, yv, T, &Q); memcpy(o, &Q, sizeof(Q)); break;
+    case 8: compute_all_kernels_SYMXY_v2(xv, yv, T, K); memcpy(o, K, sizeof(K[0])); break;
+    case 9: compute_all_kernels_SYMXY0(xv, yv, T, &Q); memcpy(o, &Q, sizeof(Q)); break;
+    case 10: compute_all_kernels_SYMXY0_v2(xv, yv, T, K); memcpy(o, K, sizeof(K[0])); break;
+    case 11: QED_Mkernel_L2(M[0], xv, yv, T, kerv); memcpy(o, kerv, sizeof(kerv)); break;
+    }
+  }
+  return 0;
+}

@@ -11,7 +11,10 @@ reference sources exist; the fixtures travel, the reference does not).
    form-factor table, for seeded pairs covering every branch, plus the table's
    checksums so a test can confirm the same table is in use.
 
-Usage: python tests/golden/make_golden.py   (needs `make -C oracle ref`)
+3. ref_composite.npz -- the reference's composite kernels on seeded pairs.
+
+Usage: python tests/golden/make_golden.py [axis] [synth] [composite]
+       (default: all three; needs `make -C oracle ref`)
 """
 import ctypes
 import os
@@ -106,9 +109,49 @@ def ref_synth():
     np.savez_compressed(os.path.join(HERE, "ref_synth.npz"), x=x, y=y, table_cksum=ck, **out)
 
 
+def ref_composite():
+    """3. ref_composite.npz -- the reference's composite kernels
+    (src/LIBFILES/all_kernels.c, con_kernel.c, sub_kernel.c, SYMXY.c,
+    SYMXY0.c, kernels.c:181-231) through the same library, two of the
+    composite_pairs() per composite, with each pair's term scale (the largest
+    |L0| the composite combines, from the reference's own L0)."""
+    from _helpers import (COMPOSITE_SIZE, composite_masses, composite_pairs,  # noqa: E402
+                          composite_scale)
+    os.environ["KQEDREF_PATH"] = os.path.join(ROOT, "kqed_gb300")
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libkqedref_scalar.so"))
+    assert lib.ref_init() == 0, "reference initialise() failed"
+    dp = ctypes.POINTER(ctypes.c_double)
+
+    def ref_l0(a, b):
+        a = np.ascontiguousarray(a)
+        b = np.ascontiguousarray(b)
+        o = np.zeros((len(a), 384))
+        lib.ref_kernel(0, len(a), a.ctypes.data_as(dp), b.ctypes.data_as(dp),
+                       o.ctypes.data_as(dp), 1)
+        return o
+
+    px, py = composite_pairs()
+    out = {}
+    for w in range(len(COMPOSITE_SIZE)):
+        sel = [w % len(px), (w + 3) % len(px)]
+        x, y = np.ascontiguousarray(px[sel]), np.ascontiguousarray(py[sel])
+        M = composite_masses(w)
+        o = np.zeros((2, COMPOSITE_SIZE[w]))
+        assert lib.ref_composite(w, M.ctypes.data_as(dp), 2, x.ctypes.data_as(dp),
+                                 y.ctypes.data_as(dp), o.ctypes.data_as(dp), 1) == 0
+        out["x%d" % w], out["y%d" % w], out["out%d" % w] = x, y, o
+        out["scale%d" % w] = composite_scale(w, x, y, ref_l0)
+    np.savez_compressed(os.path.join(HERE, "ref_composite.npz"), **out)
+
+
 if __name__ == "__main__":
     if not os.path.isdir(REF):
         sys.exit("reference sources not found at %s" % REF)
-    reg_axis()
-    ref_synth()
+    parts = sys.argv[1:] or ["axis", "synth", "composite"]
+    if "axis" in parts:
+        reg_axis()
+    if "synth" in parts:
+        ref_synth()
+    if "composite" in parts:
+        ref_composite()
     print("wrote", os.listdir(HERE))
