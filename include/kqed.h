@@ -78,6 +78,19 @@ int initialize_QED_kernel_temps(struct QED_kernel_temps *t);
 /* Replaces free_QED_temps(), src/LIBFILES/init.c:38 (src/HEADERS/init.h:4). */
 void free_QED_temps(struct QED_kernel_temps *t);
 
+/* Replace the table readers and writers of src/LIBFILES/io.c:42-412
+   (src/HEADERS/io.h:4-20).  The readers fill the Grid fields from
+   LIB_PATH/PRECOMP with checksum validation (0 on success, 1 with a message
+   on stderr); initialise() calls the same code.  The writers produce the
+   same checksummed files under ./PRECOMP of the working directory:
+   FFxy_single_cksum2.bin, taylorx_cksum.bin, taylory_cksum.bin. */
+int read_ff(struct Grid_coeffs *Grid);
+int read_TAYLORX(struct Grid_coeffs *Grid);
+int read_TAYLORY(struct Grid_coeffs *Grid);
+void write_ff(const struct Grid_coeffs *Grid);
+void write_TAYLORX(const struct Grid_coeffs *Grid);
+void write_TAYLORY(const struct Grid_coeffs *Grid);
+
 /* Replace QED_kernel_L0..L3, src/LIBFILES/kernels.c:81-177
    (src/HEADERS/kernels.h:4-33).  kerv is fully overwritten; a pair outside
    the tabulated grid gives an all-zero kernel, as in the reference.

@@ -66,12 +66,18 @@ constexpr Perm NLM{1, 2, 0}; /* [nu][la][mu] */
 
 /* coef * S[perm]                                  (g == G1), or
    (coef * e_g[mass]) * (S[perm] - (M[mass] * u[o[uslot]]) * pf),
-   pf = sum_alpha w[alpha] S[perm with source position wpos = alpha] */
+   pf = sum_alpha w[alpha] S[perm with source position wpos = alpha]; pf
+   comes from contraction table ct (one per distinct (src, wpos, w)) */
 struct CTerm {
   uint8_t src, p0, p1, p2;
-  int8_t g, mass, u, uslot, w, wpos;
-  int16_t pad;
+  int8_t g, mass, u, uslot, w, wpos, ct;
+  int8_t pad;
   double coef;
+};
+/* contraction table: T[rs][a][b] = sum_alpha w[alpha] S_src[rs][..alpha..]
+   with alpha at source position wpos and (a, b) the other two positions */
+struct CCon {
+  int8_t src, wpos, w, pad;
 };
 struct CSlot {
   uint16_t first, count;
@@ -80,12 +86,14 @@ struct CSlot {
   double div;  /* 1: none */
 };
 
-constexpr int kMaxSrc = 12, kMaxSlot = 24, kMaxTerm = 112, kComp = 384;
+constexpr int kMaxSrc = 12, kMaxSlot = 24, kMaxTerm = 112, kMaxCon = 8, kComp = 384;
+constexpr int kConLen = 96; /* 6 x 4 x 4 */
 
 struct CProgram {
-  int nsrc, nslot, nout;
+  int nsrc, nslot, nout, ncon, nterm;
   int8_t a[kMaxSrc], b[kMaxSrc];
   double M[4];
+  CCon con[kMaxCon];
   CSlot slot[kMaxSlot];
   CTerm term[kMaxTerm];
 };
@@ -113,10 +121,22 @@ struct PB {
     s.count = (uint16_t)ts.size();
     s.out = (int16_t)out;
     s.div = div;
-    for (const CTerm &t : ts) {
+    for (CTerm t : ts) {
       if (t.src >= p.nsrc + p.nslot) bad = true; /* only earlier slots */
+      if (t.g != 0) {
+        int c = 0;
+        while (c < p.ncon && !(p.con[c].src == t.src && p.con[c].wpos == t.wpos &&
+                               p.con[c].w == t.w))
+          c++;
+        if (c == p.ncon) {
+          if (p.ncon >= kMaxCon) { bad = true; c = 0; }
+          else p.con[p.ncon++] = CCon{(int8_t)t.src, t.wpos, t.w, 0};
+        }
+        t.ct = (int8_t)c;
+      }
       p.term[nterm++] = t;
     }
+    p.nterm = nterm;
     if (out >= 0) p.nout = std::max(p.nout, out + 1);
     return p.nsrc + p.nslot++;
   }
@@ -402,7 +422,11 @@ __global__ void derive_kernel(const __grid_constant__ CProgram P, const double *
 __device__ __forceinline__ int lorentz(int opack, int k) { return (opack >> (2 * k)) & 3; }
 
 /* one block per pair, one thread per component; S = the pair's sources and
-   slots in shared memory, [nsrc + nslot][384] */
+   slots in shared memory, [nsrc + nslot][384], then the contraction tables
+   [ncon][96].  Per pair, once: the Gaussian factors, M[mass] * u[i] and
+   coef * e_g[mass] of every Gaussian term, and every contraction table, so
+   that a Gaussian term costs each component one product, one difference,
+   one product and the sum (the reference's order of operations). */
 __global__ void __launch_bounds__(kComp) combine_kernel(const __grid_constant__ CProgram P,
                                                         const double *__restrict__ Tsrc, size_t n,
                                                         const double *__restrict__ x,
@@ -410,8 +434,11 @@ __global__ void __launch_bounds__(kComp) combine_kernel(const __grid_constant__ 
                                                         double *__restrict__ out)
 {
   extern __shared__ double S[];
-  __shared__ double vec[4][4];  /* VN, VX, VY, VXMY */
-  __shared__ double gau[4][4];  /* [Gau][mass] */
+  __shared__ double vec[4][4];      /* VN, VX, VY, VXMY */
+  __shared__ double gau[4][4];      /* [Gau][mass] */
+  __shared__ double mu[4][4][4];    /* [mass][Vec][i] = M[mass] * vec[Vec][i] */
+  __shared__ double cg[kMaxTerm];   /* coef * e_g[mass] of the Gaussian terms */
+  double *CT = S + (P.nsrc + P.nslot) * kComp;
   const size_t i = blockIdx.x;
   const int c = threadIdx.x;
   for (int j = 0; j < P.nsrc; j++) S[j * kComp + c] = Tsrc[((size_t)j * n + i) * kComp + c];
@@ -434,7 +461,26 @@ __global__ void __launch_bounds__(kComp) combine_kernel(const __grid_constant__ 
                                   __dmul_rn(v[3], v[3]));
       gau[g][m] = exp(__ddiv_rn(__dmul_rn(-P.M[m], sq), 2.0));
     }
+  } else if (c >= 64 && c < 128) {
+    const int k = c - 64, m = k >> 4, v = (k >> 2) & 3, e = k & 3;
+    mu[m][v][e] = __dmul_rn(P.M[m], vec[v][e]);
   }
+  /* contraction tables (sources only: they are complete after the first barrier) */
+  for (int e = c; e < P.ncon * kConLen; e += kComp) {
+    const CCon cc = P.con[e / kConLen];
+    const int r = e % kConLen, rs = r >> 4, a = (r >> 2) & 3, b = r & 3;
+    const int stride = cc.wpos == 0 ? 16 : (cc.wpos == 1 ? 4 : 1);
+    const int base = rs * 64 + (cc.wpos == 0 ? a * 4 + b : (cc.wpos == 1 ? a * 16 + b : a * 16 + b * 4));
+    const double *src = S + cc.src * kComp;
+    const double *w = vec[cc.w];
+    CT[e] = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(w[0], src[base]),
+                                          __dmul_rn(w[1], src[base + stride])),
+                                __dmul_rn(w[2], src[base + 2 * stride])),
+                      __dmul_rn(w[3], src[base + 3 * stride]));
+  }
+  __syncthreads();
+  if (c < P.nterm && P.term[c].g != G1)
+    cg[c] = __dmul_rn(P.term[c].coef, gau[P.term[c].g][P.term[c].mass]);
   __syncthreads();
   const int rs = c >> 6;
   const int opack = ((c >> 4) & 3) | (((c >> 2) & 3) << 2) | ((c & 3) << 4);
@@ -442,34 +488,32 @@ __global__ void __launch_bounds__(kComp) combine_kernel(const __grid_constant__ 
     const CSlot sl = P.slot[s];
     double acc = 0.0;
     for (int k = 0; k < sl.count; k++) {
-      const CTerm t = P.term[sl.first + k];
-      const double *src = S + t.src * kComp;
+      const int ti = sl.first + k;
+      const CTerm t = P.term[ti];
       const int i0 = lorentz(opack, t.p0), i1 = lorentz(opack, t.p1), i2 = lorentz(opack, t.p2);
-      const int sidx = rs * 64 + i0 * 16 + i1 * 4 + i2;
+      const double sv = S[t.src * kComp + rs * 64 + i0 * 16 + i1 * 4 + i2];
       double v;
       if (t.g == G1) {
-        v = __dmul_rn(t.coef, src[sidx]);
+        v = t.coef == 1.0 ? sv : (t.coef == -1.0 ? -sv : __dmul_rn(t.coef, sv));
       } else {
-        const int stride = t.wpos == 0 ? 16 : (t.wpos == 1 ? 4 : 1);
-        const int base = sidx - (t.wpos == 0 ? i0 : (t.wpos == 1 ? i1 : i2)) * stride;
-        const double *w = vec[t.w];
-        const double pf = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(w[0], src[base]),
-                                                        __dmul_rn(w[1], src[base + stride])),
-                                              __dmul_rn(w[2], src[base + 2 * stride])),
-                                    __dmul_rn(w[3], src[base + 3 * stride]));
-        const double mu = __dmul_rn(P.M[t.mass], vec[t.u][lorentz(opack, t.uslot)]);
-        v = __dmul_rn(__dmul_rn(t.coef, gau[t.g][t.mass]), __dsub_rn(src[sidx], __dmul_rn(mu, pf)));
+        const int ci = rs * 16 + (t.wpos == 0 ? i1 * 4 + i2 : (t.wpos == 1 ? i0 * 4 + i2 : i0 * 4 + i1));
+        const double pf = CT[t.ct * kConLen + ci];
+        v = __dmul_rn(cg[ti], __dsub_rn(sv, __dmul_rn(mu[t.mass][t.u][lorentz(opack, t.uslot)], pf)));
       }
       acc = __dadd_rn(acc, v);
     }
-    if (sl.div != 1.0) acc = __ddiv_rn(acc, sl.div);
+    if (sl.div == 2.0) acc = __dmul_rn(acc, 0.5);   /* exact */
+    else if (sl.div != 1.0) acc = __ddiv_rn(acc, sl.div);
     S[(P.nsrc + s) * kComp + c] = acc;
     if (sl.out >= 0) out[(i * P.nout + sl.out) * kComp + c] = acc;
     __syncthreads();
   }
 }
 
-size_t combine_smem(const CProgram &P) { return (size_t)(P.nsrc + P.nslot) * kComp * sizeof(double); }
+size_t combine_smem(const CProgram &P)
+{
+  return ((size_t)(P.nsrc + P.nslot) * kComp + (size_t)P.ncon * kConLen) * sizeof(double);
+}
 
 /* pairs per launch group: the sources of one group, nsrc * chunk * (8 + 384)
    doubles, stay at about 1.2 GB or less */
@@ -501,7 +545,8 @@ int composite_dev(const struct QED_kernel_temps *t, int which, const double *M, 
   /* the attribute is per function: set the largest any program needs, so
      that concurrent callers with different programs never lower it */
   if (cudaFuncSetAttribute(combine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)((kMaxSrc + kMaxSlot) * kComp * sizeof(double))) != cudaSuccess)
+                           (int)(((kMaxSrc + kMaxSlot) * kComp + kMaxCon * kConLen) *
+                                 sizeof(double))) != cudaSuccess)
     return set_error("composite kernels: shared memory attribute refused");
   const size_t osz = (size_t)P.nout * kComp;
   for (size_t p0 = 0; p0 < n; p0 += chunk) {

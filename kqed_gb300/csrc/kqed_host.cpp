@@ -339,6 +339,112 @@ bad:
   return fail("|IO| %s malformed or checksums do not match", path.c_str());
 }
 
+/* ------------------------------------------- table readers and writers */
+
+/* read_ff / read_TAYLORX / read_TAYLORY, src/LIBFILES/io.c:42-289
+   (src/HEADERS/io.h:4-11): fill the Grid fields from LIB_PATH/PRECOMP with
+   checksum validation; 0 on success, 1 with a message on failure */
+extern "C" int read_ff(struct Grid_coeffs *Grid)
+{
+  if (!Grid) return fail("null grid");
+  if (load_ff(lib_path(), Grid)) {
+    fprintf(stderr, "%s\n", tl_err.c_str());
+    return 1;
+  }
+  return 0;
+}
+
+extern "C" int read_TAYLORX(struct Grid_coeffs *Grid)
+{
+  if (!Grid) return fail("null grid");
+  if (load_taylor(lib_path(), "taylorx_cksum.bin", 23, 810, &Grid->TX, &Grid->NtayY, &Grid->NY_tay)) {
+    fprintf(stderr, "%s\n", tl_err.c_str());
+    return 1;
+  }
+  return 0;
+}
+
+extern "C" int read_TAYLORY(struct Grid_coeffs *Grid)
+{
+  if (!Grid) return fail("null grid");
+  if (load_taylor(lib_path(), "taylory_cksum.bin", 14, 100, &Grid->TY, &Grid->NtayX, &Grid->NX_tay)) {
+    fprintf(stderr, "%s\n", tl_err.c_str());
+    return 1;
+  }
+  return 0;
+}
+
+/* the checksummed table writers of src/LIBFILES/io.c:292-412: the same
+   layouts (magic 816968, counts, values, rank-rotated CRC32C pairs), the
+   same relative paths under ./PRECOMP (write_ff to FFxy_single_cksum2.bin,
+   so that the table in use is not overwritten) */
+static bool wr(FILE *f, const void *p, size_t sz, size_t n) { return fwrite(p, sz, n, f) == n; }
+
+extern "C" void write_ff(const struct Grid_coeffs *G)
+{
+  FILE *f = G ? fopen("./PRECOMP/FFxy_single_cksum2.bin", "wb") : nullptr;
+  if (!f) {
+    fprintf(stderr, "|IO| cannot write ./PRECOMP/FFxy_single_cksum2.bin\n");
+    return;
+  }
+  const int magic = 816968;
+  bool ok = wr(f, &magic, 4, 1);
+  uint32_t ck[2];
+  ck[0] = ck[1] = 0;
+  kqed_cksum_accum(&ck[0], &ck[1], 0, G->XX, sizeof(double) * G->nstpx);
+  ok = ok && wr(f, &G->nstpx, 4, 1) && wr(f, G->XX, 8, G->nstpx) && wr(f, ck, 4, 2);
+  ck[0] = ck[1] = 0;
+  kqed_cksum_accum(&ck[0], &ck[1], 0, G->YY, sizeof(double) * G->nstpy);
+  ok = ok && wr(f, &G->nstpy, 4, 1) && wr(f, G->YY, 8, G->nstpy) && wr(f, ck, 4, 2);
+  ok = ok && wr(f, &G->Nffa, 4, 1);
+  uint32_t ma = 0, mb = 0, pa = 0, pb = 0, rank = 0;
+  for (int ia = 0; ok && ia < G->Nffa; ia++) {
+    ok = wr(f, &G->nstpx, 4, 1);
+    for (int ix = 0; ok && ix < G->nstpx; ix++) {
+      const int nf = G->nfx[ix];
+      ok = wr(f, &G->nstpy, 4, 1);
+      for (int iy = 0; ok && iy < G->nstpy; iy++, rank++) {
+        const float *fm = G->Ffm[ia][ix][iy], *fp = G->Ffp[ia][ix][iy];
+        ok = wr(f, &nf, 4, 1) && wr(f, fm, 4, nf) && wr(f, fp, 4, nf);
+        kqed_cksum_accum(&ma, &mb, rank, fm, sizeof(float) * nf);
+        kqed_cksum_accum(&pa, &pb, rank, fp, sizeof(float) * nf);
+      }
+    }
+  }
+  const uint32_t tail[4] = {ma, mb, pa, pb};
+  ok = ok && wr(f, tail, 4, 4);
+  if (fclose(f) != 0 || !ok) fprintf(stderr, "|IO| write of FFxy_single_cksum2.bin failed\n");
+}
+
+static void write_taylor(const char *path, const char *what, int nrows, int ncols,
+                         double *const *rows)
+{
+  FILE *f = fopen(path, "wb");
+  if (!f) {
+    fprintf(stderr, "|IO| cannot write to file %s\n", what);
+    return;
+  }
+  const int magic = 816968;
+  bool ok = wr(f, &magic, 4, 1) && wr(f, &nrows, 4, 1);
+  uint32_t a = 0, b = 0;
+  for (int i = 0; ok && i < nrows; i++) {
+    ok = wr(f, &ncols, 4, 1) && wr(f, rows[i], 8, ncols);
+    kqed_cksum_accum(&a, &b, (uint32_t)i, rows[i], sizeof(double) * ncols);
+  }
+  ok = ok && wr(f, &a, 4, 1) && wr(f, &b, 4, 1);
+  if (fclose(f) != 0 || !ok) fprintf(stderr, "|IO| write of %s failed\n", path);
+}
+
+extern "C" void write_TAYLORX(const struct Grid_coeffs *G)
+{
+  if (G) write_taylor("./PRECOMP/taylorx_cksum.bin", "TAYLORX", G->NtayY, G->NY_tay, G->TX);
+}
+
+extern "C" void write_TAYLORY(const struct Grid_coeffs *G)
+{
+  if (G) write_taylor("./PRECOMP/taylory_cksum.bin", "TAYLORY", G->NtayX, G->NX_tay, G->TY);
+}
+
 /* the reference's per-call y-power scaling (getff2, src/LIBFILES/getff-new.c:103-152),
    applied once per node; out arrays are indexed by Chebyshev index U_K */
 static void scale_node(int nm, double y, int nf, const float *fm, const float *fp, double *fval,
