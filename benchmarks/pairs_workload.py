@@ -5,7 +5,7 @@
 Pairs: the 4160 pairs of workloads.config1_pairs (4096 with components
 U[-2,2], 64 with one side of norm 1e-6..1e-3), tiled `--repeat` times so
 that one launch keeps the GPU busy; device-resident inputs and outputs,
-timed with CUDA events.  Both precision forms, with the mixed form's
+timed with CUDA events, clocks sampled.  Both precision forms, with the mixed form's
 per-pair norm-relative error against the FP64 form.  Prints one JSON line.
 """
 import argparse
@@ -28,6 +28,7 @@ def main():
     import torch
 
     import kqed_gb300 as K
+    from benchmarks.clocks import ClockSampler
     from kqed_gb300.workloads import config1_pairs
     t = K.KernelTemps()
     x, y = config1_pairs()
@@ -43,6 +44,8 @@ def main():
         for _ in range(2):
             K.kernel_batch_dev(t, a.variant, dx.data_ptr(), dy.data_ptr(), o.data_ptr(), n, prec)
         torch.cuda.synchronize()
+        clk = ClockSampler(torch.cuda.current_device())
+        clk.start()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -52,7 +55,7 @@ def main():
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / a.steps
         res[name] = o
-        out[name] = {"ms_per_step": ms, "evals_per_s": n / (ms / 1e3)}
+        out[name] = {"ms_per_step": ms, "evals_per_s": n / (ms / 1e3), "clocks": clk.stop()}
     a64, a32 = res["fp64"], res["fp32_mixed"]
     nrm = a64.abs().max(1).values
     live = nrm > 0

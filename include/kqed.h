@@ -57,8 +57,9 @@ struct Grid_coeffs {
   int *nfx;
 };
 
-/* src/HEADERS/KQED.h:90-93.  G8 (the Dirac-trace table used only by the
-   reference's perturbative pion-loop code, not by the kernel) is left NULL. */
+/* src/HEADERS/KQED.h:90-93.  G8: the 65,536-entry Dirac-trace table of the
+   perturbative lepton-loop Pi-hat, filled by initialise() as the
+   reference's (init_g8) and freed by free_QED_temps(). */
 struct QED_kernel_temps {
   struct Grid_coeffs Grid;
   int *G8;
@@ -171,6 +172,24 @@ void average_all_QED_kernels(struct QED_Kernels *K, const struct QED_Kernels W);
 void average_con_kernels(struct Kernels *K, const struct Kernels *W);
 void swap_munu_Lyx(struct QED_Kernels *K);
 
+/* Replace the perturbative lepton-loop functions of src/LIBFILES/pi_pert.c
+   (src/HEADERS/pi_pert.h): the (rho, sigma)-antisymmetrised Pi-hat of a
+   free lepton loop, and the one-loop tensor it is built from, evaluated on
+   the GPU (kqed_pihat_batch below is the batched form); the Dirac traces,
+   the Bessel functions K_0..K_n and the analytic a_mu and vacuum-
+   polarisation results, on the host.  The analytic functions print nothing
+   (the reference prints its partial sums). */
+void ipihatFermLoop_antisym(const double x[4], const double y[4], const struct QED_kernel_temps t,
+                            double vpihat[6][4][4][4]);
+void pihat1(const double x[4], const double y[4], const struct QED_kernel_temps t,
+            double vpihat1[4][4][4][4][4], double vpihatr1[4][4][4][4]);
+void init_g8(struct QED_kernel_temps *t);
+int diractrace(const int n, const int *idx);
+void bessk(const int n, const double x, double *bv);
+double amu_heavlept(const double mh);
+double amu_lightlept(const double ml);
+double vac_pol(const double ml);
+
 /* ------------------------------------------------------------------------
  * Part 2: batched and fused entry points (no counterpart in the reference's
  * library; they replace the caller-side loop of src/amu_forlattice.c:1419-1429
@@ -248,6 +267,18 @@ int kqed_composite_batch(const struct QED_kernel_temps *t, int which, const doub
 int kqed_composite_batch_dev(const struct QED_kernel_temps *t, int which, const double *M,
                              size_t n, const double *d_x, const double *d_y, double *d_out,
                              int precision, void *stream);
+
+/* out[i][384] = ipihatFermLoop_antisym(x[i], y[i]) for i < n: host buffers,
+   or device buffers enqueued on `stream`. */
+int kqed_pihat_batch(size_t n, const double *x, const double *y, double *out);
+int kqed_pihat_batch_dev(size_t n, const double *d_x, const double *d_y, double *d_out,
+                         void *stream);
+/* d_pi[k][n][384] = ipihatFermLoop_antisym(scale x_k, scale y_n): the
+   perturbative Pi-hat of a lepton of mass `scale` (in units of the kernel's
+   mass) laid out as the fused lattice sums take it (the reference's
+   lepton-loop check, src/amu_forlattice.c:65-116, uses scale = 2). */
+int kqed_pihat_lattice_dev(size_t nx, const double *d_x, size_t ny, const double *d_y,
+                           double scale, double *d_pi, void *stream);
 
 /* Fused lattice integrand.  For each of nx points x_k and all ny sites y_n:
      sums[k] = sum_n sum_c L<variant>_c(x_k, y_n) * pi[k][n][c]

@@ -206,6 +206,19 @@ def lib():
             f.restype = None
         L.QED_Mkernel_L2.argtypes = [ctypes.c_double, dp, dp, QED_kernel_temps, dp]
         L.QED_Mkernel_L2.restype = None
+        L.kqed_pihat_batch.argtypes = [ctypes.c_size_t, dp, dp, dp]
+        L.kqed_pihat_batch.restype = ctypes.c_int
+        L.kqed_pihat_batch_dev.argtypes = [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p]
+        L.kqed_pihat_batch_dev.restype = ctypes.c_int
+        L.kqed_pihat_lattice_dev.argtypes = [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                             ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                                             ctypes.c_void_p]
+        L.kqed_pihat_lattice_dev.restype = ctypes.c_int
+        L.ipihatFermLoop_antisym.argtypes = [dp, dp, QED_kernel_temps, dp]
+        L.ipihatFermLoop_antisym.restype = None
+        L.pihat1.argtypes = [dp, dp, QED_kernel_temps, dp, dp]
+        L.pihat1.restype = None
         L.kqed_fp32_peak_gflops.argtypes = [dp]
         L.kqed_fp32_peak_gflops.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
@@ -371,6 +384,45 @@ def composite_call(name, x, y, t, M=None):
     else:
         f(_dptr(x), _dptr(y), t.t, _dptr(out))
     return out
+
+
+def pihat_batch(x, y):
+    """ipihatFermLoop_antisym(x[i], y[i]) for all i: [n][384] (the reference's
+    perturbative lepton-loop Pi-hat, src/LIBFILES/pi_pert.c)"""
+    x, y = _pairs(x), _pairs(y)
+    if x.shape != y.shape:
+        raise ValueError("x and y must have the same number of pairs")
+    out = np.empty((x.shape[0], 384))
+    _check(lib().kqed_pihat_batch(x.shape[0], _dptr(x), _dptr(y), _dptr(out)))
+    return out
+
+
+def pihat_batch_dev(x_ptr, y_ptr, out_ptr, n, stream=None):
+    _check(lib().kqed_pihat_batch_dev(n, x_ptr, y_ptr, out_ptr, stream))
+
+
+def pihat_lattice_dev(x_ptr, nx, y_ptr, ny, scale, pi_ptr, stream=None):
+    """pi[k][n][384] = Pi-hat(scale x_k, scale y_n), the fused sums' layout"""
+    _check(lib().kqed_pihat_lattice_dev(nx, x_ptr, ny, y_ptr, scale, pi_ptr, stream))
+
+
+def ipihatFermLoop_antisym(x, y, t):
+    """ipihatFermLoop_antisym, src/LIBFILES/pi_pert.c:162-198 (one pair)"""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(4)
+    y = np.ascontiguousarray(y, dtype=np.float64).reshape(4)
+    out = np.zeros((6, 4, 4, 4))
+    lib().ipihatFermLoop_antisym(_dptr(x), _dptr(y), t.t, _dptr(out))
+    return out
+
+
+def pihat1(x, y, t):
+    """pihat1, src/LIBFILES/pi_pert.c:236-389: (vpihat1[4][4][4][4][4], vpihatr1[4][4][4][4])"""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(4)
+    y = np.ascontiguousarray(y, dtype=np.float64).reshape(4)
+    p = np.zeros((4, 4, 4, 4, 4))
+    r = np.zeros((4, 4, 4, 4))
+    lib().pihat1(_dptr(x), _dptr(y), t.t, _dptr(p), _dptr(r))
+    return p, r
 
 
 def lattice_sum(t, variant, x, ysites, pi, precision=KQED_FP64):

@@ -81,11 +81,12 @@ def build_lib(verbose=False):
     cu4 = os.path.join(CSRC, "kqed_mlp.cu")
     cu5 = os.path.join(CSRC, "kqed_mlp_infer.cu")
     cu6 = os.path.join(CSRC, "kqed_composite.cu")
+    cu7 = os.path.join(CSRC, "kqed_pihat.cu")
     host = os.path.join(CSRC, "kqed_host.cpp")
     crc = os.path.join(CSRC, "kqed_crc32c.c")
     hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
     hdrs.append(os.path.join(ROOT, "include", "kqed.h"))
-    srcs = [f for f in (cu, cu2, cu3, cu4, cu5, cu6, host, crc) if os.path.exists(f)]
+    srcs = [f for f in (cu, cu2, cu3, cu4, cu5, cu6, cu7, host, crc) if os.path.exists(f)]
     if _newer(so, srcs + hdrs):
         return so
     lib_default = '-DKQED_DEFAULT_LIB_PATH="%s"' % HERE
@@ -97,6 +98,7 @@ def build_lib(verbose=False):
     o_cu4 = os.path.join(OUT, "kqed_mlp.o")
     o_cu5 = os.path.join(OUT, "kqed_mlp_infer.o")
     o_cu6 = os.path.join(OUT, "kqed_composite.o")
+    o_cu7 = os.path.join(OUT, "kqed_pihat.o")
     jobs = [
         [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v" if verbose else "-O3", "-c", cu, "-o", o_cu],
@@ -109,10 +111,14 @@ def build_lib(verbose=False):
                          "-o", o_cu3],
     ]
     objs = [o_cu, o_cu2, o_cu3]
-    for src, obj in ((cu4, o_cu4), (cu5, o_cu5), (cu6, o_cu6)):
+    # the perturbative Pi-hat keeps the reference's order of operations:
+    # no multiply-add contraction on the device or the host side
+    exact = ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]
+    for src, obj, extra in ((cu4, o_cu4, []), (cu5, o_cu5, []), (cu6, o_cu6, []),
+                            (cu7, o_cu7, exact)):
         if os.path.exists(src):
-            jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                                         "-c", src, "-o", obj])
+            jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"] +
+                        extra + ["-c", src, "-o", obj])
             objs.append(obj)
     with cf.ThreadPoolExecutor(len(jobs)) as ex:
         results = list(ex.map(_run, jobs))

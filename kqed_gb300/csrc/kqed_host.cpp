@@ -682,7 +682,10 @@ extern "C" int initialise(struct QED_kernel_temps *t)
   }
   G->PC = (struct AVX_precomps *)calloc(1, sizeof(struct AVX_precomps));
   G->PC->Fm = c;
-  t->G8 = nullptr;
+  /* the Dirac-trace table of the perturbative Pi-hat, as the reference's
+     initialise fills it (src/LIBFILES/init.c:149-150) */
+  t->G8 = (int *)malloc(65536 * sizeof(int));
+  if (t->G8) init_g8(t);
   return 0;
 }
 

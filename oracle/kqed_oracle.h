@@ -46,6 +46,13 @@ long oracle_composite_size(int which);
 int oracle_composite(int which, const double *M, long n, const double *x, const double *y,
                      double *out, int nthreads);
 
+/* The perturbative lepton-loop Pi-hat of the reference
+   (ipihatFermLoop_antisym, src/LIBFILES/pi_pert.c:162-198), restated in
+   kqed_pihat_oracle.c: out[n][6][4][4][4]; and the Dirac-trace table G8
+   (init_g8, pi_pert.c:140-160) into out[65536]. */
+int oracle_pihat(long n, const double *x, const double *y, double *out, int nthreads);
+int oracle_g8(int *out);
+
 /* dots[i] = sum_c L<variant>_c(x[i],y[i]) * pi[i][c] */
 int oracle_contract(int variant, long n, const double *x, const double *y, const double *pi,
                     double *dots, int nthreads);

@@ -162,3 +162,39 @@ int ref_composite(int which, const double *M, long n, const double *x, const dou
   }
   return 0;
 }
+
+/* the reference's perturbative Pi-hat, ipihatFermLoop_antisym
+   (src/LIBFILES/pi_pert.c:162-198), over n pairs: out[n][384] */
+int ref_pihat(long n, const double *x, const double *y, double *out, int nthreads)
+{
+  if (!T_ready) return 1;
+  if (nthreads <= 0 || nthreads > T_threads) nthreads = T_threads;
+  long i;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4)
+  for (i = 0; i < n; i++) {
+    double v[6][4][4][4];
+    ipihatFermLoop_antisym(x + 4 * i, y + 4 * i, T, v);
+    memcpy(out + 384 * i, v, sizeof(v));
+  }
+  return 0;
+}
+
+/* the reference's G8 table as initialise() filled it */
+int ref_g8(int *out)
+{
+  if (!T_ready || !T.G8) return 1;
+  memcpy(out, T.G8, 65536 * sizeof(int));
+  return 0;
+}
+
+/* the reference's one-loop tensor pihat1 (pi_pert.c:236-389) of one pair:
+   out[1024 + 256] = vpihat1 then vpihatr1 */
+int ref_pihat1(const double *x, const double *y, double *out)
+{
+  if (!T_ready) return 1;
+  double p[4][4][4][4][4], r[4][4][4][4];
+  pihat1(x, y, T, p, r);
+  memcpy(out, p, sizeof(p));
+  memcpy(out + 1024, r, sizeof(r));
+  return 0;
+}

@@ -181,3 +181,22 @@ def composite_pairs():
     y = np.array([g[1], [0.8, 0.45, -0.3, 0.75], [-0.9, 0.3, 1.0, 0.5], [0.6, -0.2, 0.4, 1.3],
                   np.zeros(4), [1.1, 0.2, -0.6, 0.4], [0.3, 0.15, -0.3, 0.6], [1.0, 1.0, 1.0, 1.0]])
     return x, y
+
+
+def oracle_pihat(x, y, nthreads=0):
+    """[n][384]: the oracle's ipihatFermLoop_antisym(x[i], y[i])"""
+    O = oracle()
+    O.oracle_pihat.argtypes = [ctypes.c_long, _dp, _dp, _dp, ctypes.c_int]
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.zeros((len(x), 384))
+    assert O.oracle_pihat(len(x), x.ctypes.data_as(_dp), y.ctypes.data_as(_dp),
+                          out.ctypes.data_as(_dp), nthreads) == 0
+    return out
+
+
+def oracle_g8():
+    O = oracle()
+    out = np.zeros(65536, dtype=np.int32)
+    O.oracle_g8(out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return out

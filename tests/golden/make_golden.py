@@ -12,8 +12,9 @@ reference sources exist; the fixtures travel, the reference does not).
    checksums so a test can confirm the same table is in use.
 
 3. ref_composite.npz -- the reference's composite kernels on seeded pairs.
+4. ref_pihat.npz -- the reference's perturbative lepton-loop Pi-hat.
 
-Usage: python tests/golden/make_golden.py [axis] [synth] [composite]
+Usage: python tests/golden/make_golden.py [axis] [synth] [composite] [pihat]
        (default: all three; needs `make -C oracle ref`)
 """
 import ctypes
@@ -144,14 +145,67 @@ def ref_composite():
     np.savez_compressed(os.path.join(HERE, "ref_composite.npz"), **out)
 
 
+def pihat_pairs():
+    """seeded pairs for the perturbative Pi-hat: generic, short and long
+    separations, and the reference's lepton-loop check points
+    (src/amu_forlattice.c:80-96, scaled by the mass ratio 2)"""
+    rng = np.random.default_rng(8080)
+    x = rng.uniform(-1.5, 1.5, (6, 4))
+    y = rng.uniform(-1.5, 1.5, (6, 4))
+    x[1] = 0.02 * x[1]
+    y[2] = x[2] + 0.01 * y[2]
+    pts = []
+    for xm, b, ym in ((0.405, 0.005 + np.pi / 4, 0.205), (0.805, 0.005 + np.pi / 2, 0.605)):
+        pts.append((2 * np.array([0, 0, xm * np.sin(b), xm * np.cos(b)]), 2 * np.array([0, 0, 0, ym])))
+    x = np.vstack([x] + [p[0][None] for p in pts])
+    y = np.vstack([y] + [p[1][None] for p in pts])
+    return x, y
+
+
+def ref_pihat():
+    """4. ref_pihat.npz -- the reference's perturbative lepton-loop Pi-hat
+    (ipihatFermLoop_antisym and pihat1, src/LIBFILES/pi_pert.c) and its
+    analytic functions, through the same library"""
+    os.environ["KQEDREF_PATH"] = os.path.join(ROOT, "kqed_gb300")
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libkqedref_scalar.so"))
+    assert lib.ref_init() == 0, "reference initialise() failed"
+    dp = ctypes.POINTER(ctypes.c_double)
+    x, y = pihat_pairs()
+    anti = np.zeros((len(x), 384))
+    assert lib.ref_pihat(len(x), x.ctypes.data_as(dp), y.ctypes.data_as(dp),
+                         anti.ctypes.data_as(dp), 1) == 0
+    raw = np.zeros((2, 1280))
+    for i in range(2):
+        xi, yi = np.ascontiguousarray(x[i]), np.ascontiguousarray(y[i])
+        assert lib.ref_pihat1(xi.ctypes.data_as(dp), yi.ctypes.data_as(dp),
+                              raw[i].ctypes.data_as(dp)) == 0
+    for f in ("amu_heavlept", "amu_lightlept", "vac_pol"):
+        getattr(lib, f).restype = ctypes.c_double
+        getattr(lib, f).argtypes = [ctypes.c_double]
+    args = np.array([0.5, 2.0, 1.0 / 206.768262, 16.8])
+    heav = np.array([lib.amu_heavlept(a) for a in args])
+    light = np.array([lib.amu_lightlept(a) for a in args])
+    vac = np.array([lib.vac_pol(a) for a in args])
+    bess = np.zeros((5, 6))
+    lib.bessk.argtypes = [ctypes.c_int, ctypes.c_double, dp]
+    bx = np.array([0.05, 0.7, 2.0, 2.5, 9.0])
+    for i, v in enumerate(bx):
+        lib.bessk(4, v, bess[i].ctypes.data_as(dp))
+    np.savez_compressed(os.path.join(HERE, "ref_pihat.npz"), x=x, y=y, pihat=anti, pihat1=raw,
+                        fn_args=args, amu_heavlept=heav, amu_lightlept=light, vac_pol=vac,
+                        bessk_x=bx, bessk=bess[:, :5])
+
+
 if __name__ == "__main__":
     if not os.path.isdir(REF):
         sys.exit("reference sources not found at %s" % REF)
-    parts = sys.argv[1:] or ["axis", "synth", "composite"]
+    parts = sys.argv[1:] or ["axis", "synth", "composite", "pihat"]
     if "axis" in parts:
         reg_axis()
     if "synth" in parts:
         ref_synth()
     if "composite" in parts:
         ref_composite()
+    if "pihat" in parts:
+        ref_pihat()
     print("wrote", os.listdir(HERE))
