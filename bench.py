@@ -53,6 +53,9 @@ def parse():
     p.add_argument("--variant", type=int, default=2)
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--strong", action="store_true",
+                   help="N > 1: one lattice, its sites split across the ranks "
+                        "(kqed_gb300/shard.py), per-x partial sums gathered and combined")
     return p.parse_args()
 
 
@@ -235,12 +238,27 @@ def run_gb300(args):
     g = t.grid()
     prec = {"fp64": K.KQED_FP64, "fp32": K.KQED_FP32_MIXED}[args.precision]
 
-    xs = diagonal_x(args.nx, args.spacing) * x_direction(rank)[None, :]
-    ys = lattice_sites(args.L, args.spacing)
+    if args.strong:
+        # strong scaling: every rank takes the same x points and its own slab
+        # of the lattice's sites; Pi is the library's generated Pi at the
+        # sites' global indices, so the combined sums do not depend on N
+        from kqed_gb300.shard import site_slab
+        xs = diagonal_x(args.nx, args.spacing)
+        ys_all = lattice_sites(args.L, args.spacing)
+        lo, hi = site_slab(len(ys_all), rank, world)
+        ys = ys_all[lo:hi]
+    else:
+        xs = diagonal_x(args.nx, args.spacing) * x_direction(rank)[None, :]
+        ys = lattice_sites(args.L, args.spacing)
     nx, ny = len(xs), len(ys)
     dx = torch.as_tensor(xs, dtype=torch.float64, device=dev)
     dy = torch.as_tensor(ys, dtype=torch.float64, device=dev)
-    pi = pi_synth_torch(xs, ys, seed=2 + rank, device=dev)
+    if args.strong:
+        pi = torch.empty((nx, ny, 384), dtype=torch.float64, device=dev)
+        K.pi_synth_dev(dx.data_ptr(), nx, dy.data_ptr(), ny, 7, pi.data_ptr(), y_offset=lo)
+        torch.cuda.synchronize(dev)
+    else:
+        pi = pi_synth_torch(xs, ys, seed=2 + rank, device=dev)
     sums = torch.empty(nx, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -282,7 +300,9 @@ def run_gb300(args):
         mt = torch.tensor([ms_step], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(mt, op=torch.distributed.ReduceOp.MAX)
         ms_step = float(mt.item())
-    value = world * nx * ny / (ms_step / 1e3)
+    # weak: every rank its own lattice; strong: the ranks' slabs make one lattice
+    total_pairs = nx * len(ys_all) if args.strong else world * nx * ny
+    value = total_pairs / (ms_step / 1e3)
 
     # ---- both precision forms on the same resident inputs: time and the
     #      mixed form's integrand error against the FP64 sums
@@ -301,7 +321,7 @@ def run_gb300(args):
         torch.cuda.synchronize(dev)
         fms = f0.elapsed_time(f1) / args.steps
         fsums[name] = sums.cpu().numpy().copy()
-        forms[name] = {"value": world * nx * ny / (fms / 1e3), "ms_per_step": fms}
+        forms[name] = {"value": total_pairs / (fms / 1e3), "ms_per_step": fms}
     ref = fsums["fp64"]
     err = np.abs(fsums["fp32_mixed"] - ref)
     rms = float(np.sqrt(np.mean(ref ** 2)))
@@ -337,7 +357,10 @@ def run_gb300(args):
 
     # ---- end to end through the host entry point (Pi from pinned memory)
     def measure_e2e(pi):
-        pi_host = torch.empty(pi.shape, dtype=torch.float64, pin_memory=True)
+        # the caller's Pi in page-locked memory from the library's allocator
+        # (cudaHostAlloc: the full host link rate)
+        pinned = K.PinnedArray(tuple(pi.shape))
+        pi_host = torch.from_numpy(pinned.array)
         pi_host.copy_(pi)
         xh = np.ascontiguousarray(xs)
         yh = np.ascontiguousarray(ys)
@@ -381,7 +404,7 @@ def run_gb300(args):
         torch.cuda.synchronize(dev)
         h2d_gbs = moved / (time.perf_counter() - c0) / 1e9
         del scratch
-        e2e = {"value": world * nx * ny / e2e_s, "unit": UNIT,
+        e2e = {"value": total_pairs / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(pi_host.numel() * 8 + xh.nbytes + yh.nbytes),
                "d2h_bytes_per_step": int(sh.nbytes),
                "precision": args.precision,
@@ -391,11 +414,12 @@ def run_gb300(args):
                "copy_ms_per_step": e2e_copy_ms / args.e2e_steps,
                "h2d_gbs_during_step": pi_host.numel() * 8 / (e2e_copy_ms / args.e2e_steps / 1e3) / 1e9
                if e2e_copy_ms > 0 else None,
-               "copy_bound_evals_per_s": world * nx * ny / (pi_host.numel() * 8 / (h2d_gbs * 1e9))}
-        return e2e, pi_host
+               "copy_bound_evals_per_s": total_pairs / (pi_host.numel() * 8 / (h2d_gbs * 1e9))}
+        return e2e, pi_host, pinned
 
+    pinned = None
     if args.e2e_steps > 0:
-        e2e, pi_host = measure_e2e(pi)
+        e2e, pi_host, pinned = measure_e2e(pi)
         del pi
         torch.cuda.empty_cache()
     else:
@@ -413,14 +437,27 @@ def run_gb300(args):
         parity = parity_of(fsums["fp64"], checked)
         parity["against"] = kind
 
+    # strong scaling: the per-x partial sums of the slabs, gathered and
+    # added in rank order (the only collective: nx doubles per rank)
+    if args.strong and world > 1:
+        from kqed_gb300.shard import combine_rank_order
+        mine = torch.as_tensor(fsums["fp64"], device=dev)
+        got = [torch.empty_like(mine) for _ in range(world)]
+        torch.distributed.all_gather(got, mine)
+        fsums["fp64"] = combine_rank_order([g.cpu().numpy() for g in got])
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "higher_is_better": True, "scaling": "strong" if args.strong else "weak",
+            "vs_baseline": None,
             "dtype": {"fp64": "f64 (double-float assembly)", "fp32": "f32+f64"}[args.precision],
             "data": "synthetic",
-            "config": workload_config(args, ny),
+            "config": workload_config(args, len(ys_all) if args.strong else ny) | (
+                {"parallelism": "sites sharded over %d ranks (kqed_gb300/shard.py); Pi "
+                                "generated by the library at global site indices (seed 7)" % world}
+                if args.strong else {}),
             "e2e": e2e,
             "forms": forms,
             "gpu_launches": launches,
@@ -444,6 +481,9 @@ def run_gb300(args):
             "checksum": [float(v) for v in fsums["fp64"][:4]],
         }
         print(json.dumps(line), flush=True)
+    pi_host = None
+    if pinned is not None:
+        pinned.free()
     t.free()
     if world > 1:
         torch.distributed.destroy_process_group()

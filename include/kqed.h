@@ -335,6 +335,22 @@ int kqed_pi_synth_dev(size_t nx, const double *d_x, size_t ny, const double *d_y
                       uint32_t stream_id, size_t x_offset, size_t y_offset, double *d_pi,
                       void *stream);
 
+/* Page-locked host memory (cudaHostAlloc) for the inputs of the host entry
+   points, e.g. the caller's Pi of kqed_lattice_sum: copies from it run at
+   the full host link rate.  Free with kqed_pinned_free. */
+int kqed_pinned_alloc(size_t bytes, void **ptr);
+int kqed_pinned_free(void *ptr);
+
+/* Multi-GPU sharding of a lattice sum, one process per GPU: rank `rank` of
+   `world` takes sites [*begin, *end) (contiguous slabs of whole 64-site
+   tiles) and evaluates them against all x -- kqed_lattice_sum_dev on its
+   slab of sites and Pi, or kqed_lattice_sum_synth with y_offset = *begin;
+   the caller gathers the nx partial sums of every rank (one MPI_Allgather /
+   ncclAllGather of nx doubles) into parts[world][nx], and
+   kqed_shard_combine adds them in rank order with compensated summation. */
+int kqed_shard_slab(size_t ny, int rank, int world, size_t *begin, size_t *end);
+int kqed_shard_combine(size_t nx, int world, const double *parts, double *sums);
+
 /* Message of the last error on the calling thread ("" if none). */
 const char *kqed_last_error(void);
 

@@ -219,6 +219,10 @@ def lib():
         L.ipihatFermLoop_antisym.restype = None
         L.pihat1.argtypes = [dp, dp, QED_kernel_temps, dp, dp]
         L.pihat1.restype = None
+        L.kqed_pinned_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+        L.kqed_pinned_alloc.restype = ctypes.c_int
+        L.kqed_pinned_free.argtypes = [ctypes.c_void_p]
+        L.kqed_pinned_free.restype = ctypes.c_int
         L.kqed_fp32_peak_gflops.argtypes = [dp]
         L.kqed_fp32_peak_gflops.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
@@ -423,6 +427,31 @@ def pihat1(x, y, t):
     r = np.zeros((4, 4, 4, 4))
     lib().pihat1(_dptr(x), _dptr(y), t.t, _dptr(p), _dptr(r))
     return p, r
+
+
+class PinnedArray:
+    """A float64 array in page-locked host memory from kqed_pinned_alloc
+    (cudaHostAlloc): `.array` is a numpy view of it; free() releases it."""
+
+    def __init__(self, shape):
+        self.shape = tuple(int(v) for v in np.atleast_1d(shape))
+        n = int(np.prod(self.shape))
+        self.ptr = ctypes.c_void_p()
+        _check(lib().kqed_pinned_alloc(max(n, 1) * 8, ctypes.byref(self.ptr)))
+        buf = (ctypes.c_double * max(n, 1)).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=n).reshape(self.shape)
+
+    def free(self):
+        if self.ptr and self.ptr.value:
+            self.array = None
+            lib().kqed_pinned_free(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def lattice_sum(t, variant, x, ysites, pi, precision=KQED_FP64):

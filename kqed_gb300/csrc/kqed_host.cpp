@@ -1237,6 +1237,69 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
   return 0;
 }
 
+/* --------------------------------------------- pinned host buffers */
+
+/* Page-locked host memory for a caller's Pi (or any input of the host entry
+   points), allocated with cudaHostAlloc: host-to-device copies from it run
+   at the full host link rate (about 211 GB/s on the GB300 machines, Grace's
+   NVLink-C2C), which memory pinned by other allocators did not always
+   reach. */
+extern "C" int kqed_pinned_alloc(size_t bytes, void **ptr)
+{
+  if (!ptr) return fail("null buffer");
+  *ptr = nullptr;
+  if (bytes == 0) return 0;
+  if (cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    *ptr = nullptr;
+    return fail("cudaHostAlloc of %zu bytes failed", bytes);
+  }
+  return 0;
+}
+
+extern "C" int kqed_pinned_free(void *ptr)
+{
+  if (ptr && cudaFreeHost(ptr) != cudaSuccess) return fail("cudaFreeHost failed");
+  return 0;
+}
+
+/* ---------------------------------------------- multi-GPU sharding */
+
+/* Rank `rank` of `world` takes sites [*begin, *end): contiguous slabs of
+   whole 64-site tiles, sizes differing by at most one tile (the slabs of
+   kqed_gb300/shard.py).  Every rank evaluates its slab against all x
+   (kqed_lattice_sum_dev on the slab, or kqed_lattice_sum_synth with
+   y_offset = *begin); the per-x partial sums are then gathered and added by
+   kqed_shard_combine. */
+extern "C" int kqed_shard_slab(size_t ny, int rank, int world, size_t *begin, size_t *end)
+{
+  if (!begin || !end) return fail("null buffer");
+  if (world < 1 || rank < 0 || rank >= world) return fail("rank %d not in a world of %d", rank, world);
+  const size_t tiles = (ny + kTile - 1) / kTile;
+  const size_t lo = (size_t)rank * tiles / (size_t)world, hi = (size_t)(rank + 1) * tiles / (size_t)world;
+  *begin = std::min(lo * kTile, ny);
+  *end = std::min(hi * kTile, ny);
+  return 0;
+}
+
+/* sums[k] = compensated (Neumaier) sum over ranks r = 0 .. world-1, in rank
+   order, of parts[r][k]: the result does not depend on the order in which a
+   collective delivered the parts */
+extern "C" int kqed_shard_combine(size_t nx, int world, const double *parts, double *sums)
+{
+  if (world < 1) return fail("world %d", world);
+  if (nx && (!parts || !sums)) return fail("null buffer");
+  for (size_t k = 0; k < nx; k++) {
+    double sm = 0.0, c = 0.0;
+    for (int r = 0; r < world; r++) {
+      const double p = parts[(size_t)r * nx + k], t = sm + p;
+      c += std::fabs(sm) >= std::fabs(p) ? (sm - t) + p : (p - t) + sm;
+      sm = t;
+    }
+    sums[k] = sm + c;
+  }
+  return 0;
+}
+
 /* ---------------------------------------------- internal accessors */
 
 namespace kqed {
@@ -1574,8 +1637,15 @@ extern "C" int kqed_batch_plan_create(const struct QED_kernel_temps *t, int njob
       A.Bx2 = p->bx2[j];
     }
   }
-  /* record space: the batch's kernels and the term launches share it */
-  size_t cap = std::min(std::max(total_pairs, zmax), kRecPairs);
+  /* record space: the batch's kernels and the term launches share it; a
+     plan owns its own, so it takes up to 16 M pairs (11 GB) -- at most an
+     eighth of the free device memory -- and the captured graph holds 16x
+     fewer record / assembly launch pairs than with the per-call chunk */
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const size_t per_pair = kRec * sizeof(double) + 12;
+  const size_t plan_cap = std::max(kRecPairs, std::min((size_t)16 << 20, free_b / 8 / per_pair));
+  size_t cap = std::min(std::max(total_pairs, zmax), plan_cap);
   cap = (cap + kTile - 1) / kTile * kTile;
   double *rb = nullptr;
   if (plan_alloc(p, &rb, cap * kRec + cap + cap / 2 + 1 + cap / 8 + 1)) return 1;

@@ -95,3 +95,36 @@ def test_two_gloo_ranks_reproduce_the_single_process_sum():
             np.testing.assert_allclose(res[r][("seed", v)], fullg, rtol=1e-13,
                                        atol=1e-13 * np.abs(fullg).max())
         assert np.array_equal(res[0][("pi", v)], res[1][("pi", v)])
+
+
+def test_c_abi_shard_helpers_match_the_python_design():
+    """kqed_shard_slab / kqed_shard_combine (the C callers' form of the
+    sharding) give shard.py's slabs and its rank-order compensated sums, bit
+    for bit; host code only"""
+    import ctypes
+
+    from kqed_gb300 import build as B
+    B.build()
+    import kqed_gb300 as K
+    from kqed_gb300.shard import combine_rank_order, site_slab
+    L = K.lib()
+    L.kqed_shard_slab.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
+    L.kqed_shard_combine.argtypes = [ctypes.c_size_t, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double)]
+    b, e = ctypes.c_size_t(), ctypes.c_size_t()
+    for ny in (0, 1, 63, 64, 65, 1000, 331776, 5308416):
+        for world in (1, 2, 3, 4, 7, 8):
+            for rank in range(world):
+                assert L.kqed_shard_slab(ny, rank, world, ctypes.byref(b), ctypes.byref(e)) == 0
+                assert (b.value, e.value) == site_slab(ny, rank, world)
+    assert L.kqed_shard_slab(10, 2, 2, ctypes.byref(b), ctypes.byref(e)) != 0
+    rng = np.random.default_rng(9)
+    dp = ctypes.POINTER(ctypes.c_double)
+    for world in (1, 2, 5, 8):
+        parts = rng.standard_normal((world, 32)) * 10.0 ** rng.integers(-8, 8, (world, 32))
+        parts = np.ascontiguousarray(parts)
+        out = np.zeros(32)
+        assert L.kqed_shard_combine(32, world, parts.ctypes.data_as(dp), out.ctypes.data_as(dp)) == 0
+        assert np.array_equal(out, combine_rank_order(parts))
