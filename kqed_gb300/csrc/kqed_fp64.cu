@@ -1700,10 +1700,11 @@ __device__ __forceinline__ uint8_t pair_code(int kind, bool f64, int status)
 }
 
 /* records of pairs p0 + r, r < np, of a batch (x[p], y[p]) */
-/* capped at 168 registers (6 blocks of 64 per SM), as lattice_rec_kernel:
-   pair batches of the FP64 form ran 18% faster (4160 pairs x 64, L0) */
+/* register-capped as lattice_rec_kernel (at least 7 blocks of 64 per SM:
+   128 registers): FP64 pair batches (4160 pairs x 64, L0) ran at 32.3 M
+   evals/s uncapped, 38.0 M at 168 registers and 40.0 M at 128 */
 template <typename SI>
-__global__ void __launch_bounds__(64, 6) l0_rec_kernel(DevTables T, L0Args A, size_t p0, size_t np,
+__global__ void __launch_bounds__(64, 7) l0_rec_kernel(DevTables T, L0Args A, size_t p0, size_t np,
                                                     int mixed, double near2, double orig2,
                                                     int chnr32)
 {
@@ -1767,11 +1768,13 @@ __device__ __forceinline__ bool record_pair(const LatticeArgs &A, const LatticeA
    t = u' % tiles, u' = u - u_begin; record r = uu * kTile + j.  With
    A.list, only the records A.list[0 .. *A.count) (the pairs the lean float
    pass left). */
-/* 6 blocks of 64 per SM: the register cap (168) costs a few spills but
-   12 instead of 8 resident warps hide the column-table loads better; with
-   no cap the step took 8% longer (24^4 lattice, 32 x, L2) */
+/* at least 7 blocks of 64 per SM (the compiler then allocates 128
+   registers: 8 blocks): the cap costs spills, but 16 instead of 8 resident
+   warps hide the column-table loads better; the FP64 step (24^4 lattice,
+   32 x, L2) took 152.5 ms with no cap, 139.8 ms at 168 registers and
+   137.2 ms at 128 */
 template <typename SI>
-__global__ void __launch_bounds__(64, 6) lattice_rec_kernel(DevTables T, const __grid_constant__ LatticeArgs A,
+__global__ void __launch_bounds__(64, 7) lattice_rec_kernel(DevTables T, const __grid_constant__ LatticeArgs A,
                                                          const LatticeArgs *jobs, int njobs,
                                                          size_t u0, size_t nu, int mixed,
                                                          double near2, double orig2, int chnr32)
