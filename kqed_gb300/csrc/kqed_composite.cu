@@ -23,9 +23,11 @@
  *      kernels, FP64 or mixed form);
  *   3. combine_kernel: one block per pair, one thread per component
  *      (rs, mu, nu, lambda); the pair's sources are staged in shared memory,
- *      every slot is evaluated in FP64 in the reference's order of
- *      operations (no contraction into FMAs), and outputs are written
- *      coalesced in the reference's struct layout.
+ *      every slot is evaluated in FP64 -- in the FP64 form in the
+ *      reference's order of operations (no contraction into FMAs), in the
+ *      mixed form with each Gaussian term as two fused multiply-adds (half
+ *      the FP64 operations; this kernel is FP64-pipe-bound on GB300) --
+ *      and outputs are written coalesced in the reference's struct layout.
  * The programs are written out below, term by term from the reference
  * functions they replace; the kernels are generic over them.
  */
@@ -427,6 +429,7 @@ __device__ __forceinline__ int lorentz(int opack, int k) { return (opack >> (2 *
    coef * e_g[mass] of every Gaussian term, and every contraction table, so
    that a Gaussian term costs each component one product, one difference,
    one product and the sum (the reference's order of operations). */
+template <bool FUSED>
 __global__ void __launch_bounds__(kComp) combine_kernel(const __grid_constant__ CProgram P,
                                                         const double *__restrict__ Tsrc, size_t n,
                                                         const double *__restrict__ x,
@@ -498,7 +501,12 @@ __global__ void __launch_bounds__(kComp) combine_kernel(const __grid_constant__ 
       } else {
         const int ci = rs * 16 + (t.wpos == 0 ? i1 * 4 + i2 : (t.wpos == 1 ? i0 * 4 + i2 : i0 * 4 + i1));
         const double pf = CT[t.ct * kConLen + ci];
-        v = __dmul_rn(cg[ti], __dsub_rn(sv, __dmul_rn(mu[t.mass][t.u][lorentz(opack, t.uslot)], pf)));
+        const double m = mu[t.mass][t.u][lorentz(opack, t.uslot)];
+        if (FUSED) { /* two fused multiply-adds */
+          acc = fma(cg[ti], fma(-m, pf, sv), acc);
+          continue;
+        }
+        v = __dmul_rn(cg[ti], __dsub_rn(sv, __dmul_rn(m, pf)));
       }
       acc = __dadd_rn(acc, v);
     }
@@ -544,7 +552,9 @@ int composite_dev(const struct QED_kernel_temps *t, int which, const double *M, 
   const size_t smem = combine_smem(P);
   /* the attribute is per function: set the largest any program needs, so
      that concurrent callers with different programs never lower it */
-  if (cudaFuncSetAttribute(combine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const void *cfn = precision == KQED_FP64 ? (const void *)combine_kernel<false>
+                                           : (const void *)combine_kernel<true>;
+  if (cudaFuncSetAttribute(cfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(((kMaxSrc + kMaxSlot) * kComp + kMaxCon * kConLen) *
                                  sizeof(double))) != cudaSuccess)
     return set_error("composite kernels: shared memory attribute refused");
@@ -556,8 +566,12 @@ int composite_dev(const struct QED_kernel_temps *t, int which, const double *M, 
     if (cudaGetLastError() != cudaSuccess) return set_error("composite derive launch failed");
     g_launches++;
     if (l0_pairs(t, X, Y, th, Tsrc, precision, s)) return 1;
-    combine_kernel<<<(unsigned)m, kComp, smem, s>>>(P, Tsrc, m, dx + 4 * p0, dy + 4 * p0,
-                                                    dout + p0 * osz);
+    if (precision == KQED_FP64)
+      combine_kernel<false><<<(unsigned)m, kComp, smem, s>>>(P, Tsrc, m, dx + 4 * p0, dy + 4 * p0,
+                                                             dout + p0 * osz);
+    else
+      combine_kernel<true><<<(unsigned)m, kComp, smem, s>>>(P, Tsrc, m, dx + 4 * p0, dy + 4 * p0,
+                                                            dout + p0 * osz);
     if (cudaGetLastError() != cudaSuccess) return set_error("composite combine launch failed");
     g_launches++;
   }
