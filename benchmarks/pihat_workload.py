@@ -11,7 +11,8 @@ lattice integrand it feeds.
    (src/amu_forlattice.c:65-116) on a periodic L^4 lattice at spacing 0.1,
    its sites shifted by half a spacing in every direction (the massive
    propagators are singular at y = 0 and y = x, which the reference's own
-   check avoids), with nx points on the diagonal: Pi-hat(Mv x, Mv y), Mv = 2, generated in
+   check avoids), with nx points on the diagonal from x = 0.1 (1,1,1,1) on:
+   Pi-hat(Mv x, Mv y), Mv = 2, generated in
    the fused sums' layout (kqed_pihat_lattice_dev), then the fused FP64
    lattice sum of L0 against it (kqed_lattice_sum_dev); the time of each.
 Prints one JSON line.
@@ -78,7 +79,7 @@ def main():
                            "sample": "first %d pairs" % m}
     res["pairs"]["parity"] = {"max_rel": float(d), "tol": 1e-12, "ok": bool(d <= 1e-12)}
     # the lepton-loop integrand on a lattice
-    xs = diagonal_x(a.nx, 0.1)
+    xs = diagonal_x(a.nx + 1, 0.1)[1:]   # x = 0 is singular for Pi-hat
     ys = lattice_sites(a.L, 0.1) + 0.05
     nx, ny = len(xs), len(ys)
     gx = torch.as_tensor(xs, device="cuda")
