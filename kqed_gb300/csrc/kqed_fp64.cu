@@ -1509,39 +1509,54 @@ __device__ __forceinline__ void stv_y0(const S *R, S *stv, int lane)
   }
 }
 
-/* the STV -> 384 map for the current pair, rows dealt to lanes; result into
-   tbuf (natural row order) */
-template <typename S>
-__device__ __forceinline__ void apply_map_warp(const uint16_t *ent, const uint16_t *rows,
-                                               const MapSched &M, const S *coef, const S *stv,
-                                               S *tbuf, int lane)
+/* The float form's STV components and map, in the warp's region:
+     tab[code * 256 + col] = coefficient(code) * stv[col] for the six
+     coefficients 1, -1, 2, -2, 1/2, -1/2 (codes 0..5; copy 0 is stv itself,
+     the 1/2 copies have columns 0..7 only), so a map term is one entry load,
+     one table load and one add.  Each product by a power of two is exact, so
+     the sums equal those of fmaf(coefficient, stv, acc) bit for bit;
+   - the float record sits in the unused part of copy 4 while the components
+     are computed;
+   - the 384 results overlay the table once the map is done. */
+constexpr int kFCopy = 256;                /* floats between copies */
+constexpr int kFRec = 4 * kFCopy + 8;      /* the float record */
+constexpr int kFTab = 5 * kFCopy + 8;      /* floats the table spans */
+static_assert(kFRec + REC <= 5 * kFCopy, "float record inside copy 4's unused columns");
+
+/* copies 1..5 of the components from copy 0 */
+__device__ __forceinline__ void expand_copies(float *tab, int lane)
 {
-#pragma unroll 1
+#pragma unroll
+  for (int i = lane; i < 202; i += 32) {
+    const float v = tab[i];
+    tab[kFCopy + i] = -v;
+    tab[2 * kFCopy + i] = 2.0f * v;
+    tab[3 * kFCopy + i] = -2.0f * v;
+    if (i < 8) {
+      tab[4 * kFCopy + i] = 0.5f * v;
+      tab[5 * kFCopy + i] = -0.5f * v;
+    }
+  }
+}
+
+/* rows dealt to (round, lane); each lane's 12 row sums stay in registers
+   until the whole warp has read the table, then go to tab[row] */
+__device__ __forceinline__ void map_f32(const uint16_t *ent, const uint16_t *rows,
+                                        const MapSched &M, float *tab, int lane)
+{
+  float res[kMapRounds];
+#pragma unroll
   for (int r = 0; r < kMapRounds; r++) {
     const uint16_t *e = ent + M.off[r] + lane;
     const int len = M.len[r];
-    if (sizeof(S) == 8) {
-      S acc = S(0);
+    float acc = 0.0f;
 #pragma unroll 4
-      for (int q = 0; q < len; q++) {
-        const uint16_t v = e[q * 32];
-        acc = fma(coef[v >> 8], stv[v & 0xff], acc);
-      }
-      tbuf[rows[r * 32 + lane]] = acc;
-    } else {
-      /* float: a plain sum of the (exact) products by +-1/2, +-1, +-2; with
-         the pairs that cancel strongly assembled in FP64, compensation here
-         changed the lattice integrand error by less than its run-to-run
-         spread and cost 4% of the mixed form's time */
-      S acc = S(0);
-#pragma unroll 4
-      for (int q = 0; q < len; q++) {
-        const uint16_t v = e[q * 32];
-        acc = fmaf(coef[v >> 8], stv[v & 0xff], acc);
-      }
-      tbuf[rows[r * 32 + lane]] = acc;
-    }
+    for (int q = 0; q < len; q++) acc += tab[e[q * 32]];
+    res[r] = acc;
   }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < kMapRounds; r++) tab[rows[r * 32 + lane]] = res[r];
 }
 
 /* the map in double-float (FP64 form): coefficients are 0, +-1/2, +-1, +-2,
@@ -1848,6 +1863,7 @@ __global__ void __launch_bounds__(64) lattice_rec_lean_kernel(DevTables T,
    384 components, sized for doubles and reused as floats; per block the map
    schedules and coefficients and the reduction slots. */
 constexpr int kWarpDoubles = REC + 202 + 384;
+static_assert(kFTab <= 2 * kWarpDoubles, "the float form's table fits the warp's region");
 constexpr size_t kSchedBytes = (size_t)(2 * 3072 + 2 * 384) * sizeof(uint16_t);
 
 static size_t asm_smem_bytes(int wpb)
@@ -1860,6 +1876,7 @@ size_t smem_bytes_l0(int wpb) { return asm_smem_bytes(wpb); }
 
 struct AsmSmem {
   double *rec, *stv, *tbuf;        /* this warp's */
+  float *ftab;                     /* this warp's region in the float form */
   double *coefd;
   float *coeff;
   uint16_t *eg, *ez, *rg, *rz;     /* map schedules */
@@ -1871,6 +1888,7 @@ __device__ __forceinline__ AsmSmem carve_asm(int wpb)
   AsmSmem L;
   double *w = reinterpret_cast<double *>(smem_raw) + (size_t)(threadIdx.x >> 5) * kWarpDoubles;
   L.rec = w;
+  L.ftab = reinterpret_cast<float *>(w);
   L.stv = w + REC;
   L.tbuf = L.stv + 202;
   L.coefd = reinterpret_cast<double *>(smem_raw) + (size_t)wpb * kWarpDoubles;
@@ -1885,7 +1903,7 @@ __device__ __forceinline__ AsmSmem carve_asm(int wpb)
 __device__ __forceinline__ void asm_prologue(const DevMaps &M, AsmSmem &L)
 {
   if (threadIdx.x < 8) {
-    const float c[8] = {-2.0f, -1.0f, -0.5f, 0.5f, 1.0f, 2.0f, 0.0f, 0.0f};
+    const float c[8] = {1.0f, -1.0f, 2.0f, -2.0f, 0.5f, -0.5f, 0.0f, 0.0f};
     L.coefd[threadIdx.x] = (double)c[threadIdx.x];
     L.coeff[threadIdx.x] = c[threadIdx.x];
   }
@@ -1909,18 +1927,21 @@ __device__ __forceinline__ void assemble_df(const AsmSmem &L, const DevMaps &M, 
   __syncwarp();
 }
 
-/* the 384 components of one pair into tbuf (type A) */
-template <typename A>
-__device__ __forceinline__ void assemble(const AsmSmem &L, const DevMaps &M, int kind, const A *R,
-                                         A *stv, A *tbuf, const A *coef, int lane)
+/* the 384 float components of one pair into L.ftab[0..383], from the float
+   record at L.ftab + kFRec */
+__device__ __forceinline__ void assemble_f32(const AsmSmem &L, const DevMaps &M, int kind, int lane)
 {
-  if (lane == 0) { stv[200] = A(0); stv[201] = A(0); }
-  if (kind == K_GEN) stv_generic<A>(R, stv, lane);
-  else if (kind == K_X0) stv_x0<A>(R, stv, lane);
-  else stv_y0<A>(R, stv, lane);
+  float *tab = L.ftab;
+  const float *R = tab + kFRec;
+  if (lane == 0) { tab[200] = 0.0f; tab[201] = 0.0f; }
+  if (kind == K_GEN) stv_generic<float>(R, tab, lane);
+  else if (kind == K_X0) stv_x0<float>(R, tab, lane);
+  else stv_y0<float>(R, tab, lane);
   __syncwarp();
-  if (kind == K_GEN) apply_map_warp<A>(L.eg, L.rg, M.gen, coef, stv, tbuf, lane);
-  else apply_map_warp<A>(L.ez, L.rz, M.zero, coef, stv, tbuf, lane);
+  expand_copies(tab, lane);
+  __syncwarp();
+  if (kind == K_GEN) map_f32(L.eg, L.rg, M.gen, tab, lane);
+  else map_f32(L.ez, L.rz, M.zero, tab, lane);
   __syncwarp();
 }
 
@@ -2020,11 +2041,10 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
     assemble_df(L, M, kind, rd, reinterpret_cast<df *>(L.stv), reinterpret_cast<df *>(L.tbuf),
                 lane);
   } else {
-    float *rf = reinterpret_cast<float *>(L.rec);
+    float *rf = L.ftab + kFRec;
     for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));
     __syncwarp();
-    assemble<float>(L, M, kind, rf, reinterpret_cast<float *>(L.stv),
-                    reinterpret_cast<float *>(L.tbuf), L.coeff, lane);
+    assemble_f32(L, M, kind, lane);
   }
   return true;
 }
@@ -2033,7 +2053,7 @@ __device__ __forceinline__ double kcomp(const AsmSmem &L, bool t64, bool perm, i
 {
   const int j = perm ? mulam(i) : i;
   const double v = t64 ? df_to_d(reinterpret_cast<const df *>(L.tbuf)[j])
-                       : (double)reinterpret_cast<const float *>(L.tbuf)[j];
+                       : (double)L.ftab[j];
   return perm ? -v : v;
 }
 
@@ -2141,7 +2161,7 @@ __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm,
     acc[0] += df_to_d<HW>(pacc);
     return;
   }
-  const float *tb = reinterpret_cast<const float *>(L.tbuf);
+  const float *tb = L.ftab;
   float accl = 0.0f;
 #pragma unroll
   for (int r = 0; r < 12; r++) {

@@ -506,19 +506,24 @@ static int build_sched(const unsigned short *row, const unsigned char *col, cons
       for (int l = 0; l < 32; l++) {
         const int i = order[r * 32 + l];
         const int nz = row[i + 1] - row[i];
-        uint16_t e = (uint16_t)(200 | (6 << 8)); /* padding: zero slot, coefficient 0 */
+        uint16_t e = (uint16_t)200; /* padding: the zero slot, coefficient 1 */
         if (s < nz) {
           const int k = row[i] + s;
+          /* codes 0..5 = coefficients 1, -1, 2, -2, 1/2, -1/2: the float
+             assembly reads the product from a table at code * 256 + col, and
+             in this order (the 1/2 terms use columns 0..7 only) the table
+             spans 1288 floats */
           int code;
           switch (q4[k]) {
-          case -8: code = 0; break;
+          case 4: code = 0; break;
           case -4: code = 1; break;
-          case -2: code = 2; break;
-          case 2: code = 3; break;
-          case 4: code = 4; break;
-          case 8: code = 5; break;
+          case 8: code = 2; break;
+          case -8: code = 3; break;
+          case 2: code = 4; break;
+          case -2: code = 5; break;
           default: return 1;
           }
+          if (code >= 4 && col[k] >= 8) return 1;
           e = (uint16_t)(col[k] | (code << 8));
         }
         ent.push_back(e);
