@@ -967,14 +967,24 @@ __device__ int V_taylor(const DevTables &T, VS &D, double x, double y, double xs
 
 /* Destination of a pair's record: float (mixed form) or double */
 __device__ __forceinline__ double f2d_exact(float f);
+__device__ __forceinline__ float d2f_round(double v);
 
+/* A pair's record slot (REC doubles): FP64 values for the pairs assembled in
+   FP64 or double-float, float values (the slot's first half) for the mixed
+   form's float-assembled pairs, which the assembly then reads as they are. */
 struct Sink {
   float *f;
   double *d;
+  __device__ __forceinline__ Sink(double *slot, bool as_float)
+      : f(as_float ? reinterpret_cast<float *>(slot) : nullptr), d(as_float ? nullptr : slot)
+  {
+  }
+  /* FP64 values into a float record are rounded by integer bit manipulation
+     (no FP64-pipe conversion) */
   __device__ __forceinline__ void put(int i, double v) const
   {
     if (d) d[i] = v;
-    else f[i] = (float)v;
+    else f[i] = d2f_round(v);
   }
   /* float values (the mixed form's chain rule) enter FP64 records exactly,
      without FP64-pipe conversions */
@@ -1729,9 +1739,7 @@ __global__ void __launch_bounds__(64, 7) l0_rec_kernel(DevTables T, L0Args A, si
     double xv[4], yv[4];
     for (int m = 0; m < 4; m++) { xv[m] = A.x[4 * p + m]; yv[m] = A.y[4 * p + m]; }
     const bool f64 = mixed && fp64_assembly(xv, yv, near2, orig2);
-    Sink sk;
-    sk.f = nullptr;
-    sk.d = A.rec + r * REC;
+    const Sink sk(A.rec + r * REC, false);
     int status;
     const int kind = phase_a<SI>(T, xv, yv, sk, status, (const SI *)nullptr, nullptr, f64,
                                  chnr32 != 0);
@@ -1810,9 +1818,7 @@ __global__ void __launch_bounds__(64, 7) lattice_rec_kernel(DevTables T, const _
       continue;
     }
     const bool f64 = mixed && fp64_assembly(xv, yv, near2, orig2);
-    Sink sk;
-    sk.f = nullptr;
-    sk.d = A.rec + r * REC;
+    const Sink sk(A.rec + r * REC, sizeof(SI) == 4 && mixed && !f64);
     int status;
     const SI *col = column_of<SI>(J);
     const int kind = phase_a<SI>(T, xv, yv, sk, status, col ? col + k * per_x : nullptr,
@@ -1844,9 +1850,7 @@ __global__ void __launch_bounds__(64) lattice_rec_lean_kernel(DevTables T,
     for (int m = 0; m < 4; m++) { xv[m] = J.x[4 * k + m]; yv[m] = J.y[4 * n + m]; }
     int kind = -1, status = 0;
     if (!fp64_assembly(xv, yv, near2, orig2)) {
-      Sink sk;
-      sk.f = nullptr;
-      sk.d = A.rec + r * REC;
+      const Sink sk(A.rec + r * REC, true);
       kind = phase_a_lean(T, xv, yv, sk, status, J.col32 ? J.col32 + k * per_x : nullptr);
     }
     if (kind < 0) {
@@ -1971,7 +1975,9 @@ __device__ __forceinline__ float d2f_round(double v)
 /* one pair by the warp, in the assembly precision S (the mixed form's
    flagged pairs in FP64): record from global memory to shared memory, then
    assemble.  Returns false for a zero kernel; t64 says whether the
-   components are double-float (else float).
+   components are double-float (else float).  FREC: the float-assembled
+   pairs' records are float (the lattice sums' record kernels), else FP64
+   (the pair batches, whose record kernel writes FP64 for every pair).
 
    Two kinds of pair leave the assembly with their components rounded
    through FP64:
@@ -2018,7 +2024,7 @@ __device__ __noinline__ void asm_pair_rare(const AsmSmem &L, const DevMaps &M, c
   __syncwarp();
 }
 
-template <typename S>
+template <typename S, bool FREC>
 __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, const double *grec,
                                          int code, int lane, bool &perm, bool &t64,
                                          bool round_axis = false)
@@ -2042,7 +2048,12 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
                 lane);
   } else {
     float *rf = L.ftab + kFRec;
-    for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));
+    if (FREC) {
+      const float *gf = reinterpret_cast<const float *>(grec);
+      for (int i = lane; i < REC; i += 32) rf[i] = __ldg(gf + i);
+    } else {
+      for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));
+    }
     __syncwarp();
     assemble_f32(L, M, kind, lane);
   }
@@ -2074,7 +2085,7 @@ __global__ void __launch_bounds__(256) l0_asm_kernel(DevMaps M, L0Args A, size_t
   for (size_t r = (size_t)blockIdx.x * wpb + warp; r < np; r += (size_t)gridDim.x * wpb) {
     const int code = A.code[r];
     bool perm, t64;
-    const bool live = asm_pair<S>(L, M, A.rec + r * REC, code, lane, perm, t64);
+    const bool live = asm_pair<S, false>(L, M, A.rec + r * REC, code, lane, perm, t64);
     double *o = A.out + (p0 + r) * 384;
 #pragma unroll
     for (int q = 0; q < 12; q++) {
@@ -2100,6 +2111,18 @@ __device__ __forceinline__ double f2d_exact(float f)
   const unsigned e = (u >> 23) & 0xffu;
   const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
   return e == 0 ? 0.0 : __hiloint2double((int)hi, (int)(u << 29));
+}
+
+/* float approximation of an FP64 value from its high word alone: the top 20
+   mantissa bits (truncated), the exponent clamped to the float range (values
+   below 2^-126 give zero).  For the product of Pi with the low parts of the
+   per-site and per-x terms, themselves below 2^-24 of the components they
+   complete, its relative error of 2^-20 is 2^-44 of the contribution. */
+__device__ __forceinline__ float d2f_hiword(double v)
+{
+  const int hi = __double2hiint(v);
+  const int m = min(max((hi & 0x7fffffff) - ((1023 - 127) << 20), 0), 0x0fefffff);
+  return __int_as_float((m << 3) | (hi & (int)0x80000000));
 }
 
 /* Pi component r*32 + lane of a pair, r = 4g + w: stored (pi) or, GEN,
@@ -2135,7 +2158,8 @@ template <> struct PiSrc<true> {
    per-x terms as float (hi, lo) pairs: the hi parts are added in float,
    where L1..L3's near-cancelling terms subtract exactly, and each component
    enters an FP64 product with Pi, so neither Pi nor the sum is rounded to
-   float; the lo parts go through a float accumulator. */
+   float; the lo parts go through a float accumulator, against Pi's high
+   word. */
 template <bool GEN, bool HW>
 __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm, bool t64,
                                          const PiSrc<GEN> &P, const double *ky, const double *bx,
@@ -2172,7 +2196,7 @@ __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm,
     if (bx2) { const float2 q = __ldg(bx2 + i); kh += q.x; kl += q.y; }
     const double p = P.get(r, pg, lane);
     acc[r & 1] = fma(f2d_exact(kh), p, acc[r & 1]);
-    if (ky2 || bx2) accl = fmaf(kl, d2f_round(p), accl);
+    if (ky2 || bx2) accl = fmaf(kl, d2f_hiword(p), accl);
   }
   if (ky2 || bx2) acc[1] += f2d_exact(accl);
 }
@@ -2221,7 +2245,7 @@ __global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __
       const int code = A.code[r];
       if ((code & 7) == K_VANISH) continue;
       bool perm, t64;
-      const bool live = asm_pair<S>(L, M, A.rec + r * REC, code, lane, perm, t64, true);
+      const bool live = asm_pair<S, true>(L, M, A.rec + r * REC, code, lane, perm, t64, true);
       const double *ky = J.Ky ? J.Ky + n * 384 : nullptr, *bx = J.Bx ? J.Bx + k * 384 : nullptr;
       const float2 *ky2 = J.Ky2 ? J.Ky2 + n * 384 : nullptr;
       const float2 *bx2 = J.Bx2 ? J.Bx2 + k * 384 : nullptr;
@@ -2454,9 +2478,7 @@ __global__ void __launch_bounds__(64) lattice_sur_select_kernel(DevTables T,
        pass for the float pairs, the full record kernel for the rest */
     int kind = -1, status = 0;
     if (!fp64_assembly(xv, yv, near2, orig2)) {
-      Sink sk;
-      sk.f = nullptr;
-      sk.d = A.rec + r * REC;
+      const Sink sk(A.rec + r * REC, true);
       const size_t per_x = (size_t)T.nstpy * T.NK * kRow;
       kind = phase_a_lean(T, xv, yv, sk, status, J.col32 ? J.col32 + k * per_x : nullptr);
     }
@@ -2500,9 +2522,7 @@ __global__ void __launch_bounds__(64) lattice_sur_record_kernel(DevTables T,
     const int flag_hy = (I.y >= __ldg(T.YY + T.nstpy - 1));
     const bool dd = I.flag2 && !flag_hy && I.iy + 1 < T.nstpy - 1;
     if (!dd) { W[37] = 0.0f; W[38] = 0.0f; }
-    Sink sk;
-    sk.f = nullptr;
-    sk.d = A.rec + r * REC;
+    const Sink sk(A.rec + r * REC, true);
     fill_record_f32(sk, xv, yv, I, W, T.ystp);
     A.code[r] = pair_code(K_GEN, false, I.flag2 ? 4 : 0);
     if (!J.pi) A.env[r] = pi_envelope(xv, yv);
