@@ -1549,19 +1549,23 @@ __device__ __forceinline__ void expand_copies(float *tab, int lane)
   }
 }
 
-/* rows dealt to (round, lane); each lane's 12 row sums stay in registers
-   until the whole warp has read the table, then go to tab[row] */
-__device__ __forceinline__ void map_f32(const uint16_t *ent, const uint16_t *rows,
-                                        const MapSched &M, float *tab, int lane)
+/* rows dealt to (round, lane); the rounds' lengths are compile-time
+   constants (map_round_len), so every entry load has a fixed offset and the
+   loads of a round can be issued ahead of its adds.  Each lane's 12 row sums
+   stay in registers until the whole warp has read the table, then go to
+   tab[row]. */
+template <bool GEN>
+__device__ __forceinline__ void map_f32(const uint16_t *ent, const uint16_t *rows, float *tab,
+                                        int lane)
 {
   float res[kMapRounds];
+  const uint16_t *e = ent + lane;
 #pragma unroll
   for (int r = 0; r < kMapRounds; r++) {
-    const uint16_t *e = ent + M.off[r] + lane;
-    const int len = M.len[r];
     float acc = 0.0f;
-#pragma unroll 4
-    for (int q = 0; q < len; q++) acc += tab[e[q * 32]];
+#pragma unroll
+    for (int q = 0; q < map_round_len(GEN, r); q++) acc += tab[e[q * 32]];
+    e += 32 * map_round_len(GEN, r);
     res[r] = acc;
   }
   __syncwarp();
@@ -1944,8 +1948,8 @@ __device__ __forceinline__ void assemble_f32(const AsmSmem &L, const DevMaps &M,
   __syncwarp();
   expand_copies(tab, lane);
   __syncwarp();
-  if (kind == K_GEN) map_f32(L.eg, L.rg, M.gen, tab, lane);
-  else map_f32(L.ez, L.rz, M.zero, tab, lane);
+  if (kind == K_GEN) map_f32<true>(L.eg, L.rg, tab, lane);
+  else map_f32<false>(L.ez, L.rz, tab, lane);
   __syncwarp();
 }
 

@@ -531,6 +531,9 @@ static int build_sched(const unsigned short *row, const unsigned char *col, cons
     off += len * 32;
   }
   S.total = off;
+  const bool gen = row == KQ_MAP_GEN_ROW;
+  for (int r = 0; r < kMapRounds; r++)
+    if (S.len[r] != map_round_len(gen, r)) return 1;
   return off > 3072 ? 1 : 0;
 }
 

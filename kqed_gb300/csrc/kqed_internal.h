@@ -68,6 +68,14 @@ struct MapSched {
   int total;                /* entries in total (multiple of 32) */
 };
 
+/* The round lengths the two constant maps give (the float assembly unrolls
+   its rounds with them; the host checks its schedules against them) */
+__host__ __device__ constexpr int map_round_len(bool gen, int r)
+{
+  return gen ? (r == 0 ? 14 : r < 3 ? 13 : r == 3 ? 8 : r == 4 ? 7 : r < 8 ? 6 : r == 8 ? 4 : r < 11 ? 3 : 2)
+             : (r < 3 ? 12 : r < 5 ? 8 : r < 7 ? 6 : r == 7 ? 5 : r == 8 ? 4 : r < 11 ? 3 : 2);
+}
+
 struct DevMaps {
   const uint16_t *ent_gen, *ent_zero;   /* col | code<<8 */
   const uint16_t *row_gen, *row_zero;   /* [round*32 + lane] -> output row */
