@@ -1403,10 +1403,21 @@ __device__ int phase_a_lean(const DevTables &T, const double *xv, const double *
 
 /* ------------------------------------------------ phases B and C (warp) */
 
+/* Where the STV components go: StvOut stores each once (the FP64 and
+   double-float assemblies); the float assembly's StvTab stores each with the
+   pre-scaled copies the map reads (layout at kFCopy below): Tx and Ty
+   (columns 8..135) with 1, -1, 2, -2, V (136..199) with 1, -1, the S
+   vectors (0..7) with 1/2, -1/2. */
+template <typename S> struct StvOut {
+  S *p;
+  __device__ __forceinline__ void t(int c, S v) const { p[c] = v; }
+  __device__ __forceinline__ void v(int c, S v) const { p[c] = v; }
+  __device__ __forceinline__ void s(int c, S v) const { p[c] = v; }
+};
 /* 200 STV components of one generic pair into stv[] (lane-parallel):
    chnr_dS.c:85-93, chnr_dT.c:353-385, get_dv chnr_dV.c:326-357 */
-template <typename S>
-__device__ __forceinline__ void stv_generic(const S *R, S *stv, int lane)
+template <typename S, typename O>
+__device__ __forceinline__ void stv_generic(const S *R, const O &stv, int lane)
 {
   const S z = S(0);
 #pragma unroll
@@ -1422,10 +1433,10 @@ __device__ __forceinline__ void stv_generic(const S *R, S *stv, int lane)
     const S t4 = yv[a] * yv[d] - (d_ad ? R[R_YSQ] * S(0.25) : z);
     const S t5 = xv[a] * yv[d] + yv[a] * xv[d] - (d_ad ? S(0.5) * R[R_XDY] : z);
     const S *T = R + R_T;
-    stv[72 + idx] = t1 * T[1] + t2 * T[2] + t3 * (c1 * T[4] + c2 * T[5]) +
-                    t4 * (c1 * T[7] + c2 * T[8]) + t5 * (c1 * T[10] + c2 * T[11]);
-    stv[8 + idx] = t2 * T[0] + t1 * T[2] + t3 * (c3 * T[3] + c4 * T[5]) +
-                   t4 * (c3 * T[6] + c4 * T[8]) + t5 * (c3 * T[9] + c4 * T[11]);
+    stv.t(72 + idx, t1 * T[1] + t2 * T[2] + t3 * (c1 * T[4] + c2 * T[5]) +
+                    t4 * (c1 * T[7] + c2 * T[8]) + t5 * (c1 * T[10] + c2 * T[11]));
+    stv.t(8 + idx, t2 * T[0] + t1 * T[2] + t3 * (c3 * T[3] + c4 * T[5]) +
+                   t4 * (c3 * T[6] + c4 * T[8]) + t5 * (c3 * T[9] + c4 * T[11]));
   }
 #pragma unroll
   for (int r = 0; r < 2; r++) {
@@ -1447,18 +1458,18 @@ __device__ __forceinline__ void stv_generic(const S *R, S *stv, int lane)
     f += (Dv[8 + d] * xb + Dv[12 + d] * yb) * c4a;
     f += (Dv[16 + d] * xa + Dv[20 + d] * c4a) * c2c4;
     f += Dv[24 + d] * (dab - xaxb);
-    stv[136 + idx] = f + Dv[28 + d] * c1;
+    stv.v(136 + idx, f + Dv[28 + d] * c1);
   }
   if (lane < 8) {
     const int b = lane & 3;
-    stv[lane] = lane < 4 ? R[R_XH + b] * R[R_S + 0] + R[R_C4 + b] * R[R_S + 2]
-                         : R[R_YH + b] * R[R_S + 1] + R[R_C2 + b] * R[R_S + 2];
+    stv.s(lane, lane < 4 ? R[R_XH + b] * R[R_S + 0] + R[R_C4 + b] * R[R_S + 2]
+                         : R[R_YH + b] * R[R_S + 1] + R[R_C2 + b] * R[R_S + 2]);
   }
 }
 
 /* x = 0: tI -> V, tII -> Tx, tIII -> Ty (Tabd.c:87-111) */
-template <typename S>
-__device__ __forceinline__ void stv_x0(const S *R, S *stv, int lane)
+template <typename S, typename O>
+__device__ __forceinline__ void stv_x0(const S *R, const O &stv, int lane)
 {
   const S z = S(0);
 #pragma unroll
@@ -1480,15 +1491,15 @@ __device__ __forceinline__ void stv_x0(const S *R, S *stv, int lane)
     tI += R[X0_YHD3 + b] * yh[a] * yh[d];
     if (d_ad) tI += R[X0_YHD1 + b];
     tI += yv[d] * tIsum;
-    stv[136 + idx] = tI;
-    stv[8 + idx] = tII;
-    stv[72 + idx] = tIII;
+    stv.v(136 + idx, tI);
+    stv.t(8 + idx, tII);
+    stv.t(72 + idx, tIII);
   }
 }
 
 /* y = 0 (and x = y): Tabd.c:196-217 */
-template <typename S>
-__device__ __forceinline__ void stv_y0(const S *R, S *stv, int lane)
+template <typename S, typename O>
+__device__ __forceinline__ void stv_y0(const S *R, const O &stv, int lane)
 {
   const S z = S(0);
 #pragma unroll
@@ -1513,9 +1524,9 @@ __device__ __forceinline__ void stv_y0(const S *R, S *stv, int lane)
     if (d_ab) sm += xh[d];
     const S tI = (sm - xh[a] * xh[b] * xh[d]) * R[Y0_D4] +
                  xh[a] * (xh[b] * xv[d] * R[Y0_D2] - (d_bd ? R[Y0_D3] : z));
-    stv[136 + idx] = tI;
-    stv[8 + idx] = tII;
-    stv[72 + idx] = tIII;
+    stv.v(136 + idx, tI);
+    stv.t(8 + idx, tII);
+    stv.t(72 + idx, tIII);
   }
 }
 
@@ -1533,30 +1544,38 @@ constexpr int kFRec = 4 * kFCopy + 8;      /* the float record */
 constexpr int kFTab = 5 * kFCopy + 8;      /* floats the table spans */
 static_assert(kFRec + REC <= 5 * kFCopy, "float record inside copy 4's unused columns");
 
-/* copies 1..5 of the components from copy 0 */
-__device__ __forceinline__ void expand_copies(float *tab, int lane)
-{
-#pragma unroll
-  for (int i = lane; i < 202; i += 32) {
-    const float v = tab[i];
-    tab[kFCopy + i] = -v;
-    tab[2 * kFCopy + i] = 2.0f * v;
-    tab[3 * kFCopy + i] = -2.0f * v;
-    if (i < 8) {
-      tab[4 * kFCopy + i] = 0.5f * v;
-      tab[5 * kFCopy + i] = -0.5f * v;
-    }
+struct StvTab {
+  float *p;
+  __device__ __forceinline__ void t(int c, float x) const
+  {
+    p[c] = x;
+    p[kFCopy + c] = -x;
+    p[2 * kFCopy + c] = 2.0f * x;
+    p[3 * kFCopy + c] = -2.0f * x;
   }
-}
+  __device__ __forceinline__ void v(int c, float x) const
+  {
+    p[c] = x;
+    p[kFCopy + c] = -x;
+  }
+  __device__ __forceinline__ void s(int c, float x) const
+  {
+    p[4 * kFCopy + c] = 0.5f * x;
+    p[5 * kFCopy + c] = -0.5f * x;
+  }
+};
 
 /* rows dealt to (round, lane); the rounds' lengths are compile-time
    constants (map_round_len), so every entry load has a fixed offset and the
    loads of a round can be issued ahead of its adds.  Each lane's 12 row sums
    stay in registers until the whole warp has read the table, then go to
-   tab[row]. */
+   tab[row], or, for a pair that takes the mu <-> lambda permutation with a
+   sign (perm, the same for the whole warp), to tab[mulam(row)] negated, so
+   that the contraction reads component i at tab[i] either way. */
+__device__ __forceinline__ int mulam(int i);
 template <bool GEN>
 __device__ __forceinline__ void map_f32(const uint16_t *ent, const uint16_t *rows, float *tab,
-                                        int lane)
+                                        int lane, bool perm)
 {
   float res[kMapRounds];
   const uint16_t *e = ent + lane;
@@ -1569,8 +1588,13 @@ __device__ __forceinline__ void map_f32(const uint16_t *ent, const uint16_t *row
     res[r] = acc;
   }
   __syncwarp();
+  if (perm) {
 #pragma unroll
-  for (int r = 0; r < kMapRounds; r++) tab[rows[r * 32 + lane]] = res[r];
+    for (int r = 0; r < kMapRounds; r++) tab[mulam(rows[r * 32 + lane])] = -res[r];
+  } else {
+#pragma unroll
+    for (int r = 0; r < kMapRounds; r++) tab[rows[r * 32 + lane]] = res[r];
+  }
 }
 
 /* the map in double-float (FP64 form): coefficients are 0, +-1/2, +-1, +-2,
@@ -1926,30 +1950,30 @@ __device__ __forceinline__ void assemble_df(const AsmSmem &L, const DevMaps &M, 
                                             const df *R, df *stv, df *tbuf, int lane)
 {
   if (lane == 0) { stv[200] = df(0.0f, 0.0f); stv[201] = df(0.0f, 0.0f); }
-  if (kind == K_GEN) stv_generic<df>(R, stv, lane);
-  else if (kind == K_X0) stv_x0<df>(R, stv, lane);
-  else stv_y0<df>(R, stv, lane);
+  const StvOut<df> o{stv};
+  if (kind == K_GEN) stv_generic(R, o, lane);
+  else if (kind == K_X0) stv_x0(R, o, lane);
+  else stv_y0(R, o, lane);
   __syncwarp();
   if (kind == K_GEN) apply_map_warp_df(L.eg, L.rg, M.gen, L.coeff, stv, tbuf, lane);
   else apply_map_warp_df(L.ez, L.rz, M.zero, L.coeff, stv, tbuf, lane);
   __syncwarp();
 }
 
-/* the 384 float components of one pair into L.ftab[0..383], from the float
-   record at L.ftab + kFRec */
-__device__ __forceinline__ void assemble_f32(const AsmSmem &L, const DevMaps &M, int kind, int lane)
+/* the 384 float components of one pair into L.ftab[0..383] (permuted and
+   negated for K_Y0PERM), from the float record at L.ftab + kFRec */
+__device__ __forceinline__ void assemble_f32(const AsmSmem &L, int kind, int lane)
 {
   float *tab = L.ftab;
   const float *R = tab + kFRec;
   if (lane == 0) { tab[200] = 0.0f; tab[201] = 0.0f; }
-  if (kind == K_GEN) stv_generic<float>(R, tab, lane);
-  else if (kind == K_X0) stv_x0<float>(R, tab, lane);
-  else stv_y0<float>(R, tab, lane);
+  const StvTab o{tab};
+  if (kind == K_GEN) stv_generic(R, o, lane);
+  else if (kind == K_X0) stv_x0(R, o, lane);
+  else stv_y0(R, o, lane);
   __syncwarp();
-  expand_copies(tab, lane);
-  __syncwarp();
-  if (kind == K_GEN) map_f32<true>(L.eg, L.rg, tab, lane);
-  else map_f32<false>(L.ez, L.rz, tab, lane);
+  if (kind == K_GEN) map_f32<true>(L.eg, L.rg, tab, lane, false);
+  else map_f32<false>(L.ez, L.rz, tab, lane, kind == K_Y0PERM);
   __syncwarp();
 }
 
@@ -2012,7 +2036,7 @@ __device__ __noinline__ void asm_pair_rare(const AsmSmem &L, const DevMaps &M, c
     for (int i = lane; i < REC; i += 32) L.rec[i] = __ldg(grec + i);
     if (lane == 0) { L.stv[200] = 0.0; L.stv[201] = 0.0; }
     __syncwarp();
-    stv_generic<double>(L.rec, L.stv, lane);
+    stv_generic(static_cast<const double *>(L.rec), StvOut<double>{L.stv}, lane);
     __syncwarp();
     df *stv = reinterpret_cast<df *>(L.stv);
     for (int i = lane; i < 202; i += 32) stv[i] = split_d<true>(L.stv[i]);
@@ -2059,16 +2083,16 @@ __device__ __forceinline__ bool asm_pair(const AsmSmem &L, const DevMaps &M, con
       for (int i = lane; i < REC; i += 32) rf[i] = d2f_round(__ldg(grec + i));
     }
     __syncwarp();
-    assemble_f32(L, M, kind, lane);
+    assemble_f32(L, kind, lane);
   }
   return true;
 }
 
 __device__ __forceinline__ double kcomp(const AsmSmem &L, bool t64, bool perm, int i)
 {
+  if (!t64) return (double)L.ftab[i]; /* already permuted */
   const int j = perm ? mulam(i) : i;
-  const double v = t64 ? df_to_d(reinterpret_cast<const df *>(L.tbuf)[j])
-                       : (double)L.ftab[j];
+  const double v = df_to_d(reinterpret_cast<const df *>(L.tbuf)[j]);
   return perm ? -v : v;
 }
 
@@ -2195,7 +2219,7 @@ __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm,
   for (int r = 0; r < 12; r++) {
     if ((r & 3) == 0) P.group(r >> 2, pg, lane);
     const int i = r * 32 + lane;
-    float kh = perm ? -tb[mulam(i)] : tb[i], kl = 0.0f;
+    float kh = tb[i], kl = 0.0f;
     if (ky2) { const float2 q = __ldg(ky2 + i); kh += q.x; kl += q.y; }
     if (bx2) { const float2 q = __ldg(bx2 + i); kh += q.x; kl += q.y; }
     const double p = P.get(r, pg, lane);
@@ -2208,10 +2232,12 @@ __device__ __forceinline__ void contract(const AsmSmem &L, bool live, bool perm,
 /* Fused lattice integrand over units u0 + uu, uu < nu (block per unit, warps
    over its sites): partial[k][t] = (sum, compensation) of the unit's pairs,
    warp sums in site order, block sum in warp order. */
-/* 4-warp blocks, up to 6 per SM (<= 80 registers): the assembly is latency
-   bound, and 24 resident warps per SM beat 16 unconstrained ones */
+/* 4-warp blocks, up to 6 per SM (<= 80 registers) for the FP64 form: the
+   assembly is latency bound, and 24 resident warps per SM beat 16
+   unconstrained ones.  The float form's unrolled map keeps more values in
+   flight: 5 blocks (96 registers) ran its 24^4 step 0.7% faster than 6. */
 template <typename S, bool BATCH>
-__global__ void __launch_bounds__(128, 6) lattice_asm_kernel(DevMaps M, const __grid_constant__ LatticeArgs A,
+__global__ void __launch_bounds__(128, sizeof(S) == 4 ? 5 : 6) lattice_asm_kernel(DevMaps M, const __grid_constant__ LatticeArgs A,
                                                           const LatticeArgs *jobs, int njobs,
                                                           size_t u0, size_t nu, int wpb)
 {
