@@ -14,8 +14,10 @@ inputs resident in HBM, in the precision form given by --precision (fp64:
 the plain FP64 form, bit-for-bit the reference's algorithm; fp32: the mixed
 form).  Both forms are always timed on the same inputs and reported under
 `forms`, with the mixed form's integrand error against the FP64 sums of the
-same run.  `e2e` times the host entry point (Pi copied from pinned host
-memory every step).  --impl reference times the reference's CPU
+same run.  `e2e` times the host entry point with Pi in page-locked host
+memory from the library's allocator: every step the kernels read it there,
+over the host link (`pi_route`; KQED_HOST_PI=copy stages it through device
+buffers instead).  --impl reference times the reference's CPU
 implementation of the same computation on the host cores (the reference
 library compiled from its sources when it is available here, else the CPU
 restatement under oracle/).
@@ -357,8 +359,8 @@ def run_gb300(args):
 
     # ---- end to end through the host entry point (Pi from pinned memory)
     def measure_e2e(pi):
-        # the caller's Pi in page-locked memory from the library's allocator
-        # (cudaHostAlloc: the full host link rate)
+        # the caller's Pi in page-locked, device-mapped memory from the
+        # library's allocator, which the kernels read in place
         pinned = K.PinnedArray(tuple(pi.shape))
         pi_host = torch.from_numpy(pinned.array)
         pi_host.copy_(pi)
@@ -390,8 +392,9 @@ def run_gb300(args):
             mt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
             torch.distributed.all_reduce(mt, op=torch.distributed.ReduceOp.MAX)
             e2e_s = float(mt.item())
-        # host->device link rate right after (the same pinned buffer, 1 GB pieces):
-        # Pi crosses the link every step, so e2e cannot beat bytes / this rate
+        # host->device copy rate right after (the same pinned buffer, 1 GB
+        # pieces): the bound of the staged route, which the in-place route,
+        # reading Pi with the GPU's own loads, can pass
         scratch = torch.empty(min(pi_host.numel(), 1 << 27), dtype=torch.float64, device=dev)
         flat = pi_host.view(-1)
         torch.cuda.synchronize(dev)
@@ -404,7 +407,11 @@ def run_gb300(args):
         torch.cuda.synchronize(dev)
         h2d_gbs = moved / (time.perf_counter() - c0) / 1e9
         del scratch
+        in_place = (K.pinned_contains(pi_host.data_ptr(), pi_host.numel() * 8)
+                    and os.environ.get("KQED_HOST_PI") != "copy")
         e2e = {"value": total_pairs / e2e_s, "unit": UNIT,
+               "pi_route": ("read in place by the kernels over the host link" if in_place
+                            else "staged through device buffers by copies"),
                "h2d_bytes_per_step": int(pi_host.numel() * 8 + xh.nbytes + yh.nbytes),
                "d2h_bytes_per_step": int(sh.nbytes),
                "precision": args.precision,
@@ -414,6 +421,7 @@ def run_gb300(args):
                "copy_ms_per_step": e2e_copy_ms / args.e2e_steps,
                "h2d_gbs_during_step": pi_host.numel() * 8 / (e2e_copy_ms / args.e2e_steps / 1e3) / 1e9
                if e2e_copy_ms > 0 else None,
+               "h2d_gbs_effective": pi_host.numel() * 8 / e2e_s / 1e9,
                "copy_bound_evals_per_s": total_pairs / (pi_host.numel() * 8 / (h2d_gbs * 1e9))}
         return e2e, pi_host, pinned
 

@@ -285,7 +285,11 @@ int kqed_pihat_lattice_dev(size_t nx, const double *d_x, size_t ny, const double
    with pi laid out [nx][ny][384].  Accumulation is FP64 with compensated
    (Neumaier) summation and a fixed reduction order, so results are
    reproducible.  An empty lattice (ny = 0) gives zero sums; its site and pi
-   pointers may then be NULL.  Host buffers. */
+   pointers may then be NULL.  Host buffers.  A pi lying wholly inside one
+   allocation of kqed_pinned_alloc is read in place by the kernels over the
+   host link (no staging copies); any other pi is copied to the device in
+   chunks overlapped with the kernels.  The sums are the same either way;
+   the environment variable KQED_HOST_PI=copy forces the copies. */
 int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, size_t nx, const double *x,
                      size_t ny, const double *y, const double *pi, double *sums, int precision);
 
@@ -335,11 +339,14 @@ int kqed_pi_synth_dev(size_t nx, const double *d_x, size_t ny, const double *d_y
                       uint32_t stream_id, size_t x_offset, size_t y_offset, double *d_pi,
                       void *stream);
 
-/* Page-locked host memory (cudaHostAlloc) for the inputs of the host entry
-   points, e.g. the caller's Pi of kqed_lattice_sum: copies from it run at
-   the full host link rate.  Free with kqed_pinned_free. */
+/* Page-locked, device-mapped host memory (cudaHostAlloc) for the inputs of
+   the host entry points, e.g. the caller's Pi of kqed_lattice_sum, which the
+   kernels then read in place.  Free with kqed_pinned_free.
+   kqed_pinned_contains: 1 if [ptr, ptr + bytes) lies wholly inside one live
+   allocation of kqed_pinned_alloc, else 0. */
 int kqed_pinned_alloc(size_t bytes, void **ptr);
 int kqed_pinned_free(void *ptr);
+int kqed_pinned_contains(const void *ptr, size_t bytes);
 
 /* Multi-GPU sharding of a lattice sum, one process per GPU: rank `rank` of
    `world` takes sites [*begin, *end) (contiguous slabs of whole 64-site

@@ -223,6 +223,8 @@ def lib():
         L.kqed_pinned_alloc.restype = ctypes.c_int
         L.kqed_pinned_free.argtypes = [ctypes.c_void_p]
         L.kqed_pinned_free.restype = ctypes.c_int
+        L.kqed_pinned_contains.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+        L.kqed_pinned_contains.restype = ctypes.c_int
         L.kqed_fp32_peak_gflops.argtypes = [dp]
         L.kqed_fp32_peak_gflops.restype = ctypes.c_int
         L.kqed_fp64_peak_gflops.argtypes = [dp]
@@ -429,9 +431,16 @@ def pihat1(x, y, t):
     return p, r
 
 
+def pinned_contains(ptr, nbytes):
+    """True if [ptr, ptr + nbytes) lies inside one kqed_pinned_alloc block
+    (kqed_lattice_sum then reads a Pi there in place)."""
+    return bool(lib().kqed_pinned_contains(ctypes.c_void_p(ptr), nbytes))
+
+
 class PinnedArray:
-    """A float64 array in page-locked host memory from kqed_pinned_alloc
-    (cudaHostAlloc): `.array` is a numpy view of it; free() releases it."""
+    """A float64 array in page-locked, device-mapped host memory from
+    kqed_pinned_alloc (cudaHostAlloc): `.array` is a numpy view of it; free()
+    releases it.  kqed_lattice_sum reads a Pi held here in place."""
 
     def __init__(self, shape):
         self.shape = tuple(int(v) for v in np.atleast_1d(shape))

@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -1186,9 +1187,27 @@ extern "C" int kqed_pi_synth_dev(size_t nx, const double *d_x, size_t ny, const 
   return 0;
 }
 
-/* Host buffers.  Pi streams to the device in per-x chunks through a double
-   buffer on a copy stream, so the transfer of chunk i+1 overlaps the fused
-   kernel on chunk i (with pinned host memory the copies run asynchronously). */
+/* the device address of [p, p + bytes) when the whole range lies in one
+   allocation of kqed_pinned_alloc (page-locked and mapped), else null */
+static const void *pinned_device_range(const void *p, size_t bytes);
+
+/* KQED_HOST_PI=copy: stage Pi through device buffers even when the kernels
+   could read it in place */
+static bool host_pi_copy_forced()
+{
+  const char *v = getenv("KQED_HOST_PI");
+  return v && strcmp(v, "copy") == 0;
+}
+
+/* Host buffers.  Pi in memory from kqed_pinned_alloc is read in place by the
+   kernels over the host link (Grace's NVLink-C2C carries the GPU's loads of
+   page-locked host memory; no staging copies, and no copy-engine warm-up:
+   on the GB300 machines a 32.6 GB Pi ran at 213 ms per FP64 step in place
+   against 240-280 ms staged).  Other host memory streams to the device in
+   per-x chunks through a double buffer on a copy stream, so the transfer of
+   chunk i+1 overlaps the fused kernel on chunk i (with pinned host memory
+   the copies run asynchronously).  The sums are the same either way, bit
+   for bit. */
 extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, size_t nx,
                                 const double *x, size_t ny, const double *y, const double *pi,
                                 double *sums, int precision)
@@ -1207,6 +1226,26 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
   if (!st.stream) CUDA_OK(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking));
   if (!st.copy_stream) CUDA_OK(cudaStreamCreateWithFlags(&st.copy_stream, cudaStreamNonBlocking));
   const size_t per_x = ny * 384;
+  if (per_x / 384 != ny || (nx * per_x) / per_x != nx || nx * per_x > SIZE_MAX / sizeof(double))
+    return fail("Pi of %zu x %zu x 384 doubles does not fit the address space", nx, ny);
+  const void *pi_dev = host_pi_copy_forced()
+                           ? nullptr
+                           : pinned_device_range(pi, nx * per_x * sizeof(double));
+  if (pi_dev) {
+    double *io = st.d_io.get(nx * 5 + ny * 4);
+    if (!io) return fail("out of device memory for %zu x %zu pairs", nx, ny);
+    double *dx = io, *dy = io + nx * 4, *ds = dy + ny * 4;
+    cudaStream_t s = st.stream;
+    CUDA_OK(cudaMemcpyAsync(dx, x, nx * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(dy, y, ny * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
+    LatticeRun R;
+    if (lattice_prepare(c, variant, nx, dx, ny, dy, s, st, R, precision)) return 1;
+    if (lattice_launch(R, 0, nx, static_cast<const double *>(pi_dev), s)) return 1;
+    CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, ds, s));
+    CUDA_OK(cudaMemcpyAsync(sums, ds, nx * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaStreamSynchronize(s));
+    return 0;
+  }
   /* chunk of about 128 M doubles (1 GB) of Pi, at least one x */
   size_t nxc = std::max((size_t)1, ((size_t)128 << 20) / std::max(per_x, (size_t)1));
   nxc = std::min(nxc, nx);
@@ -1252,22 +1291,57 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
    at the full host link rate (about 211 GB/s on the GB300 machines, Grace's
    NVLink-C2C), which memory pinned by other allocators did not always
    reach. */
+/* The library's page-locked allocations: host address -> (bytes, device
+   address), so that the host entry points can tell whether a caller's
+   buffer lies wholly inside one of them. */
+static std::mutex g_pinned_mu;
+static std::map<uintptr_t, std::pair<size_t, uintptr_t>> g_pinned;
+
 extern "C" int kqed_pinned_alloc(size_t bytes, void **ptr)
 {
   if (!ptr) return fail("null buffer");
   *ptr = nullptr;
   if (bytes == 0) return 0;
-  if (cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) != cudaSuccess) {
+  if (cudaHostAlloc(ptr, bytes, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
     *ptr = nullptr;
     return fail("cudaHostAlloc of %zu bytes failed", bytes);
   }
+  void *dev = nullptr;
+  if (cudaHostGetDevicePointer(&dev, *ptr, 0) != cudaSuccess) dev = nullptr;
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  g_pinned[(uintptr_t)*ptr] = {bytes, (uintptr_t)dev};
   return 0;
 }
 
 extern "C" int kqed_pinned_free(void *ptr)
 {
-  if (ptr && cudaFreeHost(ptr) != cudaSuccess) return fail("cudaFreeHost failed");
+  if (!ptr) return 0;
+  {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    g_pinned.erase((uintptr_t)ptr);
+  }
+  if (cudaFreeHost(ptr) != cudaSuccess) return fail("cudaFreeHost failed");
   return 0;
+}
+
+static const void *pinned_device_range(const void *p, size_t bytes)
+{
+  if (!p || bytes == 0) return nullptr;
+  const uintptr_t a = (uintptr_t)p;
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  auto it = g_pinned.upper_bound(a);
+  if (it == g_pinned.begin()) return nullptr;
+  --it;
+  const uintptr_t base = it->first;
+  const size_t size = it->second.first;
+  const uintptr_t dev = it->second.second;
+  if (!dev || a - base > size || bytes > size - (a - base)) return nullptr;
+  return (const void *)(dev + (a - base));
+}
+
+extern "C" int kqed_pinned_contains(const void *ptr, size_t bytes)
+{
+  return pinned_device_range(ptr, bytes) ? 1 : 0;
 }
 
 /* ---------------------------------------------- multi-GPU sharding */

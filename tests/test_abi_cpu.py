@@ -153,6 +153,17 @@ def test_batch_rejects_uninitialised_tables(lib):
     assert b"not initialised" in lib.kqed_last_error()
 
 
+def test_pinned_contains_rejects_foreign_memory(lib):
+    """the range query answers without a GPU: memory that kqed_pinned_alloc
+    did not hand out is never taken for page-locked, device-mapped memory"""
+    import numpy as np
+    a = np.zeros(64)
+    lib.kqed_pinned_contains.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+    assert lib.kqed_pinned_contains(ctypes.c_void_p(a.ctypes.data), a.nbytes) == 0
+    assert lib.kqed_pinned_contains(None, 8) == 0
+    assert lib.kqed_pinned_contains(ctypes.c_void_p(a.ctypes.data), 0) == 0
+
+
 def test_batch_structs_match_ctypes(tmp_path):
     """struct kqed_lattice_job / kqed_batch_info as the C compiler lays
     them out equal the ctypes mirrors the Python binding passes"""

@@ -1,0 +1,67 @@
+"""The host entry point kqed_lattice_sum with Pi in host memory: read in
+place by the kernels when it lies in kqed_pinned_alloc memory, staged
+through device buffers otherwise (or with KQED_HOST_PI=copy).  The two
+routes must give the same sums bit for bit, in both precision forms."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def temps():
+    from kqed_gb300 import build as B
+    B.build()
+    import kqed_gb300 as K
+    t = K.KernelTemps()
+    yield t
+    t.free()
+
+
+def K():
+    import kqed_gb300
+    return kqed_gb300
+
+
+def _case():
+    from kqed_gb300.workloads import diagonal_x, lattice_sites, pi_synth_numpy
+    xs = diagonal_x(5, 0.1)
+    ys = np.ascontiguousarray(lattice_sites(10, 0.1)[::3])
+    return xs, ys, pi_synth_numpy(xs, ys, seed=91)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pinned_pi_read_in_place_equals_staged_copies(temps, precision, monkeypatch):
+    prec = K().KQED_FP64 if precision == "fp64" else K().KQED_FP32_MIXED
+    xs, ys, pi = _case()
+    staged = K().lattice_sum(temps, 2, xs, ys, pi, precision=prec)   # pageable: copies
+    buf = K().PinnedArray((pi.size + 1000,))
+    try:
+        # a sub-range of the block, not at its start
+        view = buf.array[500:500 + pi.size].reshape(pi.shape)
+        view[...] = pi
+        assert K().pinned_contains(view.ctypes.data, view.nbytes)
+        in_place = K().lattice_sum(temps, 2, xs, ys, view, precision=prec)
+        assert np.array_equal(in_place, staged)
+        monkeypatch.setenv("KQED_HOST_PI", "copy")
+        forced = K().lattice_sum(temps, 2, xs, ys, view, precision=prec)
+        assert np.array_equal(forced, staged)
+    finally:
+        buf.free()
+
+
+def test_pinned_range_check(temps):
+    buf = K().PinnedArray((1024,))
+    try:
+        p = buf.array.ctypes.data
+        assert K().pinned_contains(p, 1024 * 8)
+        assert K().pinned_contains(p + 8, 1023 * 8)
+        assert not K().pinned_contains(p + 8, 1024 * 8)      # one double past the end
+        assert not K().pinned_contains(p, 0)
+    finally:
+        buf.free()
+    assert not K().pinned_contains(p, 8)                     # freed
+    a = np.zeros(16)
+    assert not K().pinned_contains(a.ctypes.data, a.nbytes)  # pageable memory
