@@ -186,7 +186,7 @@ struct ThreadStage {
   cudaStream_t stream = nullptr, copy_stream = nullptr;
   cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double *h_pin = nullptr;   /* 8 + 384 doubles */
-  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32, d_rec, d_sa, d_sb, d_cmp, d_cmp_io;
+  Scratch d_io, d_tmp, d_aux, d_aux2, d_col, d_col32, d_rec, d_rec2, d_sa, d_sb, d_cmp, d_cmp_io;
   ~ThreadStage() { reset(); }
   void reset()
   {
@@ -200,7 +200,7 @@ struct ThreadStage {
     copy_stream = nullptr;
     if (h_pin) cudaFreeHost(h_pin);
     d_io.release(); d_tmp.release(); d_aux.release(); d_aux2.release(); d_col.release(); d_col32.release();
-    d_rec.release(); d_sa.release(); d_sb.release(); d_cmp.release(); d_cmp_io.release();
+    d_rec.release(); d_rec2.release(); d_sa.release(); d_sb.release(); d_cmp.release(); d_cmp_io.release();
     stream = nullptr;
     h_pin = nullptr;
     owner = 0;
@@ -729,13 +729,13 @@ static thread_local int tl_precision = KQED_FP64;
 /* record scratch for n pairs (capped at kRecPairs; launches are chunked):
    records [cap][kRec], Pi envelopes [cap], the mixed form's deferred-record
    list [cap] + its count, codes [cap] bytes */
-static int rec_scratch(ThreadStage &st, size_t n, double **rec, uint8_t **code, size_t *cap,
-                       double **env = nullptr, uint32_t **list = nullptr,
-                       unsigned **count = nullptr)
+static int rec_scratch_in(Scratch &buf, size_t n, double **rec, uint8_t **code, size_t *cap,
+                          double **env = nullptr, uint32_t **list = nullptr,
+                          unsigned **count = nullptr)
 {
   size_t c = std::min(std::max(n, (size_t)kTile), kRecPairs);
   c = (c + kTile - 1) / kTile * kTile;
-  double *b = st.d_rec.get(c * kRec + c + c / 2 + 1 + c / 8 + 1);
+  double *b = buf.get(c * kRec + c + c / 2 + 1 + c / 8 + 1);
   if (!b) return fail("out of device memory for %zu pair records", c);
   *rec = b;
   if (env) *env = b + c * kRec;
@@ -744,6 +744,13 @@ static int rec_scratch(ThreadStage &st, size_t n, double **rec, uint8_t **code, 
   *code = reinterpret_cast<uint8_t *>(b + c * kRec + c + c / 2 + 1);
   *cap = c;
   return 0;
+}
+
+static int rec_scratch(ThreadStage &st, size_t n, double **rec, uint8_t **code, size_t *cap,
+                       double **env = nullptr, uint32_t **list = nullptr,
+                       unsigned **count = nullptr)
+{
+  return rec_scratch_in(st.d_rec, n, rec, code, cap, env, list, count);
 }
 
 /* explicit record space (batch plans own theirs) */
@@ -1016,6 +1023,7 @@ struct LatticeRun {
   uint64_t pi_seed;       /* generated Pi (lattice_launch with d_pi == NULL) */
   uint32_t pi_stream;
   size_t x_offset, y_offset;   /* generated Pi: global indices of x[0], y[0] */
+  int asm_blocks;              /* > 0: the assembly kernels' grid (else the tuned one) */
 };
 
 static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, size_t ny,
@@ -1027,6 +1035,7 @@ static int lattice_prepare(Ctx *c, int variant, size_t nx, const double *d_x, si
   R.pi_seed = 0;
   R.pi_stream = 0;
   R.x_offset = R.y_offset = 0;
+  R.asm_blocks = 0;
   R.Ky2 = R.Bx2 = nullptr;
   R.col32 = nullptr;
   R.coldf = nullptr;
@@ -1109,16 +1118,18 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
   a.k0 = R.x_offset + x0;
   a.n0 = R.y_offset;
   a.zero_x_vanishes = R.variant >= 2;
+  LaunchCfg cfg = R.c->cfg;
+  if (R.asm_blocks > 0) cfg.blocks = R.asm_blocks;
   TimedLaunch tl;
   prof_begin(s, tl);
   if (sur) {
     SurHook hook;
     if (surrogate_hook(R.c, R.rec_cap, &hook)) return 1;
-    CUDA_OK(launch_lattice_surrogate(R.c->T, R.c->M, a, R.c->cfg, hook, s));
+    CUDA_OK(launch_lattice_surrogate(R.c->T, R.c->M, a, cfg, hook, s));
   } else if (mixed) {
-    CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, R.c->cfg, s));
+    CUDA_OK(launch_lattice_mixed(R.c->T, R.c->M, a, cfg, s));
   } else {
-    CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, R.c->cfg, s));
+    CUDA_OK(launch_lattice_fp64(R.c->T, R.c->M, a, cfg, s));
   }
   prof_end(s, tl);
   return 0;
@@ -1240,7 +1251,40 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
     CUDA_OK(cudaMemcpyAsync(dy, y, ny * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
     LatticeRun R;
     if (lattice_prepare(c, variant, nx, dx, ny, dy, s, st, R, precision)) return 1;
-    if (lattice_launch(R, 0, nx, static_cast<const double *>(pi_dev), s)) return 1;
+    /* Only the assembly reads Pi.  Two record buffers and two streams: the
+       records of one chunk of x are built while the assembly of the previous
+       chunk reads its Pi, so the host link stays busy; the assembly grid is
+       capped at 4 blocks per SM, which leaves room on every SM for record
+       blocks (24^4 lattice, 32 x: FP64 213 ms per call with one stream,
+       206 / 199 / 198 ms at 3 / 4 / 5 blocks; mixed 173, 164 / 160 / 164). */
+    /* (the surrogate form's network scratch is per context: one stream) */
+    const bool two = precision != KQED_SURROGATE;
+    LatticeRun R2 = R;
+    if (two && rec_scratch_in(st.d_rec2, nx * (size_t)R.tiles * kTile, &R2.rec, &R2.code,
+                              &R2.rec_cap, &R2.env, &R2.list, &R2.count))
+      return 1;
+    const size_t per_x_pairs = (size_t)R.tiles * kTile;
+    const size_t xc = two ? std::max((size_t)1, std::min(R.rec_cap, R2.rec_cap) / per_x_pairs) : nx;
+    int dev = 0, sms = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (xc < nx) R.asm_blocks = R2.asm_blocks = 4 * std::max(sms, 1);
+    if (!st.ev_copied[0]) {
+      for (int i = 0; i < 2; i++) {
+        CUDA_OK(cudaEventCreateWithFlags(&st.ev_copied[i], cudaEventDisableTiming));
+        CUDA_OK(cudaEventCreateWithFlags(&st.ev_free[i], cudaEventDisableTiming));
+      }
+    }
+    cudaStream_t s2 = st.copy_stream;
+    CUDA_OK(cudaEventRecord(st.ev_copied[0], s));
+    CUDA_OK(cudaStreamWaitEvent(s2, st.ev_copied[0], 0));
+    size_t i = 0;
+    for (size_t x0 = 0; x0 < nx; x0 += xc, i++)
+      if (lattice_launch((i & 1) ? R2 : R, x0, std::min(xc, nx - x0),
+                         static_cast<const double *>(pi_dev), (i & 1) ? s2 : s))
+        return 1;
+    CUDA_OK(cudaEventRecord(st.ev_free[0], s2));
+    CUDA_OK(cudaStreamWaitEvent(s, st.ev_free[0], 0));
     CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, ds, s));
     CUDA_OK(cudaMemcpyAsync(sums, ds, nx * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_OK(cudaStreamSynchronize(s));
