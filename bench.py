@@ -417,6 +417,7 @@ def run_gb300(args):
                "precision": args.precision,
                "h2d_link_gbs_measured": h2d_gbs,
                "ms_per_step": e2e_s * 1e3,
+               # summed over the lattice launches of both streams, which overlap
                "kernel_ms_per_step": e2e_kern_ms / args.e2e_steps,
                "copy_ms_per_step": e2e_copy_ms / args.e2e_steps,
                "h2d_gbs_during_step": pi_host.numel() * 8 / (e2e_copy_ms / args.e2e_steps / 1e3) / 1e9
