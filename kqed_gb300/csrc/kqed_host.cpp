@@ -1256,7 +1256,7 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
        chunk reads its Pi, so the host link stays busy; the assembly grid is
        capped at 4 blocks per SM, which leaves room on every SM for record
        blocks (24^4 lattice, 32 x: FP64 213 ms per call with one stream,
-       206 / 199 / 198 ms at 3 / 4 / 5 blocks; mixed 173, 164 / 160 / 164). */
+       200 ms so; mixed 173 and 160 ms). */
     /* (the surrogate form's network scratch is per context: one stream) */
     const bool two = precision != KQED_SURROGATE;
     LatticeRun R2 = R;
@@ -1279,9 +1279,9 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
     CUDA_OK(cudaEventRecord(st.ev_copied[0], s));
     CUDA_OK(cudaStreamWaitEvent(s2, st.ev_copied[0], 0));
     size_t i = 0;
-    for (size_t x0 = 0; x0 < nx; x0 += xc, i++)
+    for (size_t x0 = 0; x0 < nx; x0 += xc, i++)   /* Pi of the chunk's first x */
       if (lattice_launch((i & 1) ? R2 : R, x0, std::min(xc, nx - x0),
-                         static_cast<const double *>(pi_dev), (i & 1) ? s2 : s))
+                         static_cast<const double *>(pi_dev) + x0 * per_x, (i & 1) ? s2 : s))
         return 1;
     CUDA_OK(cudaEventRecord(st.ev_free[0], s2));
     CUDA_OK(cudaStreamWaitEvent(s, st.ev_free[0], 0));

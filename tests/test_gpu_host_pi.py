@@ -65,3 +65,33 @@ def test_pinned_range_check(temps):
     assert not K().pinned_contains(p, 8)                     # freed
     a = np.zeros(16)
     assert not K().pinned_contains(a.ctypes.data, a.nbytes)  # pageable memory
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_in_place_pipeline_over_several_record_passes(temps, precision):
+    """60 x against 20,000 sites: more pairs than one record pass holds, so
+    the in-place route alternates x chunks between its two streams and
+    record buffers; the sums equal the device path's bit for bit"""
+    import torch
+    from kqed_gb300.workloads import diagonal_x, lattice_sites, pi_synth_torch
+    prec = K().KQED_FP64 if precision == "fp64" else K().KQED_FP32_MIXED
+    xs = diagonal_x(60, 0.1)
+    ys = np.ascontiguousarray(lattice_sites(24, 0.1)[::16][:20000])
+    pi = pi_synth_torch(xs, ys, seed=93)                     # 3.7 GB on the device
+    dx = torch.as_tensor(xs, device="cuda")
+    dy = torch.as_tensor(ys, device="cuda")
+    dev = torch.empty(len(xs), dtype=torch.float64, device="cuda")
+    K().lattice_sum_dev(temps, 2, dx.data_ptr(), len(xs), dy.data_ptr(), len(ys), pi.data_ptr(),
+                        dev.data_ptr(), prec, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    ref = dev.cpu().numpy()
+    buf = K().PinnedArray(tuple(pi.shape))
+    try:
+        torch.from_numpy(buf.array).copy_(pi)
+        del pi
+        torch.cuda.empty_cache()
+        assert K().pinned_contains(buf.array.ctypes.data, buf.array.nbytes)
+        got = K().lattice_sum(temps, 2, xs, ys, buf.array, precision=prec)
+        assert np.array_equal(got, ref)
+    finally:
+        buf.free()
