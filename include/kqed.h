@@ -212,7 +212,9 @@ enum kqed_status_bits {
 };
 
 /* kerv[i][384] = QED_kernel_L<variant>(x[i], y[i]) for i < n, host buffers
-   (x, y: n*4 doubles; kerv: n*384 doubles; status: n bytes or NULL). */
+   (x, y: n*4 doubles; kerv: n*384 doubles; status: n bytes or NULL).  A
+   kerv lying wholly inside one allocation of kqed_pinned_alloc is written
+   in place by the kernels (no device copy); the values are the same. */
 int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, size_t n, const double *x,
                       const double *y, double *kerv, uint8_t *status, int precision);
 
@@ -259,7 +261,8 @@ size_t kqed_composite_size(int which);
    i < n.  M: host pointer to the masses (4 doubles; 1 for
    KQED_MKERNEL_L2), NULL for the forms without masses.  precision:
    KQED_FP64 or KQED_FP32_MIXED (the form of the L0 evaluations; the
-   combinations are FP64).  Host buffers. */
+   combinations are FP64).  Host buffers; an out lying wholly inside one
+   allocation of kqed_pinned_alloc is written in place by the kernels. */
 int kqed_composite_batch(const struct QED_kernel_temps *t, int which, const double *M, size_t n,
                          const double *x, const double *y, double *out, int precision);
 

@@ -318,13 +318,24 @@ def QED_kernel_L3(x, y, t):
     return _legacy(3, x, y, t)
 
 
-def kernel_batch(t, variant, x, y, precision=KQED_FP64, with_status=False):
-    """L<variant>(x[i], y[i]) for all i: returns [n][384] (and [n] status bytes)."""
+def _out_array(out, shape):
+    """the caller's output array (e.g. a PinnedArray's, which the kernels then
+    write in place), checked, or a new one"""
+    if out is None:
+        return np.empty(shape)
+    if out.shape != shape or out.dtype != np.float64 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous float64 array of shape %s" % (shape,))
+    return out
+
+
+def kernel_batch(t, variant, x, y, precision=KQED_FP64, with_status=False, out=None):
+    """L<variant>(x[i], y[i]) for all i: returns [n][384] (and [n] status bytes),
+    in `out` if given."""
     x, y = _pairs(x), _pairs(y)
     if x.shape != y.shape:
         raise ValueError("x and y must have the same number of pairs")
     n = x.shape[0]
-    out = np.empty((n, 384))
+    out = _out_array(out, (n, 384))
     st = np.zeros(n, dtype=np.uint8) if with_status else None
     stp = st.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)) if with_status else None
     _check(lib().kqed_kernel_batch(t.ptr, variant, n, _dptr(x), _dptr(y), _dptr(out), stp,
@@ -350,15 +361,16 @@ def _masses(M):
     return np.ascontiguousarray(np.atleast_1d(M), dtype=np.float64)
 
 
-def composite_batch(t, which, x, y, M=None, precision=KQED_FP64):
+def composite_batch(t, which, x, y, M=None, precision=KQED_FP64, out=None):
     """Composite kernel `which` (enum kqed_composite) at every pair: returns
-    [n][composite_size(which)] in the reference's struct layout.  M: the four
-    masses of the M-subtracted forms (one for QED_Mkernel_L2)."""
+    [n][composite_size(which)] in the reference's struct layout, in `out` if
+    given.  M: the four masses of the M-subtracted forms (one for
+    QED_Mkernel_L2)."""
     x, y = _pairs(x), _pairs(y)
     if x.shape != y.shape:
         raise ValueError("x and y must have the same number of pairs")
     n = x.shape[0]
-    out = np.empty((n, composite_size(which)))
+    out = _out_array(out, (n, composite_size(which)))
     Mv = _masses(M)
     _check(lib().kqed_composite_batch(t.ptr, which, None if Mv is None else _dptr(Mv), n,
                                       _dptr(x), _dptr(y), _dptr(out), precision))

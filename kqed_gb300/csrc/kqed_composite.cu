@@ -587,8 +587,22 @@ int composite_host(const struct QED_kernel_temps *t, int which, const double *M,
   if (!x || !y || !out) return set_error("null buffer");
   cudaStream_t s = stage_stream(t);
   if (!s) return set_error("tables not initialised");
-  const size_t chunk = std::min(n, kChunk);
   const size_t osz = kqed_composite_size(which);
+  if (n > SIZE_MAX / (sizeof(double) * (osz + 8))) return set_error("too many pairs");
+  /* an output in kqed_pinned_alloc memory is written in place by the
+     combine kernel; then one pass over all pairs, one synchronisation */
+  if (double *oin = static_cast<double *>(pinned_device(out, n * osz * sizeof(double)))) {
+    double *io = stage_scratch(t, 1, 8 * n);
+    if (!io) return set_error("out of device memory for composite kernel staging");
+    if (cudaMemcpyAsync(io, x, n * 4 * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(io + 4 * n, y, n * 4 * sizeof(double), cudaMemcpyHostToDevice, s) !=
+            cudaSuccess)
+      return set_error("composite kernels: copy to the device failed");
+    if (composite_dev(t, which, M, n, io, io + 4 * n, oin, precision, s)) return 1;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return set_error("composite kernels: execution failed");
+    return 0;
+  }
+  const size_t chunk = std::min(n, kChunk);
   double *io = stage_scratch(t, 1, chunk * (8 + osz));
   if (!io) return set_error("out of device memory for composite kernel staging");
   double *dx = io, *dy = io + 4 * chunk, *dk = io + 8 * chunk;

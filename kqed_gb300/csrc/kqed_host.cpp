@@ -886,19 +886,25 @@ extern "C" int kqed_kernel_batch(const struct QED_kernel_temps *t, int variant, 
   if (check_variant_precision(variant, precision)) return 1;
   if (n == 0) return 0;
   if (!x || !y || !kerv) return fail("null buffer");
+  if (n > SIZE_MAX / (sizeof(double) * (8 + 384 + 1))) return fail("%zu pairs do not fit the address space", n);
   ThreadStage &st = stage_for(c);
   if (!st.stream) CUDA_OK(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking));
-  double *io = st.d_io.get(n * (8 + 384) + (n + 7) / 8);
+  /* an output in kqed_pinned_alloc memory is written in place by the kernels
+     (no device copy, no copy back) */
+  double *kin = static_cast<double *>(kqed::pinned_device(kerv, n * 384 * sizeof(double)));
+  const size_t nk = kin ? 0 : n * 384;
+  double *io = st.d_io.get(n * 8 + nk + (n + 7) / 8);
   if (!io) return fail("out of device memory for %zu pairs", n);
-  double *dx = io, *dy = io + 4 * n, *dk = io + 8 * n;
-  uint8_t *dst = status ? reinterpret_cast<uint8_t *>(io + n * (8 + 384)) : nullptr;
+  double *dx = io, *dy = io + 4 * n, *dk = kin ? kin : io + 8 * n;
+  uint8_t *dst = status ? reinterpret_cast<uint8_t *>(io + n * 8 + nk) : nullptr;
   CUDA_OK(cudaMemcpyAsync(dx, x, n * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
   CUDA_OK(cudaMemcpyAsync(dy, y, n * 4 * sizeof(double), cudaMemcpyHostToDevice, st.stream));
   tl_precision = precision;
   const int rc = run_variant(c, variant, dx, dy, n, dk, dst, st.stream, st);
   tl_precision = KQED_FP64;
   if (rc) return 1;
-  CUDA_OK(cudaMemcpyAsync(kerv, dk, n * 384 * sizeof(double), cudaMemcpyDeviceToHost, st.stream));
+  if (!kin)
+    CUDA_OK(cudaMemcpyAsync(kerv, dk, n * 384 * sizeof(double), cudaMemcpyDeviceToHost, st.stream));
   if (status) CUDA_OK(cudaMemcpyAsync(status, dst, n, cudaMemcpyDeviceToHost, st.stream));
   CUDA_OK(cudaStreamSynchronize(st.stream));
   return 0;
@@ -1473,6 +1479,11 @@ cudaStream_t stage_stream(const struct QED_kernel_temps *t)
   ThreadStage &st = stage_for(c);
   if (!st.stream) cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking);
   return st.stream;
+}
+
+void *pinned_device(const void *p, size_t bytes)
+{
+  return const_cast<void *>(pinned_device_range(p, bytes));
 }
 
 } // namespace kqed

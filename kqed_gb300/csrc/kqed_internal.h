@@ -229,6 +229,10 @@ int l0_pairs(const struct QED_kernel_temps *t, const double *dx, const double *d
 double *stage_scratch(const struct QED_kernel_temps *t, int slot, size_t n);
 /* the calling thread's staging stream for this context */
 cudaStream_t stage_stream(const struct QED_kernel_temps *t);
+/* the device address of [p, p + bytes) when the range lies wholly inside
+   one allocation of kqed_pinned_alloc (page-locked, device-mapped), which
+   kernels may then read or write in place; NULL otherwise */
+void *pinned_device(const void *p, size_t bytes);
 
 } // namespace kqed
 

@@ -1,7 +1,8 @@
-"""The host entry point kqed_lattice_sum with Pi in host memory: read in
-place by the kernels when it lies in kqed_pinned_alloc memory, staged
-through device buffers otherwise (or with KQED_HOST_PI=copy).  The two
-routes must give the same sums bit for bit, in both precision forms."""
+"""Host buffers in kqed_pinned_alloc memory, which the kernels use in place:
+kqed_lattice_sum's Pi (read over the host link; other memory, or
+KQED_HOST_PI=copy, is staged through device buffers) and the outputs of
+kqed_kernel_batch and kqed_composite_batch (written in place).  Each route
+must give the same results bit for bit, in both precision forms."""
 import os
 
 import numpy as np
@@ -92,6 +93,47 @@ def test_in_place_pipeline_over_several_record_passes(temps, precision):
         torch.cuda.empty_cache()
         assert K().pinned_contains(buf.array.ctypes.data, buf.array.nbytes)
         got = K().lattice_sum(temps, 2, xs, ys, buf.array, precision=prec)
+        assert np.array_equal(got, ref)
+    finally:
+        buf.free()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_pair_batch_output_in_place(temps, variant, precision):
+    """kqed_kernel_batch writes an output in kqed_pinned_alloc memory in
+    place: the same values and status bytes as through a device buffer"""
+    from kqed_gb300.workloads import config1_pairs
+    prec = K().KQED_FP64 if precision == "fp64" else K().KQED_FP32_MIXED
+    x, y = config1_pairs()
+    x = np.vstack([x, np.zeros((1, 4)), y[:1]])     # x = 0 and x = y rows
+    y = np.vstack([y, y[:1], y[:1]])
+    ref, st_ref = K().kernel_batch(temps, variant, x, y, precision=prec, with_status=True)
+    buf = K().PinnedArray((len(x), 384))
+    try:
+        got, st = K().kernel_batch(temps, variant, x, y, precision=prec, with_status=True,
+                                   out=buf.array)
+        assert got is buf.array
+        assert np.array_equal(got, ref) and np.array_equal(st, st_ref)
+    finally:
+        buf.free()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("which", [0, 5])
+def test_composite_output_in_place(temps, which, precision):
+    """kqed_composite_batch writes an output in kqed_pinned_alloc memory in
+    place (one pass over all pairs): the same values as through staging"""
+    prec = K().KQED_FP64 if precision == "fp64" else K().KQED_FP32_MIXED
+    rng = np.random.default_rng(which + 5)
+    n = 40000                                        # more than one launch group
+    x = rng.uniform(-2, 2, (n, 4))
+    y = rng.uniform(-2, 2, (n, 4))
+    M = [0.0, 0.5, 1.0, 1.5]
+    ref = K().composite_batch(temps, which, x, y, M=M, precision=prec)
+    buf = K().PinnedArray(ref.shape)
+    try:
+        got = K().composite_batch(temps, which, x, y, M=M, precision=prec, out=buf.array)
         assert np.array_equal(got, ref)
     finally:
         buf.free()
