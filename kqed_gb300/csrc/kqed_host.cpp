@@ -1219,7 +1219,7 @@ static bool host_pi_copy_forced()
 /* Host buffers.  Pi in memory from kqed_pinned_alloc is read in place by the
    kernels over the host link (Grace's NVLink-C2C carries the GPU's loads of
    page-locked host memory; no staging copies, and no copy-engine warm-up:
-   on the GB300 machines a 32.6 GB Pi ran at 213 ms per FP64 step in place
+   on the GB300 machines a 32.6 GB Pi ran at 200 ms per FP64 step in place
    against 240-280 ms staged).  Other host memory streams to the device in
    per-x chunks through a double buffer on a copy stream, so the transfer of
    chunk i+1 overlaps the fused kernel on chunk i (with pinned host memory
@@ -1386,6 +1386,19 @@ static const void *pinned_device_range(const void *p, size_t bytes)
   const size_t size = it->second.first;
   const uintptr_t dev = it->second.second;
   if (!dev || a - base > size || bytes > size - (a - base)) return nullptr;
+  /* the driver must still see both ends as page-locked memory mapped where
+     the registry says (a block released by cudaFreeHost instead of
+     kqed_pinned_free leaves a stale entry; such memory is staged instead) */
+  const uintptr_t ends[2] = {a, a + bytes - 1};
+  for (uintptr_t e : ends) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, (const void *)e) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (pa.type != cudaMemoryTypeHost || (uintptr_t)pa.devicePointer != dev + (e - base))
+      return nullptr;
+  }
   return (const void *)(dev + (a - base));
 }
 
