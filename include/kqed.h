@@ -296,7 +296,12 @@ int kqed_pihat_lattice_dev(size_t nx, const double *d_x, size_t ny, const double
 int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, size_t nx, const double *x,
                      size_t ny, const double *y, const double *pi, double *sums, int precision);
 
-/* Same with device pointers on `stream`; d_sums must hold nx doubles. */
+/* Same with device pointers on `stream`; d_sums must hold nx doubles.  The
+   library's device scratch for these calls is per host thread (the mixed
+   form also runs part of the work on a stream of that thread, joined back
+   to `stream` by events): calls from one thread on different streams must
+   not overlap on the device (order the streams, e.g. with an event); calls
+   from different threads are independent. */
 int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t nx,
                          const double *d_x, size_t ny, const double *d_y, const double *d_pi,
                          double *d_sums, int precision, void *stream);

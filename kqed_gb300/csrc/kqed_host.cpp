@@ -1141,6 +1141,48 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
   return 0;
 }
 
+/* Two record buffers and two streams over chunks of x (one record pass
+   each): the records of one chunk are built while the assembly of the
+   previous chunk runs; blocks_per_sm > 0 caps the assembly grid so that
+   record blocks fit beside it.  pi: the Pi of x[0] (chunk x0 reads
+   pi + x0 * per_x).  Work enqueued on s after the call follows all of it.
+   (The surrogate form's network scratch is per context: one stream.) */
+static int lattice_pipeline(ThreadStage &st, LatticeRun &R, size_t nx, const double *pi,
+                            size_t per_x, int precision, cudaStream_t s, int blocks_per_sm)
+{
+  if (!st.copy_stream) CUDA_OK(cudaStreamCreateWithFlags(&st.copy_stream, cudaStreamNonBlocking));
+  const bool two = precision != KQED_SURROGATE;
+  LatticeRun R2 = R;
+  if (two && rec_scratch_in(st.d_rec2, nx * (size_t)R.tiles * kTile, &R2.rec, &R2.code,
+                            &R2.rec_cap, &R2.env, &R2.list, &R2.count))
+    return 1;
+  const size_t per_x_pairs = (size_t)R.tiles * kTile;
+  const size_t xc = two ? std::max((size_t)1, std::min(R.rec_cap, R2.rec_cap) / per_x_pairs) : nx;
+  if (xc < nx && blocks_per_sm > 0) {
+    int dev = 0, sms = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    R.asm_blocks = R2.asm_blocks = blocks_per_sm * std::max(sms, 1);
+  }
+  if (!st.ev_copied[0]) {
+    for (int i = 0; i < 2; i++) {
+      CUDA_OK(cudaEventCreateWithFlags(&st.ev_copied[i], cudaEventDisableTiming));
+      CUDA_OK(cudaEventCreateWithFlags(&st.ev_free[i], cudaEventDisableTiming));
+    }
+  }
+  cudaStream_t s2 = st.copy_stream;
+  CUDA_OK(cudaEventRecord(st.ev_copied[0], s));
+  CUDA_OK(cudaStreamWaitEvent(s2, st.ev_copied[0], 0));
+  size_t i = 0;
+  for (size_t x0 = 0; x0 < nx; x0 += xc, i++)
+    if (lattice_launch((i & 1) ? R2 : R, x0, std::min(xc, nx - x0), pi + x0 * per_x,
+                       (i & 1) ? s2 : s))
+      return 1;
+  CUDA_OK(cudaEventRecord(st.ev_free[0], s2));
+  CUDA_OK(cudaStreamWaitEvent(s, st.ev_free[0], 0));
+  return 0;
+}
+
 extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int variant, size_t nx,
                                     const double *d_x, size_t ny, const double *d_y,
                                     const double *d_pi, double *d_sums, int precision, void *stream)
@@ -1159,7 +1201,14 @@ extern "C" int kqed_lattice_sum_dev(const struct QED_kernel_temps *t, int varian
   ThreadStage &st = stage_for(c);
   LatticeRun R;
   if (lattice_prepare(c, variant, nx, d_x, ny, d_y, s, st, R, precision)) return 1;
-  if (lattice_launch(R, 0, nx, d_pi, s)) return 1;
+  /* the mixed form overlaps one chunk's records with the previous chunk's
+     assembly (24^4 lattice, 32 x: 44.2 -> 42.4 ms per call); in the FP64
+     form the overlap was slower (137.3 ms in sequence, 140.9 overlapped) */
+  if (precision == KQED_FP32_MIXED) {
+    if (lattice_pipeline(st, R, nx, d_pi, ny * 384, precision, s, 0)) return 1;
+  } else if (lattice_launch(R, 0, nx, d_pi, s)) {
+    return 1;
+  }
   CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, d_sums, s));
   return 0;
 }
@@ -1257,40 +1306,14 @@ extern "C" int kqed_lattice_sum(const struct QED_kernel_temps *t, int variant, s
     CUDA_OK(cudaMemcpyAsync(dy, y, ny * 4 * sizeof(double), cudaMemcpyHostToDevice, s));
     LatticeRun R;
     if (lattice_prepare(c, variant, nx, dx, ny, dy, s, st, R, precision)) return 1;
-    /* Only the assembly reads Pi.  Two record buffers and two streams: the
-       records of one chunk of x are built while the assembly of the previous
-       chunk reads its Pi, so the host link stays busy; the assembly grid is
-       capped at 4 blocks per SM, which leaves room on every SM for record
-       blocks (24^4 lattice, 32 x: FP64 213 ms per call with one stream,
-       200 ms so; mixed 173 and 160 ms). */
-    /* (the surrogate form's network scratch is per context: one stream) */
-    const bool two = precision != KQED_SURROGATE;
-    LatticeRun R2 = R;
-    if (two && rec_scratch_in(st.d_rec2, nx * (size_t)R.tiles * kTile, &R2.rec, &R2.code,
-                              &R2.rec_cap, &R2.env, &R2.list, &R2.count))
+    /* Only the assembly reads Pi: the records of one chunk of x are built
+       on a second stream while the assembly of the previous chunk reads its
+       Pi, so the host link stays busy; the assembly grid is capped at 4
+       blocks per SM, which leaves room on every SM for record blocks (24^4
+       lattice, 32 x: FP64 213 ms per call with one stream, 200 ms so; mixed
+       173 and 160 ms). */
+    if (lattice_pipeline(st, R, nx, static_cast<const double *>(pi_dev), per_x, precision, s, 4))
       return 1;
-    const size_t per_x_pairs = (size_t)R.tiles * kTile;
-    const size_t xc = two ? std::max((size_t)1, std::min(R.rec_cap, R2.rec_cap) / per_x_pairs) : nx;
-    int dev = 0, sms = 0;
-    CUDA_OK(cudaGetDevice(&dev));
-    CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (xc < nx) R.asm_blocks = R2.asm_blocks = 4 * std::max(sms, 1);
-    if (!st.ev_copied[0]) {
-      for (int i = 0; i < 2; i++) {
-        CUDA_OK(cudaEventCreateWithFlags(&st.ev_copied[i], cudaEventDisableTiming));
-        CUDA_OK(cudaEventCreateWithFlags(&st.ev_free[i], cudaEventDisableTiming));
-      }
-    }
-    cudaStream_t s2 = st.copy_stream;
-    CUDA_OK(cudaEventRecord(st.ev_copied[0], s));
-    CUDA_OK(cudaStreamWaitEvent(s2, st.ev_copied[0], 0));
-    size_t i = 0;
-    for (size_t x0 = 0; x0 < nx; x0 += xc, i++)   /* Pi of the chunk's first x */
-      if (lattice_launch((i & 1) ? R2 : R, x0, std::min(xc, nx - x0),
-                         static_cast<const double *>(pi_dev) + x0 * per_x, (i & 1) ? s2 : s))
-        return 1;
-    CUDA_OK(cudaEventRecord(st.ev_free[0], s2));
-    CUDA_OK(cudaStreamWaitEvent(s, st.ev_free[0], 0));
     CUDA_OK(launch_reduce_partials(R.partial, nx, R.tiles, ds, s));
     CUDA_OK(cudaMemcpyAsync(sums, ds, nx * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_OK(cudaStreamSynchronize(s));
