@@ -1150,6 +1150,7 @@ static int lattice_launch(const LatticeRun &R, size_t x0, size_t nxc, const doub
 static int lattice_pipeline(ThreadStage &st, LatticeRun &R, size_t nx, const double *pi,
                             size_t per_x, int precision, cudaStream_t s, int blocks_per_sm)
 {
+  if (!pi) return fail("the chunked lattice sum needs a stored Pi");   /* (generated Pi: lattice_launch) */
   if (!st.copy_stream) CUDA_OK(cudaStreamCreateWithFlags(&st.copy_stream, cudaStreamNonBlocking));
   const bool two = precision != KQED_SURROGATE;
   LatticeRun R2 = R;
