@@ -215,3 +215,17 @@ def test_c_program_links_every_entry_point(lib, tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
     assert int(out[0]) == len(names) and int(out[1]) == 0
+
+
+def test_out_argument_is_checked_before_any_call():
+    """kernel_batch / composite_batch write into a caller's `out` only when it
+    is a C-contiguous float64 array of the result's shape"""
+    import numpy as np
+    import kqed_gb300 as K
+    x = np.zeros((3, 4))
+    for bad in (np.zeros((3, 383)), np.zeros((3, 384), dtype=np.float32),
+                np.zeros((384, 3)).T):
+        with pytest.raises(ValueError):
+            K.kernel_batch(None, 0, x, x, out=bad)
+    with pytest.raises(ValueError):
+        K.composite_batch(None, 0, x, x, out=np.zeros((3, 7)))
